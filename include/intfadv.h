@@ -1,0 +1,172 @@
+/*
+ * libintfadv_gb300 — C-ABI of the GB300 (sm_103a) implementation of
+ * InterfaceAdvection.jl's per-step hot path.
+ *
+ * Every entry point takes plain pointers and sizes.  Field arrays are DEVICE
+ * pointers owned by the caller (Julia CuArrays, torch tensors, cudaMalloc),
+ * laid out exactly as the reference's Julia arrays: column-major (x fastest),
+ * one ghost layer (Ng = N + 2 per dimension), FP64, vector fields SoA with
+ * the component index last (component d starts at d * prod(Ng)).  u[I,d] is
+ * the velocity on the lower d-face of cell I.  Coordinates in this header are
+ * 0-based (Julia index k is k-1).
+ *
+ * The library owns its scratch (ping-pong fraction buffers, interface-cell
+ * lists, multigrid levels, status words) inside the handle.  All work is
+ * ordered on the handle's CUDA stream; calls that report a status read it
+ * back once per call.  Errors are return codes, never traps.
+ *
+ * Each entry point names the reference function it replaces
+ * (file:line within the InterfaceAdvection.jl project).
+ */
+#ifndef INTFADV_H
+#define INTFADV_H
+#include <stdint.h>
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- return codes ------------------------------------------------------- */
+#define IA_OK                     0
+#define IA_ERR_NAN                1   /* error("NaN!"), src/advection.jl:148           */
+#define IA_ERR_DIVERGENCE         2   /* error("divergence ... exploding"), :160,:180  */
+#define IA_ERR_UNSUPPORTED        3   /* udf, BDIM body, exitBC, D not in {2,3}, ...   */
+#define IA_ERR_INVALID            4   /* bad argument / unbound field                  */
+#define IA_ERR_CUDA               5   /* CUDA runtime error                            */
+#define IA_ERR_NO_DEVICE          6
+#define IA_ERR_TOO_LARGE          7
+#define IA_WARN_FILL            100   /* over/under-fill past tol (printed, not fatal)  */
+#define IA_WARN_NOT_CONVERGED   101   /* Poisson stopped at itmx                        */
+
+/* status flag bits */
+#define IA_FLAG_NAN        1u
+#define IA_FLAG_OVERFILL   2u
+#define IA_FLAG_UNDERFILL  4u
+#define IA_FLAG_DIVERGENCE 8u
+#define IA_FLAG_POISSON   16u
+
+/* normalScheme (src/normalEstimation.jl) */
+#define IA_NORMAL_WH      0   /* getInterfaceNormal_WH!  :105-154 (default) */
+#define IA_NORMAL_WY      1   /* getInterfaceNormal_WY!  :35-68             */
+#define IA_NORMAL_MYC     2   /* getInterfaceNormal_MYC! :185-202           */
+#define IA_NORMAL_Y       3   /* getInterfaceNormal_Y!   :232-247           */
+#define IA_NORMAL_COLUMN  4   /* getInterfaceNormal_Column! :75-97          */
+#define IA_NORMAL_PCD     5   /* getInterfaceNormal_PCD! :161-165           */
+#define IA_NORMAL_SLIC    6   /* getInterfaceNormal_SLIC! :172-176          */
+#define IA_NORMAL_CD      7   /* getInterfaceNormal_CD!  :266-277           */
+#define IA_NORMAL_XYLIC   8   /* getInterfaceNormal_XYLIC! :279-283         */
+
+/* momentum-flux limiter λ(u,c,d) (src/flow.jl:5-15) */
+#define IA_LIMITER_KOREN      0
+#define IA_LIMITER_UPWIND     1
+#define IA_LIMITER_MINMOD     2
+#define IA_LIMITER_VANALBADA1 3
+#define IA_LIMITER_SWEBY      4
+#define IA_LIMITER_SUPERBEE   5
+#define IA_LIMITER_TVDCEN     6
+#define IA_LIMITER_TVDDOWN    7
+
+/* Poisson solver modes */
+#define IA_POISSON_FP64    0   /* FP64 V-cycle preconditioned CG                     */
+#define IA_POISSON_MIXED   1   /* FP32 V-cycles inside FP64 defect-correction CG     */
+
+typedef struct ia_handle ia_handle;
+
+/* Construction parameters: TwoPhaseSimulation / cVOF keywords
+ * (src/InterfaceAdvection.jl:67-84, src/cVOF.jl:45-89) plus the WaterLily
+ * Flow settings the step reads (ν, constant g, constant u_BC, perdir). */
+typedef struct {
+    int32_t D;              /* 2 or 3 */
+    int32_t perdir;         /* bit j set <=> dimension j (0-based) periodic */
+    int64_t N[3];           /* interior cells per dimension (N[2] ignored for D=2) */
+    double  lrho;           /* λρ = ρ_light / ρ_dark */
+    double  lmu;            /* λμ = μ_light / μ_dark */
+    double  mu;             /* dark-fluid dynamic viscosity; 0 = off (cVOF stores nothing) */
+    double  eta;            /* surface tension coefficient; 0 = off */
+    double  nu;             /* WaterLily ν (MPCFL advective limit) */
+    double  g[3];           /* constant gravity; has_g = 0 => none */
+    int32_t has_g;
+    int32_t normal_scheme;  /* IA_NORMAL_* */
+    int32_t limiter;        /* IA_LIMITER_* */
+    int32_t poisson_mode;   /* IA_POISSON_* */
+    double  uBC[3];         /* constant boundary velocity (WaterLily u_BC tuple) */
+    double  poisson_tol;    /* L-infinity residual of the dt-scaled pressure system */
+    int32_t poisson_itmx;
+    int32_t exitBC;         /* must be 0: convective exit is not supported */
+} ia_config;
+
+/* Field pointers (device, FP64 unless noted), the reference's Flow and cVOF
+ * members.  Pointers may be NULL for fields a call does not touch. */
+typedef struct {
+    /* WaterLily Flow */
+    double *u, *u0, *force, *sigma, *p, *mu0;
+    /* cVOF (src/cVOF.jl:1-44) */
+    double *f, *f0, *alpha, *nhat, *fF, *rhou, *rhouf, *drho;
+    int8_t *cbar;
+} ia_fields;
+
+/* Per-call status (one read-back per call). */
+typedef struct {
+    int32_t  code;              /* IA_OK, IA_ERR_*, IA_WARN_* (worst seen)        */
+    uint32_t flags;             /* IA_FLAG_* */
+    double   maxf, minf;        /* extreme fractions past tol (valid per flags)   */
+    int64_t  maxid, minid;      /* their linear cell indices                      */
+    int32_t  fill_dir;          /* 0-based sweep direction of the last flag       */
+    int32_t  poisson_iters[2];  /* predictor / corrector solves                   */
+    int32_t  pad;
+    double   poisson_resid[2];  /* final L-infinity residuals (FP64)               */
+    double   dt_next;           /* min(MPCFL, 1.2 dt) after ia_mom_step            */
+} ia_status;
+
+/* Create / destroy a solver handle.  Allocates the library's scratch on the
+ * current device.  Replaces the allocation part of cVOF(N; ...) src/cVOF.jl:45-89
+ * and TwoPhaseSimulation src/InterfaceAdvection.jl:67-84. */
+int ia_create(const ia_config* cfg, ia_handle** out);
+int ia_destroy(ia_handle* h);
+
+/* Order all later work of this handle on `stream` (a cudaStream_t; NULL = legacy default). */
+int ia_set_stream(ia_handle* h, void* stream);
+
+/* Borrow the caller's field arrays (the Flow / cVOF members) for later calls. */
+int ia_bind_fields(ia_handle* h, const ia_fields* fields);
+
+/* advect!(a, c, f, u¹, u², dt) — src/advection.jl:17-23 → advectVOF! :34-78.
+ * Lie–Trotter split VOF advection of `f` (in place) by the average of u1 and u2,
+ * sweeping dimensions in the order dirO[i] = (n_dt + i) mod D, i = 1..D
+ * (n_dt = length(Δt)).  Writes the bound c̄ and, if bound, ρuf. */
+int ia_advect_vof(ia_handle* h, double* f, const double* u1, const double* u2,
+                  double dt, int64_t n_dt, ia_status* status);
+
+/* reconstructInterface!(f, α, n̂, normalScheme) — src/normalEstimation.jl:10-28,
+ * including BCVOF! src/VOFutil.jl:44-55 (f ghosts updated in place). */
+int ia_reconstruct(ia_handle* h, double* f, double* alpha, double* nhat);
+
+/* getVOFFlux!(fᶠ, f, α, n̂, u, u⁰, δt, d, ρuf, λρ) — src/advection.jl:108-137
+ * (fᶠ zeroed first; ρuf[:,d] accumulated when rhouf is not NULL). */
+int ia_vof_flux(ia_handle* h, double* fF, const double* f, const double* alpha,
+                const double* nhat, const double* u, const double* u0, double dt,
+                int32_t d, double* rhouf);
+
+/* applyVOF!(f, α, n̂, SDF) + BCf! — src/VOFutil.jl:9-37, src/cVOF.jl:56.
+ * `sdf` holds 1 + 2D scalar fields: the SDF at cell centres, then at
+ * centre ± 0.01 e_d for d = 0..D-1 (+ first).  Interior cells only. */
+int ia_apply_vof(ia_handle* h, const double* sdf, double* f, double* alpha, double* nhat);
+
+/* Σ f over interior cells (FP64, deterministic tree order): the mass the
+ * reference checks with sum(f[inside(f)]), test/maintests.jl:209,215. */
+int ia_mass(ia_handle* h, const double* f, double* mass_out);
+
+/* Per-launch kernel timing with CUDA events on the handle's stream, for the
+ * roofline figures (no reference counterpart: instrumentation only).
+ * Folds finished records into per-family totals, copies the first n totals
+ * (milliseconds, launch counts; families: 0 VOF bulk sweep, 1 VOF list sweep,
+ * 2 momentum sweep, 3 forcing/update, 4 MG smoother, 5 MG residual,
+ * 6 MG transfer, 7 Krylov vector ops, 8 other), then, if enable >= 0, resets
+ * the totals and switches recording on (1) or off (0). */
+int ia_timing(ia_handle* h, int32_t enable, double* ms_out, int64_t* launches_out, int32_t n);
+
+const char* ia_error_string(int code);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

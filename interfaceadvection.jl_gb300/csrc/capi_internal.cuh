@@ -1,0 +1,60 @@
+// Handle layout and helpers shared by the C-ABI translation units.
+#pragma once
+#include <cuda_runtime.h>
+
+#include "ia_core.cuh"
+#include "vof.cuh"
+
+#include <vector>
+
+// Kernel families timed by the optional per-launch event instrumentation.
+enum TimedKernel { TK_VOF_BULK = 0, TK_VOF_LIST = 1, TK_MOM = 2, TK_FORCE = 3, TK_MG_SMOOTH = 4,
+                   TK_MG_RESID = 5, TK_MG_TRANSFER = 6, TK_KRYLOV = 7, TK_OTHER = 8, TK_COUNT = 16 };
+
+struct Timing {
+    bool on = false;
+    std::vector<cudaEvent_t> pool;     // reusable events
+    std::vector<int> fam;              // family of record k (events 2k, 2k+1)
+    size_t used = 0;
+    double ms[TK_COUNT] = {0};
+    long long launches[TK_COUNT] = {0};
+};
+
+struct MomScratch;    // momentum / projection scratch (momentum.cu)
+struct PoissonMG;     // multigrid hierarchy (poisson.cu)
+
+struct ia_handle {
+    ia_config cfg;
+    ia::Grid g;
+    int device;
+    int list_blocks;
+    cudaStream_t stream;
+    ia_fields fld;
+    // scratch owned by the library
+    double* tmp1 = nullptr;            // ping-pong fraction buffers
+    double* tmp2 = nullptr;
+    unsigned int* list = nullptr;      // compacted interface cells
+    ia::DevStatus* dst = nullptr;      // device status
+    ia::DevStatus* hst = nullptr;      // pinned host mirror
+    double* partial = nullptr;         // reduction partials
+    double* dscalar = nullptr;         // device scalars
+    int8_t* cbar_own = nullptr;        // c̄ when the caller binds none
+    Timing timing;
+    MomScratch* mom = nullptr;
+    PoissonMG* mg = nullptr;
+};
+
+namespace ia {
+int cuda_fail(cudaError_t e);
+int status_reset(ia_handle* h);
+int status_collect(ia_handle* h, const double* u1, const double* u2, ia_status* out, bool merge);
+int advect_sweeps(ia_handle* h, double* f, const double* u1, const double* u2, double dt, const int* dirs,
+                  int nsweeps, int8_t* cbar, double* rhouf, double tol_rep, bool first_writes_cbar,
+                  int counter_base);
+// allocation hooks of the momentum / Poisson modules
+// per-launch timing: begin returns a token (-1 when off); end closes it
+int timing_begin(ia_handle* h, int family);
+void timing_end(ia_handle* h, int token);
+int extra_create(ia_handle* h);
+void extra_destroy(ia_handle* h);
+}  // namespace ia

@@ -1,0 +1,48 @@
+// VOF sweep launcher interface (see vof.cu).
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "ia_core.cuh"
+
+namespace ia {
+
+struct SweepArgs {
+    Grid g;
+    int d;                            // sweep direction (0-based)
+    int scheme;                       // IA_NORMAL_*
+    bool first;                       // first sweep of the call: computes and writes c̄
+    const double* __restrict__ fin;   // fractions before the sweep (ghosts valid)
+    double* __restrict__ fout;        // fractions after the sweep (ghosts written)
+    const double* __restrict__ u1;    // component d of the first velocity field
+    const double* __restrict__ u2;    // component d of the second velocity field
+    int8_t* cbar;                     // c̄: written when first, read otherwise
+    double* rhouf_d;                  // component d of ρuf (written in full), or nullptr
+    double h;                         // δt / 2
+    double dt;                        // δt of the sweep
+    double lrho;                      // λρ
+    double tol_rep;                   // reportFillError tolerance
+    double tol_clean;                 // cleanWisp! tolerance (10 eps)
+    unsigned long long ulim;          // bit pattern of 1/(2δt): fast-path velocity bound
+    unsigned int* list;               // compacted cells for the list pass
+    unsigned int* list_count;
+    DevStatus* st;
+};
+
+cudaError_t vof_sweep_bulk(const SweepArgs& a, cudaStream_t st);
+cudaError_t vof_sweep_list(const SweepArgs& a, cudaStream_t st, int list_blocks);
+
+// applyVOF! interior + BCf! ghosts
+cudaError_t apply_vof(const Grid& g, const double* sdf, double* f, double* alpha, double* nhat, cudaStream_t st);
+// reconstructInterface! + BCVOF!
+cudaError_t reconstruct(const Grid& g, int scheme, double* f, double* alpha, double* nhat, cudaStream_t st);
+// getVOFFlux! with caller-supplied α, n̂
+cudaError_t vof_flux(const Grid& g, double* fF, const double* f, const double* alpha, const double* nhat,
+                     const double* u, const double* u0, double dt, int d, double* rhouf, double lrho,
+                     cudaStream_t st);
+// ghosts of a scalar from their boundary-condition source cells (BCf!)
+cudaError_t fill_ghosts_scalar(const Grid& g, double* f, cudaStream_t st);
+// deterministic Σ over interior cells; partial buffer of >= 4096 doubles
+cudaError_t interior_sum(const Grid& g, const double* f, double* partial, double* out, cudaStream_t st);
+
+}  // namespace ia

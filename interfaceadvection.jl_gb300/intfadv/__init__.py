@@ -1,0 +1,15 @@
+"""intfadv — GB300 (sm_103a) implementation of InterfaceAdvection.jl's per-step hot path.
+
+Host mirror of the reference's Julia API over the C-ABI library
+libintfadv_gb300.so (include/intfadv.h).  All compute runs in hand-written
+CUDA kernels; there is no CPU fallback.
+"""
+from . import _lib
+from ._build import build
+from .core import (Flow, Handle, advect, advect_vof_raw, advectVOF, apply_vof, applyVOF, cVOF, get_vof_flux,
+                   getVOFFlux, make_config, reconstruct_interface, reconstructInterface)
+from .fields import cell_coords, face_coords, ffrom, fones, fzeros, is_fortran
+
+__all__ = ["Flow", "Handle", "advect", "advect_vof_raw", "advectVOF", "apply_vof", "applyVOF", "cVOF",
+           "get_vof_flux", "getVOFFlux", "make_config", "reconstruct_interface", "reconstructInterface", "build",
+           "cell_coords", "face_coords", "ffrom", "fones", "fzeros", "is_fortran"]
