@@ -19,7 +19,7 @@ __global__ void status_reset_k(DevStatus* s) {
     s->min_enc = ~0ull;
     s->max_key = 0ull;
     s->min_key = 0ull;
-    for (int i = 0; i < 8; ++i) s->list_count[i] = 0;
+    for (int i = 0; i < 32; ++i) s->list_count[i] = 0;
 }
 
 }  // namespace
@@ -113,14 +113,21 @@ int advect_sweeps(ia_handle* h, double* f, const double* u1, const double* u2, d
         double lim = (dt > 0.0 && std::isfinite(dt)) ? 0.5 / dt : 0.0;
         std::memcpy(&a.ulim, &lim, 8);
         a.list = h->list;
-        a.list_count = &h->dst->list_count[(counter_base + k) & 7];
+        a.list_count = &h->dst->list_count[(2 * (counter_base + k)) & 31];
+        a.flist = h->flist;
+        a.flist_count = &h->dst->list_count[(2 * (counter_base + k) + 1) & 31];
+        a.flux = h->flux;
         a.st = h->dst;
         int tk = timing_begin(h, TK_VOF_BULK);
         cudaError_t e = vof_sweep_bulk(a, h->stream);
         timing_end(h, tk);
         if (e != cudaSuccess) return IA_ERR_CUDA;
+        tk = timing_begin(h, TK_VOF_FACES);
+        e = vof_sweep_faces(a, h->stream, h->list_blocks);
+        timing_end(h, tk);
+        if (e != cudaSuccess) return IA_ERR_CUDA;
         tk = timing_begin(h, TK_VOF_LIST);
-        e = vof_sweep_list(a, h->stream, h->list_blocks);
+        e = vof_sweep_cells(a, h->stream, h->list_blocks);
         timing_end(h, tk);
         if (e != cudaSuccess) return IA_ERR_CUDA;
         in = out;
@@ -225,6 +232,8 @@ int ia_create(const ia_config* cfg, ia_handle** out) {
     e = e ? e : cudaMalloc(&h->tmp1, nb);
     e = e ? e : cudaMalloc(&h->tmp2, nb);
     e = e ? e : cudaMalloc(&h->list, sizeof(unsigned int) * (size_t)h->g.N);
+    e = e ? e : cudaMalloc(&h->flist, sizeof(unsigned int) * (size_t)h->g.N);
+    e = e ? e : cudaMalloc(&h->flux, nb);
     e = e ? e : cudaMalloc(&h->dst, sizeof(DevStatus));
     e = e ? e : cudaMalloc(&h->partial, sizeof(double) * 4096);
     e = e ? e : cudaMalloc(&h->dscalar, sizeof(double) * 64);
@@ -251,6 +260,8 @@ int ia_destroy(ia_handle* h) {
     cudaFree(h->tmp1);
     cudaFree(h->tmp2);
     cudaFree(h->list);
+    cudaFree(h->flist);
+    cudaFree(h->flux);
     cudaFree(h->dst);
     cudaFree(h->partial);
     cudaFree(h->dscalar);

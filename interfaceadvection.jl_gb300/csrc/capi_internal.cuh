@@ -8,7 +8,7 @@
 #include <vector>
 
 // Kernel families timed by the optional per-launch event instrumentation.
-enum TimedKernel { TK_VOF_BULK = 0, TK_VOF_LIST = 1, TK_MOM = 2, TK_FORCE = 3, TK_MG_SMOOTH = 4,
+enum TimedKernel { TK_VOF_BULK = 0, TK_VOF_LIST = 1, TK_VOF_FACES = 9, TK_MOM = 2, TK_FORCE = 3, TK_MG_SMOOTH = 4,
                    TK_MG_RESID = 5, TK_MG_TRANSFER = 6, TK_KRYLOV = 7, TK_OTHER = 8, TK_COUNT = 16 };
 
 struct Timing {
@@ -33,7 +33,9 @@ struct ia_handle {
     // scratch owned by the library
     double* tmp1 = nullptr;            // ping-pong fraction buffers
     double* tmp2 = nullptr;
-    unsigned int* list = nullptr;      // compacted interface cells
+    unsigned int* list = nullptr;      // compacted cells needing the full update
+    unsigned int* flist = nullptr;     // compacted faces needing reconstruction
+    double* flux = nullptr;            // cached fluxes of listed faces
     ia::DevStatus* dst = nullptr;      // device status
     ia::DevStatus* hst = nullptr;      // pinned host mirror
     double* partial = nullptr;         // reduction partials

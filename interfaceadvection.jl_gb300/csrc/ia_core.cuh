@@ -77,7 +77,7 @@ struct DevStatus {
     unsigned long long min_enc;         // ord_enc of the smallest
     unsigned long long max_key;         // (float bits of over-fill) << 32 | cell
     unsigned long long min_key;         // (float bits of under-fill) << 32 | cell
-    unsigned int list_count[8];         // compaction counters (one per sweep)
+    unsigned int list_count[32];        // compaction counters (two per sweep)
     double scratch[8];                  // reductions (CFL, norms)
 };
 

@@ -3,20 +3,23 @@
 //
 // One sweep along d maps f_in -> f_out (ping-pong buffers: the update of a
 // cell reads f up to two cells away along d, so it cannot run in place).  A
-// sweep is two kernels:
+// sweep is three kernels:
 //
 //  * vof_bulk — one thread per cell of the ghost-inclusive box.  A cell whose
 //    three cells along d are all full or all empty, equal to its c̄, and whose
 //    face velocities satisfy |u|·δt <= 1/2 leaves the sweep unchanged after
 //    cleanWisp!: the face fluxes f·δl and the dilation term cancel to within
-//    ~1e-15 < 10 eps.  Those cells are decided with integer compares only
-//    (FP64 is slow on this part).  Every other cell is appended to a compacted
-//    list.  The kernel also writes the mass flux ρuf[:,d] of faces whose donor
-//    cell is full or empty.
-//  * vof_list — one thread per listed cell (full warps of interface work):
-//    donor-cell reconstruction (normal scheme + PLIC intercept), the PLIC slab
-//    volume of each face, the conservative update with the dilation term, the
-//    fill-error status, cleanWisp! and the ρuf of the cell's lower face.
+//    ~1e-15 < 10 eps.  Those cells are decided with integer compares on the
+//    IEEE bit patterns only: on GB300 every FP64 instruction, compares
+//    included, issues at 1/64 of the FP32 rate, so the bulk path spends FP64
+//    only on the mass flux ρuf.  Cells that need the full update go to a cell
+//    list; faces whose donor cell must be reconstructed go to a face list.
+//  * vof_faces — one thread per listed face: donor reconstruction (normal
+//    scheme + PLIC intercept) and the PLIC slab volume, computed once per face
+//    and cached; the face's mass flux ρuf.
+//  * vof_cells — one thread per listed cell: the conservative update with the
+//    dilation term from the two face fluxes, the fill-error status,
+//    cleanWisp!.
 //
 // Ghost cells are written in the same pass with the value of their
 // boundary-condition source cell, so f_out leaves the sweep with BCf! applied
@@ -31,27 +34,32 @@ namespace ia {
 
 namespace {
 
-__device__ __forceinline__ bool abs_le(double v, unsigned long long lim_bits) {
-    const unsigned long long b = (unsigned long long)__double_as_longlong(v) & 0x7FFFFFFFFFFFFFFFull;
-    return b <= lim_bits;   // false for inf / NaN
+constexpr unsigned long long ONE_BITS = 0x3FF0000000000000ull;   // 1.0
+constexpr unsigned long long ABS_MASK = 0x7FFFFFFFFFFFFFFFull;
+
+__device__ __forceinline__ unsigned long long bits(double v) { return (unsigned long long)__double_as_longlong(v); }
+// |v| <= limit, decided on the bit pattern (false for inf / NaN)
+__device__ __forceinline__ bool abs_le(unsigned long long b, unsigned long long lim_bits) {
+    return (b & ABS_MASK) <= lim_bits;
+}
+// f ∈ {+0, 1} exactly
+__device__ __forceinline__ bool is_bulk(unsigned long long b) { return b == 0ull || b == ONE_BITS; }
+
+__device__ __forceinline__ double mass_flux(double dl, double F, double lrho) {
+    return dl * lrho + (1.0 - lrho) * F;   // fᶠ2ρuf, src/VOFutil.jl:218
 }
 
-// getVOFFlux! for one face K (lower d-face of cell K), src/advection.jl:113-137.
-// Returns the dark-fluid volume fᶠ crossing the face; dl = δt/2 (u1 + u2).
+// getVOFFlux! for one face K whose donor needs reconstruction
+// (src/advection.jl:113-137); dl = δt/2 (u1 + u2) is passed in.
 template <int D>
-__device__ double face_flux(const SweepArgs& a, long long K, int kd, double& dl) {
+__device__ double face_flux_recon(const SweepArgs& a, long long K, int kd, double dl) {
     const long long sd = a.g.s[a.d];
-    dl = a.h * (a.u1[K] + a.u2[K]);
-    if (dl == 0.0) return 0.0;
     const bool pos = dl > 0.0;
     const long long C = pos ? K - sd : K;
     const int cd = pos ? kd - 1 : kd;
     const double fC = a.fin[C];
     const int nd = a.g.n[a.d];
     const bool ghost = (cd == 0) || (cd == nd - 1);
-    // α, n̂ of a zero-gradient ghost are never reconstructed: Σ|n̂| = 0 branch
-    if (ghost && !a.g.isper(a.d)) return fC * dl;
-    if (fC == 0.0 || fC == 1.0) return fC * dl;
     long long R = C;   // periodic ghost donors carry their image's reconstruction (BCVOF!)
     if (ghost) R = (cd == 0) ? C + (long long)(nd - 2) * sd : C - (long long)(nd - 2) * sd;
     Stencil S;
@@ -71,8 +79,32 @@ __device__ double face_flux(const SweepArgs& a, long long K, int kd, double& dl)
     return get_volume_fraction<D>(n, b) * dl;
 }
 
-__device__ __forceinline__ double mass_flux(double dl, double F, double lrho) {
-    return dl * lrho + (1.0 - lrho) * F;   // fᶠ2ρuf, src/VOFutil.jl:218
+// Does face K (d-coordinate kd) need the donor reconstruction?  Returns false
+// and the flux when the donor is full/empty or a zero-gradient ghost (whose
+// α, n̂ the reference never reconstructs: the Σ|n̂| = 0 branch).
+__device__ __forceinline__ bool face_simple(const SweepArgs& a, long long K, int kd, double& dl, double& F) {
+    const long long sd = a.g.s[a.d];
+    dl = a.h * (a.u1[K] + a.u2[K]);
+    const unsigned long long db = bits(dl);
+    if ((db & ABS_MASK) == 0ull) {   // δl == 0: no flux, ρuf untouched
+        F = 0.0;
+        return true;
+    }
+    const bool pos = !(db >> 63);
+    const long long C = pos ? K - sd : K;
+    const int cd = pos ? kd - 1 : kd;
+    const double fC = a.fin[C];
+    const unsigned long long fb = bits(fC);
+    const bool zg_ghost = ((cd == 0) || (cd == a.g.n[a.d] - 1)) && !a.g.isper(a.d);
+    if (is_bulk(fb)) {
+        F = (fb == ONE_BITS) ? dl : 0.0 * dl;
+        return true;
+    }
+    if (zg_ghost || fC == 0.0 || fC == 1.0) {   // -0, or a mixed zero-gradient ghost donor
+        F = fC * dl;
+        return true;
+    }
+    return false;
 }
 
 template <int D>
@@ -111,48 +143,61 @@ __global__ void __launch_bounds__(256) vof_bulk(SweepArgs a) {
     const int z = blockIdx.z;
     const Grid& g = a.g;
     const bool valid = x < g.n[0] && y < g.n[1];
-    bool need = false;
+    bool need_cell = false, need_face = false;
     long long O = 0;
     if (valid) {
         O = lin(g, x, y, z);
         const int c[3] = {x, y, z};
-        const int sc[3] = {bc_src(g, 0, x), bc_src(g, 1, y), D == 3 ? bc_src(g, 2, z) : 0};
-        const long long S = lin(g, sc[0], sc[1], sc[2]);
+        const long long S = lin(g, bc_src(g, 0, x), bc_src(g, 1, y), D == 3 ? bc_src(g, 2, z) : 0);
         const long long sd = g.s[a.d];
-        const double fm = a.fin[S - sd], fc = a.fin[S], fp = a.fin[S + sd];
+        const unsigned long long bm = bits(a.fin[S - sd]), bc = bits(a.fin[S]), bp = bits(a.fin[S + sd]);
         int cb;
         if (FIRST) {
-            a.cbar[O] = (a.fin[O] < 0.5) ? 0 : 1;   // c̄ over every cell, src/advection.jl:40
-            cb = (fc < 0.5) ? 0 : 1;
+            // c̄ = f < 0.5 ? 0 : 1 over every cell (src/advection.jl:40), on the bit pattern
+            const unsigned long long bo = bits(a.fin[O]);
+            const bool lt_half = ((bo & ABS_MASK) <= 0x7FF0000000000000ull) &&            // not NaN
+                                 ((bo >> 63) || bo < 0x3FE0000000000000ull);             // negative or < 0.5
+            a.cbar[O] = lt_half ? 0 : 1;
+            cb = (bc == ONE_BITS) ? 1 : 0;          // only consulted when bc is bulk
         } else {
             cb = a.cbar[S];
         }
-        const double ul = a.u1[S], ur = a.u1[S + sd], vl = a.u2[S], vr = a.u2[S + sd];
-        const bool bulk = (fm == fc) && (fc == fp) && (fc == 0.0 || fc == 1.0) && (cb == (fc == 1.0 ? 1 : 0)) &&
-                          abs_le(ul, a.ulim) && abs_le(ur, a.ulim) && abs_le(vl, a.ulim) && abs_le(vr, a.ulim);
-        need = !bulk;
-        double m = 0.0;
-        if (a.rhouf_d && in_face_range<D>(g, a.d, c)) {
-            const double dl = a.h * (a.u1[O] + a.u2[O]);
-            if (dl != 0.0) {
-                const bool pos = dl > 0.0;
-                const int cd = pos ? c[a.d] - 1 : c[a.d];
-                const double fC = a.fin[pos ? O - sd : O];
-                const bool zg_ghost = (cd == 0 || cd == g.n[a.d] - 1) && !g.isper(a.d);
-                if (zg_ghost || fC == 0.0 || fC == 1.0) m = mass_flux(dl, fC * dl, a.lrho);
-                else need = true;
+        const bool bulk = (bm == bc) && (bc == bp) && is_bulk(bc) && (cb == (bc == ONE_BITS ? 1 : 0)) &&
+                          abs_le(bits(a.u1[S]), a.ulim) && abs_le(bits(a.u1[S + sd]), a.ulim) &&
+                          abs_le(bits(a.u2[S]), a.ulim) && abs_le(bits(a.u2[S + sd]), a.ulim);
+        need_cell = !bulk;
+        if (bulk) a.fout[O] = (bc == ONE_BITS) ? 1.0 : 0.0;
+        if (in_face_range<D>(g, a.d, c)) {
+            double dl, F;
+            if (face_simple(a, O, c[a.d], dl, F)) {
+                if (a.rhouf_d) a.rhouf_d[O] = ((bits(dl) & ABS_MASK) == 0ull) ? 0.0 : mass_flux(dl, F, a.lrho);
+            } else {
+                need_face = true;
             }
-        }
-        if (!need) {
-            a.fout[O] = (fc == 1.0) ? 1.0 : 0.0;
-            if (a.rhouf_d) a.rhouf_d[O] = m;
+        } else if (a.rhouf_d) {
+            a.rhouf_d[O] = 0.0;
         }
     }
-    warp_append(a.list, a.list_count, valid && need, (unsigned int)O);
+    warp_append(a.list, a.list_count, valid && need_cell, (unsigned int)O);
+    warp_append(a.flist, a.flist_count, valid && need_face, (unsigned int)O);
+}
+
+template <int D>
+__global__ void __launch_bounds__(128) vof_faces(SweepArgs a) {
+    const unsigned int count = *a.flist_count;
+    for (unsigned int k = blockIdx.x * blockDim.x + threadIdx.x; k < count; k += gridDim.x * blockDim.x) {
+        const long long K = a.flist[k];
+        int c[3];
+        coords_of<D>(a.g, K, c);
+        const double dl = a.h * (a.u1[K] + a.u2[K]);
+        const double F = face_flux_recon<D>(a, K, c[a.d], dl);
+        a.flux[K] = F;
+        if (a.rhouf_d) a.rhouf_d[K] = mass_flux(dl, F, a.lrho);
+    }
 }
 
 template <int D, bool FIRST>
-__global__ void __launch_bounds__(128) vof_list(SweepArgs a) {
+__global__ void __launch_bounds__(128) vof_cells(SweepArgs a) {
     const unsigned int count = *a.list_count;
     const Grid& g = a.g;
     const long long sd = g.s[a.d];
@@ -162,9 +207,9 @@ __global__ void __launch_bounds__(128) vof_list(SweepArgs a) {
         coords_of<D>(g, O, c);
         const int sc[3] = {bc_src(g, 0, c[0]), bc_src(g, 1, c[1]), D == 3 ? bc_src(g, 2, c[2]) : 0};
         const long long S = lin(g, sc[0], sc[1], sc[2]);
-        double dl_lo, dl_hi;
-        const double F_lo = face_flux<D>(a, S, sc[a.d], dl_lo);
-        const double F_hi = face_flux<D>(a, S + sd, sc[a.d] + 1, dl_hi);
+        double dl, F_lo, F_hi;
+        if (!face_simple(a, S, sc[a.d], dl, F_lo)) F_lo = a.flux[S];
+        if (!face_simple(a, S + sd, sc[a.d] + 1, dl, F_hi)) F_hi = a.flux[S + sd];
         const double fS = a.fin[S];
         const int cb = FIRST ? ((fS < 0.5) ? 0 : 1) : a.cbar[S];
         const double du = (a.u1[S + sd] - a.u1[S]) + (a.u2[S + sd] - a.u2[S]);
@@ -190,15 +235,6 @@ __global__ void __launch_bounds__(128) vof_list(SweepArgs a) {
         // cleanWisp! (src/VOFutil.jl:127-136)
         v = (v < a.tol_clean) ? 0.0 : ((v > 1.0 - a.tol_clean) ? 1.0 : v);
         a.fout[O] = v;
-        if (a.rhouf_d) {
-            double m = 0.0;
-            if (in_face_range<D>(g, a.d, c)) {
-                double dl = dl_lo, F = F_lo;
-                if (O != S) F = face_flux<D>(a, O, c[a.d], dl);
-                m = (dl == 0.0) ? 0.0 : mass_flux(dl, F, a.lrho);
-            }
-            a.rhouf_d[O] = m;
-        }
     }
 }
 
@@ -217,13 +253,19 @@ cudaError_t vof_sweep_bulk(const SweepArgs& a, cudaStream_t st) {
     return cudaGetLastError();
 }
 
-cudaError_t vof_sweep_list(const SweepArgs& a, cudaStream_t st, int list_blocks) {
+cudaError_t vof_sweep_faces(const SweepArgs& a, cudaStream_t st, int list_blocks) {
+    if (a.g.D == 2) vof_faces<2><<<list_blocks, 128, 0, st>>>(a);
+    else vof_faces<3><<<list_blocks, 128, 0, st>>>(a);
+    return cudaGetLastError();
+}
+
+cudaError_t vof_sweep_cells(const SweepArgs& a, cudaStream_t st, int list_blocks) {
     if (a.g.D == 2) {
-        if (a.first) vof_list<2, true><<<list_blocks, 128, 0, st>>>(a);
-        else vof_list<2, false><<<list_blocks, 128, 0, st>>>(a);
+        if (a.first) vof_cells<2, true><<<list_blocks, 128, 0, st>>>(a);
+        else vof_cells<2, false><<<list_blocks, 128, 0, st>>>(a);
     } else {
-        if (a.first) vof_list<3, true><<<list_blocks, 128, 0, st>>>(a);
-        else vof_list<3, false><<<list_blocks, 128, 0, st>>>(a);
+        if (a.first) vof_cells<3, true><<<list_blocks, 128, 0, st>>>(a);
+        else vof_cells<3, false><<<list_blocks, 128, 0, st>>>(a);
     }
     return cudaGetLastError();
 }

@@ -24,13 +24,17 @@ struct SweepArgs {
     double tol_rep;                   // reportFillError tolerance
     double tol_clean;                 // cleanWisp! tolerance (10 eps)
     unsigned long long ulim;          // bit pattern of 1/(2δt): fast-path velocity bound
-    unsigned int* list;               // compacted cells for the list pass
+    unsigned int* list;               // cells needing the full update
     unsigned int* list_count;
+    unsigned int* flist;              // faces whose donor needs reconstruction
+    unsigned int* flist_count;
+    double* flux;                     // cached face fluxes of listed faces
     DevStatus* st;
 };
 
 cudaError_t vof_sweep_bulk(const SweepArgs& a, cudaStream_t st);
-cudaError_t vof_sweep_list(const SweepArgs& a, cudaStream_t st, int list_blocks);
+cudaError_t vof_sweep_faces(const SweepArgs& a, cudaStream_t st, int list_blocks);
+cudaError_t vof_sweep_cells(const SweepArgs& a, cudaStream_t st, int list_blocks);
 
 // applyVOF! interior + BCf! ghosts
 cudaError_t apply_vof(const Grid& g, const double* sdf, double* f, double* alpha, double* nhat, cudaStream_t st);
