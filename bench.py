@@ -244,7 +244,7 @@ def run_gpu(args, rank, world, local_rank):
         ms = float(t.item())
     ms_step = ms / args.steps
     value = world * N ** 3 * args.steps / (ms / 1e3) / 1e6
-    launches = args.steps * (1 + 3 * 3)          # status reset + 3 × (bulk + faces + cells)
+    launches = args.steps * (1 + 3 * 4)          # status reset + 3 × (bulk + faces + cells + scatter)
 
     # ---- per-kernel durations (event instrumentation inside the library, same stream)
     T = (C.c_double * 16)()

@@ -151,6 +151,43 @@ int ia_vof_flux(ia_handle* h, double* fF, const double* f, const double* alpha,
  * centre ± 0.01 e_d for d = 0..D-1 (+ first).  Interior cells only. */
 int ia_apply_vof(ia_handle* h, const double* sdf, double* f, double* alpha, double* nhat);
 
+/* MPFMomStep!(flow, pois, intf, body; δt) — src/flow.jl:60-109, the body of
+ * sim_step!(::TwoPhaseSimulation) src/InterfaceAdvection.jl:100-103.
+ * Density-weighted RK2 step on the bound fields: CMOM momentum advection fused
+ * with the VOF sweeps (split order from n_dt = length(Δt)), viscous and
+ * surface-tension forcing, velocity update with constant gravity, projection
+ * (poisson_mode, poisson_tol, poisson_itmx of the config), then
+ * status->dt_next = min(MPCFL, 1.2 dt) for push!(Δt, ·).  `dt` is δt = last(Δt).
+ * Required bound fields: u, u0, force, sigma, p, mu0, f, f0, rhou, rhouf. */
+int ia_mom_step(ia_handle* h, double dt, int64_t n_dt, double t_now, ia_status* status);
+
+/* MPCFL(flow, intf) — src/flow.jl:262-281 (on the bound u). */
+int ia_cfl(ia_handle* h, double* dt_out);
+
+/* WaterLily BC!(a, u_BC, false, perdir) on a vector field, as the reference
+ * calls it on u, ρu, ρuf and μ₀ (src/flow.jl:69,79,82,207,258). */
+int ia_bc_velocity(ia_handle* h, double* a);
+
+/* Pressure solve of inproject!(::MultiLevelPoisson) — src/flow.jl:343-347
+ * (WaterLily solver!): A x = z with the face coefficients L (μ₀), x holding the
+ * initial guess; stops when the L-infinity FP64 residual is <= tol or after itmx
+ * iterations (IA_WARN_NOT_CONVERGED). */
+int ia_poisson_solve(ia_handle* h, double* x, const double* z, const double* L, double tol,
+                     int32_t itmx, int32_t* iters, double* resid);
+
+/* updateL!(μ₀, f) + myproject!(flow, pois, w) — src/flow.jl:254-259, 328-347, with
+ * dtp = w·last(Δt), on the bound u, p, sigma (source) and mu0; then BC!(u). */
+int ia_project(ia_handle* h, const double* f, double dtp, int32_t* iters, double* resid);
+
+/* advectfq!(flow, intf, f, u¹, u², uOld, δt) — src/flow.jl:157-232: momentum
+ * advection of the bound ρu fused with the VOF advection of f. */
+int ia_advect_momentum(ia_handle* h, double* f, const double* u1, const double* u2,
+                       const double* uOld, double dt, int64_t n_dt, ia_status* status);
+
+/* viscSurfTenρu!(r, u, ...) — src/flow.jl:113-117 into the bound force field,
+ * with the fraction f (the reference's f⁰ midpoint or f). */
+int ia_visc_surften(ia_handle* h, const double* f);
+
 /* Σ f over interior cells (FP64, deterministic tree order): the mass the
  * reference checks with sum(f[inside(f)]), test/maintests.jl:209,215. */
 int ia_mass(ia_handle* h, const double* f, double* mass_out);

@@ -86,21 +86,18 @@ int status_collect(ia_handle* h, const double* u1, const double* u2, ia_status* 
 }
 
 // One advect! (src/advection.jl:17-78) or one advectVOF1d! sweep sequence.
-int advect_sweeps(ia_handle* h, double* f, const double* u1, const double* u2, double dt, const int* dirs,
-                  int nsweeps, int8_t* cbar, double* rhouf, double tol_rep, bool first_writes_cbar,
-                  int counter_base) {
+int vof_sweep(ia_handle* h, const double* fin, double* fout, const double* u1, const double* u2, double dt, int d,
+              bool first, int8_t* cbar, double* rhouf, double tol_rep, int counter) {
     const Grid& g = h->g;
-    double* bufs[2] = {h->tmp1, h->tmp2};
-    const double* in = f;
-    for (int k = 0; k < nsweeps; ++k) {
+    {
+        const int k = 0, counter_base = counter;
         SweepArgs a;
         a.g = g;
-        a.d = dirs[k];
+        a.d = d;
         a.scheme = h->cfg.normal_scheme;
-        a.first = first_writes_cbar && k == 0;
-        a.fin = in;
-        double* out = (k == nsweeps - 1) ? f : bufs[k & 1];
-        a.fout = out;
+        a.first = first;
+        a.fin = fin;
+        a.fout = fout;
         a.u1 = u1 + (long long)a.d * g.N;
         a.u2 = u2 + (long long)a.d * g.N;
         a.cbar = cbar;
@@ -108,6 +105,8 @@ int advect_sweeps(ia_handle* h, double* f, const double* u1, const double* u2, d
         a.h = dt / 2.0;
         a.dt = dt;
         a.lrho = h->cfg.lrho;
+        a.one_m_lrho = 1.0 - h->cfg.lrho;
+        a.hl = (dt / 2.0) * h->cfg.lrho;
         a.tol_rep = tol_rep;
         a.tol_clean = 10.0 * 2.220446049250313e-16;
         double lim = (dt > 0.0 && std::isfinite(dt)) ? 0.5 / dt : 0.0;
@@ -117,6 +116,7 @@ int advect_sweeps(ia_handle* h, double* f, const double* u1, const double* u2, d
         a.flist = h->flist;
         a.flist_count = &h->dst->list_count[(2 * (counter_base + k) + 1) & 31];
         a.flux = h->flux;
+        a.vals = h->tmp1;
         a.st = h->dst;
         int tk = timing_begin(h, TK_VOF_BULK);
         cudaError_t e = vof_sweep_bulk(a, h->stream);
@@ -128,9 +128,20 @@ int advect_sweeps(ia_handle* h, double* f, const double* u1, const double* u2, d
         if (e != cudaSuccess) return IA_ERR_CUDA;
         tk = timing_begin(h, TK_VOF_LIST);
         e = vof_sweep_cells(a, h->stream, h->list_blocks);
+        if (e == cudaSuccess) e = vof_sweep_scatter(a, h->stream, h->list_blocks);
         timing_end(h, tk);
         if (e != cudaSuccess) return IA_ERR_CUDA;
-        in = out;
+    }
+    return IA_OK;
+}
+
+int advect_sweeps(ia_handle* h, double* f, const double* u1, const double* u2, double dt, const int* dirs,
+                  int nsweeps, int8_t* cbar, double* rhouf, double tol_rep, bool first_writes_cbar,
+                  int counter_base) {
+    for (int k = 0; k < nsweeps; ++k) {
+        const int rc = vof_sweep(h, f, f, u1, u2, dt, dirs[k], first_writes_cbar && k == 0, cbar, rhouf, tol_rep,
+                                 counter_base + k);
+        if (rc != IA_OK) return rc;
     }
     return IA_OK;
 }
@@ -230,7 +241,6 @@ int ia_create(const ia_config* cfg, ia_handle** out) {
     const size_t nb = sizeof(double) * (size_t)h->g.N;
     cudaError_t e = cudaSuccess;
     e = e ? e : cudaMalloc(&h->tmp1, nb);
-    e = e ? e : cudaMalloc(&h->tmp2, nb);
     e = e ? e : cudaMalloc(&h->list, sizeof(unsigned int) * (size_t)h->g.N);
     e = e ? e : cudaMalloc(&h->flist, sizeof(unsigned int) * (size_t)h->g.N);
     e = e ? e : cudaMalloc(&h->flux, nb);
@@ -258,7 +268,6 @@ int ia_destroy(ia_handle* h) {
     extra_destroy(h);
     for (cudaEvent_t ev : h->timing.pool) cudaEventDestroy(ev);
     cudaFree(h->tmp1);
-    cudaFree(h->tmp2);
     cudaFree(h->list);
     cudaFree(h->flist);
     cudaFree(h->flux);

@@ -31,8 +31,7 @@ struct ia_handle {
     cudaStream_t stream;
     ia_fields fld;
     // scratch owned by the library
-    double* tmp1 = nullptr;            // ping-pong fraction buffers
-    double* tmp2 = nullptr;
+    double* tmp1 = nullptr;            // staged values of listed cells
     unsigned int* list = nullptr;      // compacted cells needing the full update
     unsigned int* flist = nullptr;     // compacted faces needing reconstruction
     double* flux = nullptr;            // cached fluxes of listed faces
@@ -50,6 +49,9 @@ namespace ia {
 int cuda_fail(cudaError_t e);
 int status_reset(ia_handle* h);
 int status_collect(ia_handle* h, const double* u1, const double* u2, ia_status* out, bool merge);
+// one VOF sweep along d, fin -> fout (fin == fout: in place)
+int vof_sweep(ia_handle* h, const double* fin, double* fout, const double* u1, const double* u2, double dt, int d,
+              bool first, int8_t* cbar, double* rhouf, double tol_rep, int counter);
 int advect_sweeps(ia_handle* h, double* f, const double* u1, const double* u2, double dt, const int* dirs,
                   int nsweeps, int8_t* cbar, double* rhouf, double tol_rep, bool first_writes_cbar,
                   int counter_base);

@@ -1,0 +1,630 @@
+// Momentum, forcing and projection kernels of MPFMomStep! (InterfaceAdvection.jl
+// src/flow.jl, src/VOFutil.jl, src/surfaceTension.jl) on the reference's
+// staggered, ghost-padded FP64 layout.
+//
+// FP64 issues at 1/64 of the FP32 rate on this part, so the kernels keep FP64
+// for the arithmetic the reference does and move everything else off the FP64
+// pipe: comparisons, min/max and medians use monotone integer keys of the
+// IEEE bit patterns (ia_bc.cuh); full/empty cells take branches whose result
+// is a precomputed constant (density λρ or λρ+(1-λρ), their reciprocals,
+// face viscosities).  Ghost values are produced by the boundary-condition
+// source rules of ia_bc.cuh instead of separate ghost passes.
+#include <cuda_runtime.h>
+
+#include "ia_geom.cuh"
+#include "mom.cuh"
+
+namespace ia {
+
+namespace {
+
+inline dim3 blk() { return dim3(32, 8, 1); }
+inline dim3 grd(const Grid& g) { return dim3((g.n[0] + 31) / 32, (g.n[1] + 7) / 8, g.n[2]); }
+
+#define CELL_XYZ                                                                                   \
+    const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y; \
+    const int z = blockIdx.z;                                                                      \
+    if (x >= g.n[0] || y >= g.n[1]) return;
+
+// x / getρ for a face between cells with fractions fa, fb (src/VOFutil.jl:176, 198-201)
+__device__ __forceinline__ double div_rho(const MomConsts& k, double v, double fa, double fb) {
+    const unsigned long long a = dbits(fa), b = dbits(fb);
+    if (a == b && a == 0ull) return v * k.inv_lrho;
+    if (a == b && a == kOneBits) return v * k.inv_rho1;
+    return v / (k.lrho + k.one_m * ((fa + fb) / 2.0));
+}
+__device__ __forceinline__ double mul_rho(const MomConsts& k, double v, double fa, double fb) {
+    const unsigned long long a = dbits(fa), b = dbits(fb);
+    if (a == b && a == 0ull) return v * k.lrho;
+    if (a == b && a == kOneBits) return v * k.rho1;
+    return v * (k.lrho + k.one_m * ((fa + fb) / 2.0));
+}
+
+// ------------------------------------------------------------------ velocity from momentum
+__global__ void ustar_kern(MomConsts k, const double* __restrict__ rhou, const double* __restrict__ f,
+                           double* __restrict__ us) {
+    const Grid& g = k.g;
+    CELL_XYZ
+    const long long O = lin(g, x, y, z);
+    for (int i = 0; i < g.D; ++i) {
+        int c[3] = {x, y, z};
+        if (vel_bc(g, i, c)) {
+            us[O + i * g.N] = k.uBC[i];
+            continue;
+        }
+        const long long P = lin3(g, c);
+        us[O + i * g.N] = div_rho(k, rhou[P + i * g.N], f[P], f[P - g.s[i]]);
+    }
+}
+
+__global__ void u2rhou_kern(MomConsts k, double* __restrict__ rhou, const double* __restrict__ u,
+                            const double* __restrict__ f) {
+    const Grid& g = k.g;
+    CELL_XYZ
+    const int c[3] = {x, y, z};
+    if (!is_interior(g, c)) return;
+    const long long I = lin(g, x, y, z);
+    for (int i = 0; i < g.D; ++i) rhou[I + i * g.N] = mul_rho(k, u[I + i * g.N], f[I], f[I - g.s[i]]);
+}
+
+__global__ void bcvel_kern(MomConsts k, double* a, double A0, double A1, double A2) {
+    const Grid& g = k.g;
+    CELL_XYZ
+    const int c0[3] = {x, y, z};
+    const bool inner = is_interior(g, c0);
+    const long long O = lin(g, x, y, z);
+    const double A[3] = {A0, A1, A2};
+    for (int i = 0; i < g.D; ++i) {
+        int c[3] = {x, y, z};
+        if (vel_bc(g, i, c)) { a[O + i * g.N] = A[i]; continue; }
+        if (inner) continue;
+        a[O + i * g.N] = a[lin3(g, c) + i * g.N];
+    }
+}
+
+// ------------------------------------------------------------------ limiters (src/flow.jl:5-15)
+__device__ __forceinline__ double median3(double a, double b, double c) { return dmax(dmin(a, b), dmin(dmax(a, b), c)); }
+__device__ __forceinline__ double sgn(double v) { return okey(v) > 0 ? 1.0 : (okey(v) < 0 ? -1.0 : 0.0); }
+
+__device__ double limiter(int which, double u, double c, double d) {
+    switch (which) {
+        case IA_LIMITER_UPWIND: return c;
+        case IA_LIMITER_MINMOD: return median3((3.0 * c - u) * 0.5, c, (c + d) * 0.5);
+        case IA_LIMITER_VANALBADA1: {
+            const double al = c - u, be = d - c;
+            const double fac = (dbits(al) << 1) == 0 && (dbits(be) << 1) == 0 ? 0.0 : (al + be) / (al * al + be * be);
+            return c + dmax(al * be, 0.0) * fac / 2.0;
+        }
+        case IA_LIMITER_SWEBY:
+        case IA_LIMITER_SUPERBEE: {
+            const double gam = which == IA_LIMITER_SWEBY ? 1.5 : 2.0;
+            if (!dlt(dmin(u, d), c) || !dlt(c, dmax(u, d))) return c;
+            const double s = sgn(d - u);
+            return c + s * dmax(dmax(0.0, dmin(s * gam * (c - u), s * (d - c))), dmin(s * (c - u), s * gam * (d - c))) / 2.0;
+        }
+        case IA_LIMITER_TVDCEN: {
+            if (!dlt(dmin(u, d), c) || !dlt(c, dmax(u, d))) return c;
+            const double s = sgn(d - u);
+            return c + s * dmin(s * (c - u), s * (d - c) / 2.0);
+        }
+        case IA_LIMITER_TVDDOWN: {
+            if (!dlt(dmin(u, d), c) || !dlt(c, dmax(u, d))) return c;
+            const double s = sgn(d - u);
+            return c + s * dmin(s * (c - u), s * (d - c));
+        }
+        default:   // Koren
+            return median3((7.0 * c + d - 2.0 * u) * (1.0 / 6.0), c, median3(2.0 * c - u, c, d));
+    }
+}
+
+// ------------------------------------------------------------------ CMOM face flux
+struct FluxCtx {
+    MomConsts k;
+    int j, lim;
+    const double* us;
+    const double* rj;     // ρuf[:, j] before the 1/δt scaling
+    const double* fold;
+    double dt, inv_dt;
+};
+
+// BC!'d ρuf[X, j] / δt (the reference scales by inv(δt) then applies BC!)
+__device__ __forceinline__ double rflux(const FluxCtx& F, int c[3]) {
+    const Grid& g = F.k.g;
+    if (vel_bc(g, F.j, c)) return F.k.uBC[F.j];
+    return F.rj[lin3(g, c)] * F.inv_dt;
+}
+
+// 1 + (λρ - 1)... : λρ + (1-λρ) dρ[X, i], dρ = BCv!(f2face!(f_old)); the upper normal
+// face of a zero-gradient dimension is never written by the reference and keeps
+// the 1 it is initialised with (src/cVOF.jl:74).
+__device__ __forceinline__ double m_old(const FluxCtx& F, int i, int c[3], bool& is_lrho, bool& is_rho1) {
+    const Grid& g = F.k.g;
+    is_lrho = is_rho1 = false;
+    if (face_bc(g, i, c)) { is_rho1 = true; return F.k.rho1; }
+    const long long P = lin3(g, c);
+    const double fa = F.fold[P], fb = F.fold[P - g.s[i]];
+    const unsigned long long a = dbits(fa), b = dbits(fb);
+    if (a == b && a == 0ull) { is_lrho = true; return F.k.lrho; }
+    if (a == b && a == kOneBits) { is_rho1 = true; return F.k.rho1; }
+    return F.k.lrho + F.k.one_m * ((fa + fb) / 2.0);
+}
+
+// ϕq (src/flow.jl:37-57) on the upwind triple (uu, cc, dd); cic = coords of the face
+__device__ double phiq(const FluxCtx& F, int i, const int cic[3], double Psi, double uu, double cc, double dd) {
+    int c[3] = {cic[0], cic[1], cic[2]};
+    if (okey(Psi) > 0) c[F.j] -= 1;                       // IiCell = Ψ>0 ? Ii-δj : Ii
+    const double vI = cc;
+    const double vd = limiter(F.lim, uu, cc, dd);
+    const double va = 2.0 * vI - vd;
+    const double mOut = dabs(Psi) * F.dt;
+    bool isl, isr;
+    const double mOld = m_old(F, i, c, isl, isr);
+    if (dlt(mOld, mOut)) return Psi * vI;
+    const double l2 = isl ? mOut * F.k.inv_lrho : (isr ? mOut * F.k.inv_rho1 : mOut / mOld);
+    const double l1 = 1.0 - l2;
+    const double vb = l2 * va + l1 * vd;
+    return Psi * (vb + vd) / 2.0;
+}
+
+__global__ void momflux_kern(FluxCtx F, double* __restrict__ Phi) {
+    const Grid& g = F.k.g;
+    CELL_XYZ
+    const int j = F.j;
+    int c[3] = {x, y, z};
+    for (int e = 0; e < g.D; ++e) {
+        const int hi = (e == j) ? g.n[e] - 1 : g.n[e] - 2;
+        if (c[e] < 1 || c[e] > hi) return;
+    }
+    const long long K = lin(g, x, y, z);
+    const bool per = g.isper(j);
+    if (per && c[j] == g.n[j] - 1) c[j] = 1;              // periodic upper face = lower face
+    const long long Kk = lin3(g, c);
+    const int kj = c[j];
+    const long long sj = g.s[j];
+    const bool lower = kj == 1, upper = !per && kj == g.n[j] - 1;
+    for (int i = 0; i < g.D; ++i) {
+        int ca[3] = {c[0], c[1], c[2]}, cb[3] = {c[0], c[1], c[2]};
+        cb[i] -= 1;
+        const double Psi = (rflux(F, ca) + rflux(F, cb)) / 2.0;      // ϕ(i, CI(I,j), ρuf)
+        const double* u = F.us + i * g.N;
+        const bool pos = okey(Psi) > 0;
+        double uu, cc, dd;
+        if (lower && !per) {               // ϕuL: linear extrapolation below the wall
+            if (pos) { cc = u[Kk - sj]; dd = u[Kk]; uu = 2.0 * cc - dd; }
+            else { uu = u[Kk + sj]; cc = u[Kk]; dd = u[Kk - sj]; }
+        } else if (lower) {                // ϕuP: periodic image of I-2δj
+            if (pos) { uu = u[Kk + (long long)(g.n[j] - 3 - kj) * sj]; cc = u[Kk - sj]; dd = u[Kk]; }
+            else { uu = u[Kk + sj]; cc = u[Kk]; dd = u[Kk - sj]; }
+        } else if (upper) {                // ϕuR
+            if (okey(Psi) < 0) { cc = u[Kk]; dd = u[Kk - sj]; uu = 2.0 * cc - dd; }
+            else { uu = u[Kk - 2 * sj]; cc = u[Kk - sj]; dd = u[Kk]; }
+        } else {                           // ϕu
+            if (pos) { uu = u[Kk - 2 * sj]; cc = u[Kk - sj]; dd = u[Kk]; }
+            else { uu = u[Kk + sj]; cc = u[Kk]; dd = u[Kk - sj]; }
+        }
+        Phi[K + i * g.N] = phiq(F, i, c, Psi, uu, cc, dd);
+    }
+}
+
+// ρ̄∂ⱼuⱼ at a (ghost-mapped) cell: getρ(I,c̄,λρ)(∂(d,I,u)+∂(d,I,u⁰))/2, BCf! ghosts
+__device__ __forceinline__ double dila(const MomConsts& k, int d, int c[3], const double* u1, const double* u2,
+                                       const int8_t* cbar) {
+    const Grid& g = k.g;
+    for (int e = 0; e < g.D; ++e) c[e] = bc_src(g, e, c[e]);
+    const long long P = lin3(g, c);
+    const long long sd = g.s[d];
+    const double rho = cbar[P] ? k.rho1 : k.lrho;
+    return rho * ((u1[P + sd] - u1[P]) + (u2[P + sd] - u2[P])) / 2.0;
+}
+
+__global__ void momupdate_kern(MomConsts k, int j, const double* __restrict__ Phi, const double* __restrict__ uOld,
+                               const double* __restrict__ u1d, const double* __restrict__ u2d,
+                               const int8_t* __restrict__ cbar, double dt, double* __restrict__ rhou) {
+    const Grid& g = k.g;
+    CELL_XYZ
+    const int c0[3] = {x, y, z};
+    if (!is_interior(g, c0)) return;
+    const long long I = lin(g, x, y, z);
+    int cc[3] = {x, y, z};
+    const double dI = dila(k, j, cc, u1d, u2d, cbar);
+    for (int i = 0; i < g.D; ++i) {
+        int cm[3] = {x, y, z};
+        cm[i] -= 1;
+        const double dm = dila(k, j, cm, u1d, u2d, cbar);
+        const double r = (Phi[I + i * g.N] - Phi[I + g.s[j] + i * g.N]) + uOld[I + i * g.N] * ((dI + dm) / 2.0);
+        rhou[I + i * g.N] = rhou[I + i * g.N] + dt * r;
+    }
+}
+
+// ------------------------------------------------------------------ viscosity
+struct ViscCtx {
+    MomConsts k;
+    const double* u;
+    const double* f;
+    double lmu, mu, mu_face0, mu_face1;   // μ at full-light / full-dark faces
+    double ratio;                         // λμ/λρ
+};
+
+// fFace = BCv!(f2face!(f)); the reference's fFace buffer aliases n̂, whose upper
+// normal face still holds uStar's Dirichlet value u_BC[d] from the last momentum sweep.
+__device__ __forceinline__ double fface(const ViscCtx& V, int d, int c[3]) {
+    const Grid& g = V.k.g;
+    if (face_bc(g, d, c)) return V.k.uBC[d];
+    const long long P = lin3(g, c);
+    const double fa = V.f[P], fb = V.f[P - g.s[d]];
+    if (dbits(fa) == dbits(fb)) return fa;
+    return (fa + fb) / 2.0;
+}
+
+// getμ(i,j,I,fFace,λμ,μ,λρ) (src/VOFutil.jl:186-191)
+__device__ double get_mu(const ViscCtx& V, int i, int j, const int cI[3]) {
+    int a[3] = {cI[0], cI[1], cI[2]}, b[3] = {cI[0], cI[1], cI[2]}, c[3] = {cI[0], cI[1], cI[2]},
+        d[3] = {cI[0], cI[1], cI[2]};
+    a[j] -= 1;
+    c[i] -= 1;
+    const double f1 = fface(V, i, a), f2 = fface(V, i, b), f3 = fface(V, j, c), f4 = fface(V, j, d);
+    const unsigned long long b1 = dbits(f1);
+    if (b1 == dbits(f2) && b1 == dbits(f3) && b1 == dbits(f4)) {
+        if (b1 == 0ull) return V.mu_face0;
+        if (b1 == kOneBits) return V.mu_face1;
+    }
+    const double s = (f1 + f2 + f3 + f4) / 4.0;
+    const double fr = V.k.lrho < 1.0 ? dmin(dmin(f1, f2), dmin(f3, f4)) : dmax(dmax(f1, f2), dmax(f3, f4));
+    const double fac = dlt(0.5, s) ? 1.0 : V.ratio;
+    return V.mu * dmin(V.lmu + (1.0 - V.lmu) * s, fac * (V.k.lrho + V.k.one_m * fr));
+}
+
+__device__ __forceinline__ int pair_index(int D, int i, int j) {
+    if (i == j) return i;
+    const int a = i < j ? i : j, b = i < j ? j : i;
+    return D + (a == 0 ? (b - 1) : 2);   // (0,1)->D, (0,2)->D+1, (1,2)->D+2
+}
+
+__global__ void viscflux_kern(ViscCtx V, double* __restrict__ Phi6) {
+    const Grid& g = V.k.g;
+    CELL_XYZ
+    const int c[3] = {x, y, z};
+    const long long K = lin(g, x, y, z);
+    for (int i = 0; i < g.D; ++i)
+        for (int j = i; j < g.D; ++j) {
+            bool ok = true;
+            for (int e = 0; e < g.D; ++e) {
+                const int hi = (e == i || e == j) ? g.n[e] - 1 : g.n[e] - 2;
+                if (c[e] < 1 || c[e] > hi) ok = false;
+            }
+            if (!ok) continue;
+            const double mu = get_mu(V, i, j, c);
+            const double sji = V.u[K + i * g.N] - V.u[K - g.s[j] + i * g.N];
+            const double sij = V.u[K + j * g.N] - V.u[K - g.s[i] + j * g.N];
+            Phi6[pair_index(g.D, i, j) * g.N + K] = -(mu * (sji + sij));
+        }
+}
+
+__global__ void viscacc_kern(Grid g, const double* __restrict__ Phi6, double* __restrict__ r) {
+    CELL_XYZ
+    const int c[3] = {x, y, z};
+    if (!is_interior(g, c)) return;
+    const long long I = lin(g, x, y, z);
+    for (int i = 0; i < g.D; ++i) {
+        double acc = 0.0;
+        for (int j = 0; j < g.D; ++j) {
+            const double* P = Phi6 + pair_index(g.D, i, j) * g.N;
+            acc = (acc + P[I]) - P[I + g.s[j]];
+        }
+        r[I + i * g.N] = acc;
+    }
+}
+
+__global__ void zero_kern(double* a, long long n) {
+    for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < n; q += (long long)gridDim.x * blockDim.x)
+        a[q] = 0.0;
+}
+
+// ------------------------------------------------------------------ surface tension
+__global__ void fbuffer_kern(MomConsts k, int d, const double* __restrict__ f, double* __restrict__ fb) {
+    const Grid& g = k.g;
+    CELL_XYZ
+    int c[3] = {x, y, z};
+    // BCf!(d, ·): the high ghost along a zero-gradient d is not written by the
+    // reference (it keeps older buffer contents); it is taken as a zero-gradient copy here.
+    if (face_bc(g, d, c)) c[d] = g.n[d] - 2;
+    const long long P = lin3(g, c);
+    const double fa = f[P], fm = f[P - g.s[d]];
+    fb[lin(g, x, y, z)] = (dbits(fa) == dbits(fm)) ? fa : (fa + fm) / 2.0;
+}
+
+__device__ __forceinline__ bool mixed(double v) {
+    const unsigned long long b = dbits(v);
+    return b != 0ull && b < kOneBits;   // 0 < v < 1 (sign bit set → huge, excluded)
+}
+
+// getPopinetHeightAdaptive, monotonic (src/surfaceTension.jl:78-101); axis a, direction sg
+__device__ double popinet_height(const Grid& g, const double* fb, const int c0[3], int a, int sg) {
+    int c[3] = {c0[0], c0[1], c0[2]};
+    double fnow = fb[lin3(g, c)];
+    double H = fnow - 0.5;
+    bool fin = fnow < 1.0;
+    while (!fin || mixed(fnow)) {
+        c[a] += sg;
+        if (c[a] < 0 || c[a] > g.n[a] - 1) break;
+        const double fv = fb[lin3(g, c)];
+        fnow = dlt(fnow, fv) ? 0.0 : fv;
+        H += fnow;
+        if (mixed(fnow)) fin = true;
+    }
+    c[a] = c0[a];
+    fnow = fb[lin3(g, c)];
+    fin = fnow > 0.0;
+    while (!fin || mixed(fnow)) {
+        c[a] -= sg;
+        if (c[a] < 0 || c[a] > g.n[a] - 1) break;
+        const double fv = fb[lin3(g, c)];
+        fnow = dlt(fv, fnow) ? 1.0 : fv;
+        H += fnow - 1.0;
+        if (mixed(fnow)) fin = true;
+    }
+    return H;
+}
+
+// getCurvature (src/surfaceTension.jl:29-59); md = signed 1-based major direction
+__device__ double curvature(const Grid& g, const double* fb, const int c[3], int md) {
+    const int a = abs(md) - 1;
+    const int sg = md > 0 ? 1 : -1;
+    if (g.D == 3) {
+        const int am = abs(md);
+        const int ix = sg * (am % 3 + 1), iy = (am + 1) % 3 + 1;   // getXYdir
+        const int ax = abs(ix) - 1, sx = ix > 0 ? 1 : -1, ay = iy - 1;
+        double H[3][3];
+        for (int yu = -1; yu <= 1; ++yu)
+            for (int xu = -1; xu <= 1; ++xu) {
+                int q[3] = {c[0], c[1], c[2]};
+                q[ax] += xu * sx;
+                q[ay] += yu;
+                H[xu + 1][yu + 1] = popinet_height(g, fb, q, a, sg);
+            }
+        const double filt = 0.2;
+        const double Hx = (H[2][1] - H[0][1]) / 2.0, Hy = (H[1][2] - H[1][0]) / 2.0;
+        const double Hxx = ((H[2][1] + H[0][1] - 2.0 * H[1][1]) + (H[2][0] + H[0][0] - 2.0 * H[1][0]) * filt +
+                            (H[2][2] + H[0][2] - 2.0 * H[1][2]) * filt) / (1.0 + 2.0 * filt);
+        const double Hyy = ((H[1][2] + H[1][0] - 2.0 * H[1][1]) + (H[0][2] + H[0][0] - 2.0 * H[0][1]) * filt +
+                            (H[2][2] + H[2][0] - 2.0 * H[2][1]) * filt) / (1.0 + 2.0 * filt);
+        const double Hxy = (H[2][2] + H[0][0] - H[2][0] - H[0][2]) / 4.0;
+        const double q1 = 1.0 + Hx * Hx + Hy * Hy;
+        return (Hxx * (1.0 + Hy * Hy) + Hyy * (1.0 + Hx * Hx) - 2.0 * Hxy * Hx * Hy) / sqrt(q1 * q1 * q1);
+    }
+    const int am = abs(md);
+    const int ix = (am == 1) ? -2 * sg : sg;   // getXdir
+    const int ax = abs(ix) - 1, sx = ix > 0 ? 1 : -1;
+    double H[3];
+    for (int xu = -1; xu <= 1; ++xu) {
+        int q[3] = {c[0], c[1], c[2]};
+        q[ax] += xu * sx;
+        H[xu + 1] = popinet_height(g, fb, q, a, sg);
+    }
+    const double Hx = (H[2] - H[0]) / 2.0, Hxx = (H[2] + H[0] - 2.0 * H[1]);
+    const double q1 = 1.0 + Hx * Hx;
+    return Hxx / sqrt(q1 * q1 * q1);
+}
+
+template <int D>
+__global__ void surften_kern(MomConsts k, int d, const double* __restrict__ f, const double* __restrict__ fb,
+                             double eta, double* __restrict__ r) {
+    const Grid& g = k.g;
+    CELL_XYZ
+    const int c[3] = {x, y, z};
+    if (!is_interior(g, c)) return;
+    const long long I = lin(g, x, y, z);
+    if (!mixed(fb[I])) return;
+    Stencil S;
+    S.f = fb;
+    S.c = I;
+    S.s[0] = g.s[0];
+    S.s[1] = g.s[1];
+    S.s[2] = g.s[2];
+    double n[3] = {0.0, 0.0, 0.0};
+    normal_columns<D, true>(S, n);                      // getInterfaceNormal_WY!
+    const int ia = arg_abs_max<D>(n);
+    const int md = signbit(n[ia]) ? -(ia + 1) : (ia + 1);
+    const double kap = curvature(g, fb, c, md);
+    r[I + d * g.N] += eta * kap * -(f[I] - f[I - g.s[d]]);
+}
+
+// ------------------------------------------------------------------ update, L, projection
+__global__ void updateu_kern(MomConsts k, double* __restrict__ u, double* __restrict__ rhou,
+                             const double* __restrict__ u0, const double* __restrict__ F, double dt,
+                             const double* __restrict__ fref, const double* __restrict__ fupd, double w, double a,
+                             bool write_rhou) {
+    const Grid& g = k.g;
+    CELL_XYZ
+    const int c[3] = {x, y, z};
+    if (!is_interior(g, c)) return;
+    const long long I = lin(g, x, y, z);
+    for (int i = 0; i < g.D; ++i) {
+        const long long q = I + i * g.N;
+        const double rho0 = mul_rho(k, u0[q], fref[I], fref[I - g.s[i]]);   // u2ρu!(n̂, u⁰, c.f)
+        const double rn = (a * rho0 + rhou[q] + F[q] * dt) * w;
+        double v = div_rho(k, rn, fupd[I], fupd[I - g.s[i]]);
+        if (k.has_g) v = (dt * w) * k.gvec[i] + v;
+        u[q] = v;
+        if (write_rhou) rhou[q] = rn;
+    }
+}
+
+__global__ void updatel_kern(MomConsts k, double* __restrict__ mu0, const double* __restrict__ f) {
+    const Grid& g = k.g;
+    CELL_XYZ
+    const long long O = lin(g, x, y, z);
+    for (int i = 0; i < g.D; ++i) {
+        int c[3] = {x, y, z};
+        if (vel_bc(g, i, c)) { mu0[O + i * g.N] = 0.0; continue; }
+        const long long P = lin3(g, c);
+        mu0[O + i * g.N] = div_rho(k, 1.0, f[P], f[P - g.s[i]]);
+    }
+}
+
+__global__ void div_scale_kern(Grid g, const double* __restrict__ u, double* __restrict__ zz,
+                               double* __restrict__ xx, double dt) {
+    CELL_XYZ
+    const long long I = lin(g, x, y, z);
+    xx[I] *= dt;
+    const int c[3] = {x, y, z};
+    if (!is_interior(g, c)) return;
+    double s = 0.0;
+    for (int d = 0; d < g.D; ++d) s += u[I + g.s[d] + d * g.N] - u[I + d * g.N];
+    zz[I] = s;
+}
+
+__global__ void correct_kern(Grid g, double* __restrict__ u, const double* __restrict__ L,
+                             const double* __restrict__ xx) {
+    CELL_XYZ
+    const int c[3] = {x, y, z};
+    if (!is_interior(g, c)) return;
+    const long long I = lin(g, x, y, z);
+    for (int i = 0; i < g.D; ++i) u[I + i * g.N] -= L[I + i * g.N] * (xx[I] - xx[I - g.s[i]]);
+}
+
+__global__ void scale_kern(double* a, long long n, double s) {
+    for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < n; q += (long long)gridDim.x * blockDim.x)
+        a[q] *= s;
+}
+
+__global__ void average_kern(double* a, const double* b, long long n) {
+    for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < n; q += (long long)gridDim.x * blockDim.x)
+        a[q] = (a[q] + b[q]) / 2.0;
+}
+
+__device__ __forceinline__ unsigned long long nonneg_bits(double v) {
+    const unsigned long long b = dbits(v);
+    return (b == 0x8000000000000000ull) ? 0ull : b;
+}
+
+__global__ void cfl_kern(Grid g, const double* __restrict__ u, unsigned long long* out) {
+    __shared__ unsigned long long s1[256], s2[256];
+    const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y;
+    const int z = blockIdx.z;
+    const int t = threadIdx.y * blockDim.x + threadIdx.x;
+    unsigned long long a1 = 0ull, a2 = 0ull;
+    if (x < g.n[0] && y < g.n[1]) {
+        const int c[3] = {x, y, z};
+        if (is_interior(g, c)) {
+            const long long I = lin(g, x, y, z);
+            double fo = 0.0, mt = 0.0;
+            for (int i = 0; i < g.D; ++i) {
+                const double lo = u[I + i * g.N], hi = u[I + g.s[i] + i * g.N];
+                fo += dmax(0.0, hi) + dmax(0.0, -lo);        // WaterLily flux_out
+                mt += dmax(dabs(lo), dabs(hi));              // maxTotalFlux, src/flow.jl:283-289
+            }
+            a1 = nonneg_bits(fo);
+            a2 = nonneg_bits(mt);
+        }
+    }
+    s1[t] = a1;
+    s2[t] = a2;
+    __syncthreads();
+    for (int w = 128; w > 0; w >>= 1) {
+        if (t < w) {
+            s1[t] = s1[t] > s1[t + w] ? s1[t] : s1[t + w];
+            s2[t] = s2[t] > s2[t + w] ? s2[t] : s2[t + w];
+        }
+        __syncthreads();
+    }
+    if (t == 0) {
+        atomicMax(&out[0], s1[0]);
+        atomicMax(&out[1], s2[0]);
+    }
+}
+
+}  // namespace
+
+cudaError_t k_ustar(const MomConsts& k, const double* rhou, const double* f, double* ustar, cudaStream_t s) {
+    ustar_kern<<<grd(k.g), blk(), 0, s>>>(k, rhou, f, ustar);
+    return cudaGetLastError();
+}
+cudaError_t k_u2rhou(const MomConsts& k, double* rhou, const double* u, const double* f, cudaStream_t s) {
+    u2rhou_kern<<<grd(k.g), blk(), 0, s>>>(k, rhou, u, f);
+    return cudaGetLastError();
+}
+cudaError_t k_bc_vel(const MomConsts& k, double* a, const double* A, cudaStream_t s) {
+    bcvel_kern<<<grd(k.g), blk(), 0, s>>>(k, a, A[0], A[1], A[2]);
+    return cudaGetLastError();
+}
+cudaError_t k_momflux(const MomConsts& k, int j, int limiter, const double* ustar, const double* rhouf_j,
+                      const double* fold, double dt, double* Phi, cudaStream_t s) {
+    FluxCtx F;
+    F.k = k;
+    F.j = j;
+    F.lim = limiter;
+    F.us = ustar;
+    F.rj = rhouf_j;
+    F.fold = fold;
+    F.dt = dt;
+    F.inv_dt = 1.0 / dt;
+    momflux_kern<<<grd(k.g), blk(), 0, s>>>(F, Phi);
+    return cudaGetLastError();
+}
+cudaError_t k_momupdate(const MomConsts& k, int j, const double* Phi, const double* uOld, const double* u1,
+                        const double* u2, const int8_t* cbar, double dt, double* rhou, cudaStream_t s) {
+    momupdate_kern<<<grd(k.g), blk(), 0, s>>>(k, j, Phi, uOld, u1 + j * k.g.N, u2 + j * k.g.N, cbar, dt, rhou);
+    return cudaGetLastError();
+}
+cudaError_t k_visc(const MomConsts& k, const double* u, const double* f, double lmu, double mu, double* Phi6,
+                   double* r, cudaStream_t s) {
+    ViscCtx V;
+    V.k = k;
+    V.u = u;
+    V.f = f;
+    V.lmu = lmu;
+    V.mu = mu;
+    V.ratio = lmu / k.lrho;
+    // getμ at faces with all four fractions 0 or all 1
+    auto lin_prop = [](double s, double l) { return l + (1.0 - l) * s; };
+    auto mu_at = [&](double s) {
+        const double fac = (s > 0.5) ? 1.0 : lmu / k.lrho;
+        const double a = lin_prop(s, lmu), b = fac * lin_prop(s, k.lrho);
+        return mu * (b < a ? b : a);
+    };
+    V.mu_face0 = mu_at(0.0);
+    V.mu_face1 = mu_at(1.0);
+    viscflux_kern<<<grd(k.g), blk(), 0, s>>>(V, Phi6);
+    viscacc_kern<<<grd(k.g), blk(), 0, s>>>(k.g, Phi6, r);
+    return cudaGetLastError();
+}
+cudaError_t k_zero(double* a, long long n, cudaStream_t s) {
+    zero_kern<<<1216, 256, 0, s>>>(a, n);
+    return cudaGetLastError();
+}
+cudaError_t k_surften(const MomConsts& k, int d, const double* f, double eta, double* fb, double* r, cudaStream_t s) {
+    fbuffer_kern<<<grd(k.g), blk(), 0, s>>>(k, d, f, fb);
+    if (k.g.D == 2) surften_kern<2><<<grd(k.g), blk(), 0, s>>>(k, d, f, fb, eta, r);
+    else surften_kern<3><<<grd(k.g), blk(), 0, s>>>(k, d, f, fb, eta, r);
+    return cudaGetLastError();
+}
+cudaError_t k_updateu(const MomConsts& k, double* u, double* rhou, const double* u0, const double* F, double dt,
+                      const double* fref, const double* fupd, double w, bool write_rhou, cudaStream_t s) {
+    const double a = 1.0 / w - 1.0;
+    updateu_kern<<<grd(k.g), blk(), 0, s>>>(k, u, rhou, u0, F, dt, fref, fupd, w, a, write_rhou);
+    return cudaGetLastError();
+}
+cudaError_t k_updatel(const MomConsts& k, double* mu0, const double* f, cudaStream_t s) {
+    updatel_kern<<<grd(k.g), blk(), 0, s>>>(k, mu0, f);
+    return cudaGetLastError();
+}
+cudaError_t k_div_scale(const MomConsts& k, const double* u, double* zz, double* xx, double dt, cudaStream_t s) {
+    div_scale_kern<<<grd(k.g), blk(), 0, s>>>(k.g, u, zz, xx, dt);
+    return cudaGetLastError();
+}
+cudaError_t k_correct(const MomConsts& k, double* u, const double* L, double* xx, double dt, cudaStream_t s) {
+    correct_kern<<<grd(k.g), blk(), 0, s>>>(k.g, u, L, xx);
+    scale_kern<<<1216, 256, 0, s>>>(xx, k.g.N, 1.0 / dt);
+    return cudaGetLastError();
+}
+cudaError_t k_cfl(const MomConsts& k, const double* u, unsigned long long* out2, cudaStream_t s) {
+    cfl_kern<<<grd(k.g), blk(), 0, s>>>(k.g, u, out2);
+    return cudaGetLastError();
+}
+cudaError_t k_average(double* a, const double* b, long long n, cudaStream_t s) {
+    average_kern<<<1216, 256, 0, s>>>(a, b, n);
+    return cudaGetLastError();
+}
+
+}  // namespace ia

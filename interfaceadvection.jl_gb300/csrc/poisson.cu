@@ -1,0 +1,612 @@
+// Variable-coefficient pressure Poisson solve of the projection step
+// (InterfaceAdvection.jl src/flow.jl:328-347, where WaterLily's
+// MultiLevelPoisson `solver!` runs V-cycles inside a PCG wrapper).
+//
+// Operator (WaterLily `mult`): (A x)_I = Σ_i L[I,i] x[I-δi] + L[I+δi,i] x[I+δi]
+// + D_I x_I with D_I = -Σ_i (L[I,i] + L[I+δi,i]); L = μ₀ = 1/ρ on faces, zero
+// on wall faces, periodic dimensions wrap.  The solver is this library's own:
+//
+//  * geometric multigrid on cell-centred levels (2x coarsening while every
+//    interior extent is even and >= 4); coarse face coefficient = ½ Σ of the
+//    2^(D-1) fine faces it covers; restriction sums the 2^D children,
+//    prolongation injects; red-black Gauss-Seidel, ν₁ sweeps red→black
+//    before and ν₂ black→red after, so the V-cycle is a symmetric
+//    preconditioner; the coarsest level is solved by one block with a fixed
+//    number of symmetric sweeps on the mean-free right-hand side;
+//  * flexible CG in FP64 around it (β from the residual change, so an
+//    inexact FP32 V-cycle stays admissible), stopping on the L∞ norm of the
+//    FP64 true residual of the dt-scaled system.
+//
+// IA_POISSON_FP64 runs the V-cycle in FP64; IA_POISSON_MIXED runs it in FP32
+// (FP32 copies of every level's operator), the defect correction, matvec,
+// dot products and updates staying FP64.
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "capi_internal.cuh"
+#include "ia_bc.cuh"
+#include "poisson.cuh"
+
+namespace ia {
+
+namespace {
+
+inline dim3 blk() { return dim3(32, 8, 1); }
+inline dim3 grd(const Grid& g) { return dim3((g.n[0] + 31) / 32, (g.n[1] + 7) / 8, g.n[2]); }
+
+// neighbour offset of interior cell coordinate ci along dimension i (periodic wrap;
+// on a wall the ghost is read but its face coefficient is zero)
+__device__ __forceinline__ long long lo_off(const Grid& g, int i, int ci) {
+    return (g.isper(i) && ci == 1) ? (long long)(g.n[i] - 3) * g.s[i] : -g.s[i];
+}
+__device__ __forceinline__ long long hi_off(const Grid& g, int i, int ci) {
+    return (g.isper(i) && ci == g.n[i] - 2) ? -(long long)(g.n[i] - 3) * g.s[i] : g.s[i];
+}
+
+template <class T>
+__device__ __forceinline__ T offdiag(const Grid& g, const T* L, const T* x, long long I, const int c[3]) {
+    T a = T(0);
+    for (int i = 0; i < g.D; ++i)
+        a += L[I + i * g.N] * x[I + lo_off(g, i, c[i])] + L[I + g.s[i] + i * g.N] * x[I + hi_off(g, i, c[i])];
+    return a;
+}
+
+#define INTERIOR_XYZ                                                                                     \
+    const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y;     \
+    const int z = blockIdx.z;                                                                            \
+    if (x < 1 || y < 1 || x > g.n[0] - 2 || y > g.n[1] - 2) return;                                      \
+    if (g.D == 3 && (z < 1 || z > g.n[2] - 2)) return;                                                   \
+    const int c[3] = {x, y, z};                                                                          \
+    const long long I = lin(g, x, y, z);
+
+template <class T>
+__global__ void set_diag_k(Grid g, const T* __restrict__ L, T* __restrict__ iD) {
+    INTERIOR_XYZ
+    T dd = T(0);
+    for (int i = 0; i < g.D; ++i) dd -= L[I + i * g.N] + L[I + g.s[i] + i * g.N];
+    const T eps = sizeof(T) == 8 ? T(2.220446049250313e-16) : T(1.1920929e-7);
+    iD[I] = (dd * dd < T(2) * eps) ? T(0) : T(1) / dd;
+}
+
+// Coarse face coefficients: ½ Σ over the fine faces covering each coarse face
+// (all coarse faces 1..n-1 along i, interior elsewhere).
+template <class T>
+__global__ void restrict_L_k(Grid gc, Grid gf, const T* __restrict__ Lf, T* __restrict__ Lc) {
+    const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y;
+    const int z = blockIdx.z;
+    if (x >= gc.n[0] || y >= gc.n[1]) return;
+    const int c[3] = {x, y, z};
+    const long long Ic = lin(gc, x, y, z);
+    for (int i = 0; i < gc.D; ++i) {
+        bool ok = true;
+        for (int e = 0; e < gc.D; ++e) {
+            const int hi = (e == i) ? gc.n[e] - 1 : gc.n[e] - 2;
+            if (c[e] < 1 || c[e] > hi) ok = false;
+        }
+        if (!ok) continue;
+        // fine base cell of the face: coordinate 2c-1 in every dimension
+        int fb[3] = {2 * c[0] - 1, 2 * c[1] - 1, gc.D == 3 ? 2 * c[2] - 1 : 0};
+        T s = T(0);
+        const int o1 = (i == 0) ? 1 : 0, o2 = (i == 2) ? 1 : 2;   // the other dimensions
+        const int n1 = 2, n2 = (gc.D == 3) ? 2 : 1;
+        for (int b = 0; b < n2; ++b)
+            for (int a = 0; a < n1; ++a) {
+                int q[3] = {fb[0], fb[1], fb[2]};
+                q[o1] += a;
+                if (gc.D == 3) q[o2] += b;
+                s += Lf[lin(gf, q[0], q[1], q[2]) + i * gf.N];
+            }
+        Lc[Ic + i * gc.N] = T(0.5) * s;
+    }
+}
+
+template <class T>
+__global__ void rbgs_k(Grid g, const T* __restrict__ L, const T* __restrict__ iD, const T* __restrict__ b,
+                       T* __restrict__ xv, int color) {
+    INTERIOR_XYZ
+    if (((x + y + z) & 1) != color) return;
+    xv[I] = (b[I] - offdiag(g, L, xv, I, c)) * iD[I];
+}
+
+// first red sweep from x = 0: neighbours are zero
+template <class T>
+__global__ void rb_first_k(Grid g, const T* __restrict__ iD, const T* __restrict__ b, T* __restrict__ xv) {
+    INTERIOR_XYZ
+    xv[I] = (((x + y + z) & 1) == 0) ? b[I] * iD[I] : T(0);
+}
+
+template <class T>
+__global__ void residual_k(Grid g, const T* __restrict__ L, const T* __restrict__ b, const T* __restrict__ xv,
+                           T* __restrict__ r) {
+    INTERIOR_XYZ
+    T dd = T(0);
+    for (int i = 0; i < g.D; ++i) dd -= L[I + i * g.N] + L[I + g.s[i] + i * g.N];
+    r[I] = b[I] - (offdiag(g, L, xv, I, c) + dd * xv[I]);
+}
+
+template <class T>
+__global__ void restrict_k(Grid gc, Grid gf, const T* __restrict__ rf, T* __restrict__ bc) {
+    const Grid& g = gc;
+    INTERIOR_XYZ
+    const int nz = g.D == 3 ? 2 : 1;
+    T s = T(0);
+    for (int k = 0; k < nz; ++k)
+        for (int j = 0; j < 2; ++j)
+            for (int i = 0; i < 2; ++i)
+                s += rf[lin(gf, 2 * c[0] - 1 + i, 2 * c[1] - 1 + j, g.D == 3 ? 2 * c[2] - 1 + k : 0)];
+    bc[I] = s;
+}
+
+template <class T>
+__global__ void prolong_k(Grid gf, Grid gc, const T* __restrict__ xc, T* __restrict__ xf) {
+    const Grid& g = gf;
+    INTERIOR_XYZ
+    const long long P = lin(gc, (c[0] + 1) / 2, (c[1] + 1) / 2, g.D == 3 ? (c[2] + 1) / 2 : 0);
+    xf[I] += xc[P];
+}
+
+// Coarsest level: one block, mean-free right-hand side, nuc symmetric red-black sweeps from zero.
+template <class T>
+__global__ void coarse_k(Grid g, const T* __restrict__ L, const T* __restrict__ iD, T* __restrict__ b,
+                         T* __restrict__ xv, int nuc) {
+    __shared__ double red[1024];
+    const long long total = g.N;
+    double acc = 0.0;
+    long long cnt = 0;
+    for (long long q = threadIdx.x; q < total; q += blockDim.x) {
+        const int c[3] = {int(q % g.n[0]), int((q / g.n[0]) % g.n[1]), int(q / ((long long)g.n[0] * g.n[1]))};
+        if (!is_interior(g, c)) continue;
+        acc += double(b[q]);
+        ++cnt;
+    }
+    red[threadIdx.x] = acc;
+    __syncthreads();
+    for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+        if (threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
+        __syncthreads();
+    }
+    long long ninner = 1;
+    for (int e = 0; e < g.D; ++e) ninner *= (g.n[e] - 2);
+    const T mean = T(red[0] / double(ninner));
+    __syncthreads();
+    for (long long q = threadIdx.x; q < total; q += blockDim.x) {
+        const int c[3] = {int(q % g.n[0]), int((q / g.n[0]) % g.n[1]), int(q / ((long long)g.n[0] * g.n[1]))};
+        if (is_interior(g, c)) b[q] -= mean;
+        xv[q] = T(0);
+    }
+    __syncthreads();
+    for (int it = 0; it < 2 * nuc; ++it) {
+        const int color = (it & 1) ^ ((it >> 1) & 1);   // R B, B R, R B, ...
+        for (long long q = threadIdx.x; q < total; q += blockDim.x) {
+            const int c[3] = {int(q % g.n[0]), int((q / g.n[0]) % g.n[1]), int(q / ((long long)g.n[0] * g.n[1]))};
+            if (!is_interior(g, c) || ((c[0] + c[1] + c[2]) & 1) != color) continue;
+            xv[q] = (b[q] - offdiag(g, L, xv, q, c)) * iD[q];
+        }
+        __syncthreads();
+    }
+}
+
+__global__ void to_f32_k(long long n, const double* __restrict__ a, float* __restrict__ b) {
+    for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < n; q += (long long)gridDim.x * blockDim.x)
+        b[q] = float(a[q]);
+}
+__global__ void to_f64_k(long long n, const float* __restrict__ a, double* __restrict__ b) {
+    for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < n; q += (long long)gridDim.x * blockDim.x)
+        b[q] = double(a[q]);
+}
+
+// ------------------------------------------------------------------ FP64 Krylov kernels
+__device__ __forceinline__ unsigned long long abs_bits(double v) {
+    return (unsigned long long)__double_as_longlong(v) & 0x7FFFFFFFFFFFFFFFull;
+}
+
+// r = z - A x over interior cells, L∞(r) into *linf
+__global__ void true_resid_k(Grid g, const double* __restrict__ L, const double* __restrict__ zz,
+                             const double* __restrict__ xv, double* __restrict__ r, unsigned long long* linf) {
+    __shared__ unsigned long long sm[256];
+    const int t = threadIdx.y * blockDim.x + threadIdx.x;
+    unsigned long long m = 0ull;
+    {
+        const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y;
+        const int z = blockIdx.z;
+        const int c[3] = {x, y, z};
+        if (x < g.n[0] && y < g.n[1] && is_interior(g, c)) {
+            const long long I = lin(g, x, y, z);
+            double dd = 0.0;
+            for (int i = 0; i < g.D; ++i) dd -= L[I + i * g.N] + L[I + g.s[i] + i * g.N];
+            const double v = zz[I] - (offdiag(g, L, xv, I, c) + dd * xv[I]);
+            r[I] = v;
+            m = abs_bits(v);
+        }
+    }
+    sm[t] = m;
+    __syncthreads();
+    for (int w = 128; w > 0; w >>= 1) {
+        if (t < w) sm[t] = sm[t] > sm[t + w] ? sm[t] : sm[t + w];
+        __syncthreads();
+    }
+    if (t == 0) atomicMax(linf, sm[0]);
+}
+
+// q = A p and partial dot p·q
+__global__ void matvec_dot_k(Grid g, const double* __restrict__ L, const double* __restrict__ pv,
+                             double* __restrict__ q, double* __restrict__ partial) {
+    __shared__ double sm[256];
+    const int t = threadIdx.y * blockDim.x + threadIdx.x;
+    double acc = 0.0;
+    {
+        const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y;
+        const int z = blockIdx.z;
+        const int c[3] = {x, y, z};
+        if (x < g.n[0] && y < g.n[1] && is_interior(g, c)) {
+            const long long I = lin(g, x, y, z);
+            double dd = 0.0;
+            for (int i = 0; i < g.D; ++i) dd -= L[I + i * g.N] + L[I + g.s[i] + i * g.N];
+            const double v = offdiag(g, L, pv, I, c) + dd * pv[I];
+            q[I] = v;
+            acc = pv[I] * v;
+        }
+    }
+    sm[t] = acc;
+    __syncthreads();
+    for (int w = 128; w > 0; w >>= 1) {
+        if (t < w) sm[t] += sm[t + w];
+        __syncthreads();
+    }
+    if (t == 0) partial[(blockIdx.z * gridDim.y + blockIdx.y) * gridDim.x + blockIdx.x] = sm[0];
+}
+
+// partial dots s·q and s·r
+__global__ void dot2_k(Grid g, const double* __restrict__ sv, const double* __restrict__ q,
+                       const double* __restrict__ r, double* __restrict__ partial, long long nblocks) {
+    __shared__ double s1[256], s2[256];
+    const int t = threadIdx.y * blockDim.x + threadIdx.x;
+    double a1 = 0.0, a2 = 0.0;
+    {
+        const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y;
+        const int z = blockIdx.z;
+        const int c[3] = {x, y, z};
+        if (x < g.n[0] && y < g.n[1] && is_interior(g, c)) {
+            const long long I = lin(g, x, y, z);
+            a1 = sv[I] * q[I];
+            a2 = sv[I] * r[I];
+        }
+    }
+    s1[t] = a1;
+    s2[t] = a2;
+    __syncthreads();
+    for (int w = 128; w > 0; w >>= 1) {
+        if (t < w) {
+            s1[t] += s1[t + w];
+            s2[t] += s2[t + w];
+        }
+        __syncthreads();
+    }
+    if (t == 0) {
+        const long long b = (blockIdx.z * gridDim.y + blockIdx.y) * gridDim.x + blockIdx.x;
+        partial[b] = s1[0];
+        partial[nblocks + b] = s2[0];
+    }
+}
+
+// fixed-order sum of `n` partials for `k` quantities → out[0..k)
+__global__ void finalize_k(const double* __restrict__ partial, long long n, int k, double* out) {
+    __shared__ double sm[1024];
+    for (int qd = 0; qd < k; ++qd) {
+        double acc = 0.0;
+        for (long long i = threadIdx.x; i < n; i += blockDim.x) acc += partial[qd * n + i];
+        sm[threadIdx.x] = acc;
+        __syncthreads();
+        for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+            if (threadIdx.x < w) sm[threadIdx.x] += sm[threadIdx.x + w];
+            __syncthreads();
+        }
+        if (threadIdx.x == 0) out[qd] = sm[0];
+        __syncthreads();
+    }
+}
+
+__global__ void xpby_k(Grid g, const double* __restrict__ sv, double beta, double* __restrict__ pv) {
+    INTERIOR_XYZ
+    pv[I] = sv[I] + beta * pv[I];
+}
+
+// x += α p ; r -= α q ; L∞(r)
+__global__ void update_k(Grid g, double alpha, const double* __restrict__ pv, const double* __restrict__ q,
+                         double* __restrict__ xv, double* __restrict__ r, unsigned long long* linf) {
+    __shared__ unsigned long long sm[256];
+    const int t = threadIdx.y * blockDim.x + threadIdx.x;
+    unsigned long long m = 0ull;
+    {
+        const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y;
+        const int z = blockIdx.z;
+        const int c[3] = {x, y, z};
+        if (x < g.n[0] && y < g.n[1] && is_interior(g, c)) {
+            const long long I = lin(g, x, y, z);
+            xv[I] += alpha * pv[I];
+            const double v = r[I] - alpha * q[I];
+            r[I] = v;
+            m = abs_bits(v);
+        }
+    }
+    sm[t] = m;
+    __syncthreads();
+    for (int w = 128; w > 0; w >>= 1) {
+        if (t < w) sm[t] = sm[t] > sm[t + w] ? sm[t] : sm[t + w];
+        __syncthreads();
+    }
+    if (t == 0) atomicMax(linf, sm[0]);
+}
+
+// periodic ghosts of a scalar (WaterLily perBC!)
+__global__ void perbc_k(Grid g, double* a) {
+    const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y;
+    const int z = blockIdx.z;
+    if (x >= g.n[0] || y >= g.n[1]) return;
+    int c[3] = {x, y, z};
+    bool any = false;
+    for (int e = 0; e < g.D; ++e)
+        if (g.isper(e) && (c[e] == 0 || c[e] == g.n[e] - 1)) {
+            c[e] = bc_src(g, e, c[e]);
+            any = true;
+        }
+    if (!any) return;
+    // only read positions that no thread writes: the mapped position must have
+    // no periodic ghost coordinate left (it has none after mapping)
+    a[lin(g, x, y, z)] = a[lin3(g, c)];
+}
+
+template <class T>
+__global__ void zero_k(long long n, T* a) {
+    for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < n; q += (long long)gridDim.x * blockDim.x)
+        a[q] = T(0);
+}
+
+}  // namespace
+
+// ------------------------------------------------------------------ host side
+
+template <class T>
+static cudaError_t vcycle(PoissonMG* mg, int l, cudaStream_t st, int nu1, int nu2, int nuc) {
+    auto& L = mg->lev[l];
+    T* x = L.template x_<T>();
+    T* b = L.template b_<T>();
+    T* r = L.template r_<T>();
+    const T* Lc = L.template L_<T>();
+    const T* iD = L.template iD_<T>();
+    if (l == mg->nlev - 1) {
+        coarse_k<T><<<1, 1024, 0, st>>>(L.g, Lc, iD, b, x, nuc);
+        return cudaGetLastError();
+    }
+    rb_first_k<T><<<grd(L.g), blk(), 0, st>>>(L.g, iD, b, x);
+    rbgs_k<T><<<grd(L.g), blk(), 0, st>>>(L.g, Lc, iD, b, x, 1);
+    for (int k = 1; k < nu1; ++k) {
+        rbgs_k<T><<<grd(L.g), blk(), 0, st>>>(L.g, Lc, iD, b, x, 0);
+        rbgs_k<T><<<grd(L.g), blk(), 0, st>>>(L.g, Lc, iD, b, x, 1);
+    }
+    residual_k<T><<<grd(L.g), blk(), 0, st>>>(L.g, Lc, b, x, r);
+    auto& C = mg->lev[l + 1];
+    restrict_k<T><<<grd(C.g), blk(), 0, st>>>(C.g, L.g, r, C.template b_<T>());
+    cudaError_t e = vcycle<T>(mg, l + 1, st, nu1, nu2, nuc);
+    if (e != cudaSuccess) return e;
+    prolong_k<T><<<grd(L.g), blk(), 0, st>>>(L.g, C.g, C.template x_<T>(), x);
+    for (int k = 0; k < nu2; ++k) {
+        rbgs_k<T><<<grd(L.g), blk(), 0, st>>>(L.g, Lc, iD, b, x, 1);
+        rbgs_k<T><<<grd(L.g), blk(), 0, st>>>(L.g, Lc, iD, b, x, 0);
+    }
+    return cudaGetLastError();
+}
+
+int mg_create(ia_handle* h) {
+    PoissonMG* mg = new PoissonMG();
+    h->mg = mg;
+    const Grid& g0 = h->g;
+    long long Nint[3] = {g0.n[0] - 2, g0.n[1] - 2, g0.D == 3 ? g0.n[2] - 2 : 1};
+    const bool mixed = h->cfg.poisson_mode == IA_POISSON_MIXED;
+    int nl = 0;
+    while (nl < MG_MAX_LEVELS) {
+        int64_t N[3] = {Nint[0], Nint[1], Nint[2]};
+        MGLevel& L = mg->lev[nl];
+        L.g = make_grid(g0.D, g0.per, N);
+        const size_t n = (size_t)L.g.N;
+        cudaError_t e = cudaSuccess;
+        // FP64 levels always exist for level 0 (fine operator copies) and for the FP64 mode
+        if (!mixed) {
+            e = e ? e : cudaMalloc(&L.x, 8 * n);
+            e = e ? e : cudaMalloc(&L.b, 8 * n);
+            e = e ? e : cudaMalloc(&L.r, 8 * n);
+            e = e ? e : cudaMalloc(&L.L, 8 * n * g0.D);
+            e = e ? e : cudaMalloc(&L.iD, 8 * n);
+            if (!e) {
+                cudaMemset(L.x, 0, 8 * n);
+                cudaMemset(L.b, 0, 8 * n);
+                cudaMemset(L.r, 0, 8 * n);
+                cudaMemset(L.iD, 0, 8 * n);
+                cudaMemset(L.L, 0, 8 * n * g0.D);
+            }
+        } else {
+            e = e ? e : cudaMalloc(&L.x32, 4 * n);
+            e = e ? e : cudaMalloc(&L.b32, 4 * n);
+            e = e ? e : cudaMalloc(&L.r32, 4 * n);
+            e = e ? e : cudaMalloc(&L.L32, 4 * n * g0.D);
+            e = e ? e : cudaMalloc(&L.iD32, 4 * n);
+            if (!e) {
+                cudaMemset(L.x32, 0, 4 * n);
+                cudaMemset(L.b32, 0, 4 * n);
+                cudaMemset(L.r32, 0, 4 * n);
+                cudaMemset(L.iD32, 0, 4 * n);
+                cudaMemset(L.L32, 0, 4 * n * g0.D);
+            }
+        }
+        if (e != cudaSuccess) return IA_ERR_CUDA;
+        ++nl;
+        bool can = true;
+        for (int d = 0; d < g0.D; ++d)
+            if (Nint[d] % 2 != 0 || Nint[d] < 4) can = false;
+        long long cells = 1;
+        for (int d = 0; d < g0.D; ++d) cells *= Nint[d];
+        if (!can || cells <= 512) break;
+        for (int d = 0; d < g0.D; ++d) Nint[d] /= 2;
+    }
+    mg->nlev = nl;
+    const size_t N = (size_t)g0.N;
+    cudaError_t e = cudaSuccess;
+    e = e ? e : cudaMalloc(&mg->r, 8 * N);
+    e = e ? e : cudaMalloc(&mg->s, 8 * N);
+    e = e ? e : cudaMalloc(&mg->p, 8 * N);
+    e = e ? e : cudaMalloc(&mg->q, 8 * N);
+    const dim3 gb = grd(g0);
+    mg->nblocks = (long long)gb.x * gb.y * gb.z;
+    e = e ? e : cudaMalloc(&mg->partial, 8 * 2 * (size_t)mg->nblocks);
+    e = e ? e : cudaMalloc(&mg->dsc, 8 * 16);
+    e = e ? e : cudaMallocHost(&mg->hsc, 8 * 16);
+    if (e != cudaSuccess) return IA_ERR_CUDA;
+    cudaMemset(mg->r, 0, 8 * N);
+    cudaMemset(mg->s, 0, 8 * N);
+    cudaMemset(mg->p, 0, 8 * N);
+    cudaMemset(mg->q, 0, 8 * N);
+    mg->nu1 = 2;
+    mg->nu2 = 2;
+    mg->nuc = 16;
+    return IA_OK;
+}
+
+void mg_destroy(ia_handle* h) {
+    PoissonMG* mg = h->mg;
+    if (!mg) return;
+    for (int l = 0; l < MG_MAX_LEVELS; ++l) {
+        MGLevel& L = mg->lev[l];
+        cudaFree(L.x); cudaFree(L.b); cudaFree(L.r); cudaFree(L.L); cudaFree(L.iD);
+        cudaFree(L.x32); cudaFree(L.b32); cudaFree(L.r32); cudaFree(L.L32); cudaFree(L.iD32);
+    }
+    cudaFree(mg->r); cudaFree(mg->s); cudaFree(mg->p); cudaFree(mg->q);
+    cudaFree(mg->partial); cudaFree(mg->dsc);
+    if (mg->hsc) cudaFreeHost(mg->hsc);
+    delete mg;
+    h->mg = nullptr;
+}
+
+// build every level's operator from the fine coefficients L0 (μ₀, FP64)
+static cudaError_t mg_setup(ia_handle* h, const double* L0) {
+    PoissonMG* mg = h->mg;
+    cudaStream_t st = h->stream;
+    const bool mixed = h->cfg.poisson_mode == IA_POISSON_MIXED;
+    MGLevel& F = mg->lev[0];
+    const long long nv = F.g.N * F.g.D;
+    if (!mixed) {
+        cudaMemcpyAsync(F.L, L0, 8 * nv, cudaMemcpyDeviceToDevice, st);
+        set_diag_k<double><<<grd(F.g), blk(), 0, st>>>(F.g, F.L, F.iD);
+        for (int l = 1; l < mg->nlev; ++l) {
+            restrict_L_k<double><<<grd(mg->lev[l].g), blk(), 0, st>>>(mg->lev[l].g, mg->lev[l - 1].g,
+                                                                       mg->lev[l - 1].L, mg->lev[l].L);
+            set_diag_k<double><<<grd(mg->lev[l].g), blk(), 0, st>>>(mg->lev[l].g, mg->lev[l].L, mg->lev[l].iD);
+        }
+    } else {
+        to_f32_k<<<1216, 256, 0, st>>>(nv, L0, F.L32);
+        set_diag_k<float><<<grd(F.g), blk(), 0, st>>>(F.g, F.L32, F.iD32);
+        for (int l = 1; l < mg->nlev; ++l) {
+            restrict_L_k<float><<<grd(mg->lev[l].g), blk(), 0, st>>>(mg->lev[l].g, mg->lev[l - 1].g,
+                                                                      mg->lev[l - 1].L32, mg->lev[l].L32);
+            set_diag_k<float><<<grd(mg->lev[l].g), blk(), 0, st>>>(mg->lev[l].g, mg->lev[l].L32, mg->lev[l].iD32);
+        }
+    }
+    return cudaGetLastError();
+}
+
+// s = M r (one V-cycle)
+static cudaError_t mg_precondition(ia_handle* h) {
+    PoissonMG* mg = h->mg;
+    cudaStream_t st = h->stream;
+    MGLevel& F = mg->lev[0];
+    const long long N = F.g.N;
+    cudaError_t e;
+    if (h->cfg.poisson_mode == IA_POISSON_MIXED) {
+        int tk = timing_begin(h, TK_MG_TRANSFER);
+        to_f32_k<<<1216, 256, 0, st>>>(N, mg->r, F.b32);
+        timing_end(h, tk);
+        tk = timing_begin(h, TK_MG_SMOOTH);
+        e = vcycle<float>(mg, 0, st, mg->nu1, mg->nu2, mg->nuc);
+        timing_end(h, tk);
+        if (e != cudaSuccess) return e;
+        to_f64_k<<<1216, 256, 0, st>>>(N, F.x32, mg->s);
+    } else {
+        cudaMemcpyAsync(F.b, mg->r, 8 * N, cudaMemcpyDeviceToDevice, st);
+        int tk = timing_begin(h, TK_MG_SMOOTH);
+        e = vcycle<double>(mg, 0, st, mg->nu1, mg->nu2, mg->nuc);
+        timing_end(h, tk);
+        if (e != cudaSuccess) return e;
+        cudaMemcpyAsync(mg->s, F.x, 8 * N, cudaMemcpyDeviceToDevice, st);
+    }
+    return cudaGetLastError();
+}
+
+static double read_linf(ia_handle* h, unsigned long long* dlinf) {
+    unsigned long long v = 0;
+    cudaMemcpyAsync(&h->mg->hsc[0], dlinf, 8, cudaMemcpyDeviceToHost, h->stream);
+    cudaStreamSynchronize(h->stream);
+    std::memcpy(&v, &h->mg->hsc[0], 8);
+    double d;
+    std::memcpy(&d, &v, 8);
+    return d;
+}
+
+// Solve A x = z to L∞(z - A x) <= tol (x holds the initial guess); L = μ₀.
+int poisson_solve(ia_handle* h, double* xv, const double* zz, const double* L, double tol, int itmx, int* iters,
+                  double* resid) {
+    PoissonMG* mg = h->mg;
+    if (!mg) return IA_ERR_INVALID;
+    cudaStream_t st = h->stream;
+    const Grid& g = h->g;
+    const dim3 gb = grd(g);
+    if (mg_setup(h, L) != cudaSuccess) return IA_ERR_CUDA;
+    unsigned long long* dlinf = reinterpret_cast<unsigned long long*>(mg->dsc + 8);
+    double* dots = mg->dsc;
+    cudaMemsetAsync(dlinf, 0, 8, st);
+    int tk = timing_begin(h, TK_KRYLOV);
+    true_resid_k<<<gb, blk(), 0, st>>>(g, L, zz, xv, mg->r, dlinf);
+    timing_end(h, tk);
+    double res = read_linf(h, dlinf);
+    int it = 0;
+    double rho_prev = 0.0, alpha_prev = 0.0;
+    while (!(res <= tol) && it < itmx) {
+        if (mg_precondition(h) != cudaSuccess) return IA_ERR_CUDA;
+        tk = timing_begin(h, TK_KRYLOV);
+        dot2_k<<<gb, blk(), 0, st>>>(g, mg->s, mg->q, mg->r, mg->partial, mg->nblocks);
+        finalize_k<<<1, 1024, 0, st>>>(mg->partial, mg->nblocks, 2, dots);
+        timing_end(h, tk);
+        cudaMemcpyAsync(mg->hsc + 2, dots, 16, cudaMemcpyDeviceToHost, st);
+        if (cudaStreamSynchronize(st) != cudaSuccess) return IA_ERR_CUDA;
+        const double sq = mg->hsc[2], sr = mg->hsc[3];
+        // flexible CG: β = s_k·(r_k - r_{k-1}) / (s_{k-1}·r_{k-1}) with r_k - r_{k-1} = -α q_{k-1}
+        const double beta = (it == 0) ? 0.0 : (-alpha_prev * sq) / rho_prev;
+        const double rho = sr;
+        tk = timing_begin(h, TK_KRYLOV);
+        xpby_k<<<gb, blk(), 0, st>>>(g, mg->s, beta, mg->p);
+        matvec_dot_k<<<gb, blk(), 0, st>>>(g, L, mg->p, mg->q, mg->partial);
+        finalize_k<<<1, 1024, 0, st>>>(mg->partial, mg->nblocks, 1, dots);
+        timing_end(h, tk);
+        cudaMemcpyAsync(mg->hsc + 2, dots, 8, cudaMemcpyDeviceToHost, st);
+        if (cudaStreamSynchronize(st) != cudaSuccess) return IA_ERR_CUDA;
+        const double pq = mg->hsc[2];
+        if (!(pq != 0.0) || !std::isfinite(pq)) break;
+        const double alpha = rho / pq;
+        cudaMemsetAsync(dlinf, 0, 8, st);
+        tk = timing_begin(h, TK_KRYLOV);
+        update_k<<<gb, blk(), 0, st>>>(g, alpha, mg->p, mg->q, xv, mg->r, dlinf);
+        timing_end(h, tk);
+        res = read_linf(h, dlinf);
+        rho_prev = rho;
+        alpha_prev = alpha;
+        ++it;
+    }
+    perbc_k<<<gb, blk(), 0, st>>>(g, xv);
+    if (cudaGetLastError() != cudaSuccess) return IA_ERR_CUDA;
+    *iters = it;
+    *resid = res;
+    return (res <= tol) ? IA_OK : IA_WARN_NOT_CONVERGED;
+}
+
+}  // namespace ia

@@ -1,0 +1,54 @@
+// Multigrid hierarchy and Krylov state of the pressure solve (poisson.cu).
+#pragma once
+#include <cuda_runtime.h>
+
+#include "ia_core.cuh"
+
+struct ia_handle;
+
+namespace ia {
+
+constexpr int MG_MAX_LEVELS = 12;
+
+struct MGLevel {
+    Grid g;
+    // FP64 operator and vectors (IA_POISSON_FP64)
+    double *x = nullptr, *b = nullptr, *r = nullptr, *L = nullptr, *iD = nullptr;
+    // FP32 operator and vectors (IA_POISSON_MIXED)
+    float *x32 = nullptr, *b32 = nullptr, *r32 = nullptr, *L32 = nullptr, *iD32 = nullptr;
+    template <class T> T* x_();
+    template <class T> T* b_();
+    template <class T> T* r_();
+    template <class T> T* L_();
+    template <class T> T* iD_();
+};
+template <> inline double* MGLevel::x_<double>() { return x; }
+template <> inline double* MGLevel::b_<double>() { return b; }
+template <> inline double* MGLevel::r_<double>() { return r; }
+template <> inline double* MGLevel::L_<double>() { return L; }
+template <> inline double* MGLevel::iD_<double>() { return iD; }
+template <> inline float* MGLevel::x_<float>() { return x32; }
+template <> inline float* MGLevel::b_<float>() { return b32; }
+template <> inline float* MGLevel::r_<float>() { return r32; }
+template <> inline float* MGLevel::L_<float>() { return L32; }
+template <> inline float* MGLevel::iD_<float>() { return iD32; }
+
+}  // namespace ia
+
+struct PoissonMG {
+    int nlev = 0;
+    ia::MGLevel lev[ia::MG_MAX_LEVELS];
+    double *r = nullptr, *s = nullptr, *p = nullptr, *q = nullptr;   // fine-level Krylov vectors (FP64)
+    double* partial = nullptr;                                        // per-block dot partials
+    long long nblocks = 0;
+    double* dsc = nullptr;                                            // device scalars
+    double* hsc = nullptr;                                            // pinned host scalars
+    int nu1 = 2, nu2 = 2, nuc = 16;
+};
+
+namespace ia {
+int mg_create(ia_handle* h);
+void mg_destroy(ia_handle* h);
+int poisson_solve(ia_handle* h, double* x, const double* z, const double* L, double tol, int itmx, int* iters,
+                  double* resid);
+}  // namespace ia

@@ -1,9 +1,10 @@
 // Direction-split conservative VOF advection (InterfaceAdvection.jl
 // src/advection.jl:17-137 with src/normalEstimation.jl and src/PLIC.jl).
 //
-// One sweep along d maps f_in -> f_out (ping-pong buffers: the update of a
-// cell reads f up to two cells away along d, so it cannot run in place).  A
-// sweep is three kernels:
+// One sweep along d updates f in place, like the reference.  Only interface
+// cells change; their new values are staged in a compact buffer and written
+// back after every read of the old field has finished.  A sweep is four
+// kernels:
 //
 //  * vof_bulk — one thread per cell of the ghost-inclusive box.  A cell whose
 //    three cells along d are all full or all empty, equal to its c̄, and whose
@@ -19,11 +20,12 @@
 //    and cached; the face's mass flux ρuf.
 //  * vof_cells — one thread per listed cell: the conservative update with the
 //    dilation term from the two face fluxes, the fill-error status,
-//    cleanWisp!.
+//    cleanWisp!, staged in vals[k].
+//  * vof_scatter — f[list[k]] = vals[k].
 //
-// Ghost cells are written in the same pass with the value of their
-// boundary-condition source cell, so f_out leaves the sweep with BCf! applied
-// (src/VOFutil.jl:64-75) and the next sweep reads valid ghosts.
+// Ghost cells take the value of their boundary-condition source cell in the
+// same sweep, so f leaves the sweep with BCf! applied (src/VOFutil.jl:64-75)
+// and the next sweep reads valid ghosts.
 #include <cuda_runtime.h>
 
 #include "ia_core.cuh"
@@ -107,6 +109,35 @@ __device__ __forceinline__ bool face_simple(const SweepArgs& a, long long K, int
     return false;
 }
 
+// Mass flux ρuf of face K when its donor is full, empty or a zero-gradient
+// ghost: with s = u1 + u2 and δl = s·δt/2 the reference's δl λρ + (1-λρ) fᶠ
+// is δl for a full donor and δl λρ for an empty one (two FP64 operations;
+// the products are re-associated, a relative change below 1e-15).  Returns
+// false when the donor needs reconstruction.
+__device__ __forceinline__ bool face_mass_simple(const SweepArgs& a, long long K, int kd, double& m) {
+    const long long sd = a.g.s[a.d];
+    const double s = a.u1[K] + a.u2[K];
+    const unsigned long long sb = bits(s);
+    if ((sb & ABS_MASK) == 0ull) {   // δl == 0: ρuf stays 0
+        m = 0.0;
+        return true;
+    }
+    const bool pos = !(sb >> 63);
+    const long long C = pos ? K - sd : K;
+    const int cd = pos ? kd - 1 : kd;
+    const double fC = a.fin[C];
+    const unsigned long long fb = bits(fC);
+    if (fb == ONE_BITS) { m = a.h * s; return true; }
+    if (fb == 0ull) { m = a.hl * s; return true; }
+    const bool zg_ghost = ((cd == 0) || (cd == a.g.n[a.d] - 1)) && !a.g.isper(a.d);
+    if (zg_ghost || fC == 0.0 || fC == 1.0) {
+        const double dl = a.h * s;
+        m = dl * a.lrho + a.one_m_lrho * (fC * dl);
+        return true;
+    }
+    return false;
+}
+
 template <int D>
 __device__ __forceinline__ void coords_of(const Grid& g, long long O, int c[3]) {
     c[0] = int(O % g.n[0]);
@@ -166,11 +197,14 @@ __global__ void __launch_bounds__(256) vof_bulk(SweepArgs a) {
                           abs_le(bits(a.u1[S]), a.ulim) && abs_le(bits(a.u1[S + sd]), a.ulim) &&
                           abs_le(bits(a.u2[S]), a.ulim) && abs_le(bits(a.u2[S + sd]), a.ulim);
         need_cell = !bulk;
-        if (bulk) a.fout[O] = (bc == ONE_BITS) ? 1.0 : 0.0;
+        // in place a bulk cell keeps its value and only a stale ghost copy needs a write;
+        // out of place (the coupled step keeps f_old) every bulk cell is written
+        if (bulk && (a.fin != a.fout || ((O != S) && bits(a.fin[O]) != bc)))
+            a.fout[O] = (bc == ONE_BITS) ? 1.0 : 0.0;
         if (in_face_range<D>(g, a.d, c)) {
-            double dl, F;
-            if (face_simple(a, O, c[a.d], dl, F)) {
-                if (a.rhouf_d) a.rhouf_d[O] = ((bits(dl) & ABS_MASK) == 0ull) ? 0.0 : mass_flux(dl, F, a.lrho);
+            double m;
+            if (face_mass_simple(a, O, c[a.d], m)) {
+                if (a.rhouf_d) a.rhouf_d[O] = m;
             } else {
                 need_face = true;
             }
@@ -234,8 +268,14 @@ __global__ void __launch_bounds__(128) vof_cells(SweepArgs a) {
         }
         // cleanWisp! (src/VOFutil.jl:127-136)
         v = (v < a.tol_clean) ? 0.0 : ((v > 1.0 - a.tol_clean) ? 1.0 : v);
-        a.fout[O] = v;
+        a.vals[k] = v;
     }
+}
+
+__global__ void __launch_bounds__(256) vof_scatter(SweepArgs a) {
+    const unsigned int count = *a.list_count;
+    for (unsigned int k = blockIdx.x * blockDim.x + threadIdx.x; k < count; k += gridDim.x * blockDim.x)
+        a.fout[a.list[k]] = a.vals[k];
 }
 
 template <int D, bool FIRST>
@@ -256,6 +296,11 @@ cudaError_t vof_sweep_bulk(const SweepArgs& a, cudaStream_t st) {
 cudaError_t vof_sweep_faces(const SweepArgs& a, cudaStream_t st, int list_blocks) {
     if (a.g.D == 2) vof_faces<2><<<list_blocks, 128, 0, st>>>(a);
     else vof_faces<3><<<list_blocks, 128, 0, st>>>(a);
+    return cudaGetLastError();
+}
+
+cudaError_t vof_sweep_scatter(const SweepArgs& a, cudaStream_t st, int list_blocks) {
+    vof_scatter<<<list_blocks / 2, 256, 0, st>>>(a);
     return cudaGetLastError();
 }
 

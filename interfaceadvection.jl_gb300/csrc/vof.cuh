@@ -12,8 +12,8 @@ struct SweepArgs {
     int d;                            // sweep direction (0-based)
     int scheme;                       // IA_NORMAL_*
     bool first;                       // first sweep of the call: computes and writes c̄
-    const double* __restrict__ fin;   // fractions before the sweep (ghosts valid)
-    double* __restrict__ fout;        // fractions after the sweep (ghosts written)
+    const double* fin;                // fractions before the sweep (ghosts valid)
+    double* fout;                     // fractions after the sweep: the same array (in place)
     const double* __restrict__ u1;    // component d of the first velocity field
     const double* __restrict__ u2;    // component d of the second velocity field
     int8_t* cbar;                     // c̄: written when first, read otherwise
@@ -21,6 +21,8 @@ struct SweepArgs {
     double h;                         // δt / 2
     double dt;                        // δt of the sweep
     double lrho;                      // λρ
+    double one_m_lrho;                // 1 - λρ
+    double hl;                        // δt/2 · λρ
     double tol_rep;                   // reportFillError tolerance
     double tol_clean;                 // cleanWisp! tolerance (10 eps)
     unsigned long long ulim;          // bit pattern of 1/(2δt): fast-path velocity bound
@@ -29,12 +31,14 @@ struct SweepArgs {
     unsigned int* flist;              // faces whose donor needs reconstruction
     unsigned int* flist_count;
     double* flux;                     // cached face fluxes of listed faces
+    double* vals;                     // staged new values of listed cells
     DevStatus* st;
 };
 
 cudaError_t vof_sweep_bulk(const SweepArgs& a, cudaStream_t st);
 cudaError_t vof_sweep_faces(const SweepArgs& a, cudaStream_t st, int list_blocks);
 cudaError_t vof_sweep_cells(const SweepArgs& a, cudaStream_t st, int list_blocks);
+cudaError_t vof_sweep_scatter(const SweepArgs& a, cudaStream_t st, int list_blocks);
 
 // applyVOF! interior + BCf! ghosts
 cudaError_t apply_vof(const Grid& g, const double* sdf, double* f, double* alpha, double* nhat, cudaStream_t st);

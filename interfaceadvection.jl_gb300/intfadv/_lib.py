@@ -67,6 +67,14 @@ _SIGS = {
     "ia_mass": (C.c_int, [C.c_void_p, C.c_void_p, C.POINTER(C.c_double)]),
     "ia_error_string": (C.c_char_p, [C.c_int]),
     "ia_timing": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p, C.c_int32]),
+    "ia_mom_step": (C.c_int, [C.c_void_p, C.c_double, C.c_int64, C.c_double, C.POINTER(Status)]),
+    "ia_cfl": (C.c_int, [C.c_void_p, C.POINTER(C.c_double)]),
+    "ia_bc_velocity": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "ia_poisson_solve": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_double, C.c_int32,
+                                   C.POINTER(C.c_int32), C.POINTER(C.c_double)]),
+    "ia_project": (C.c_int, [C.c_void_p, C.c_void_p, C.c_double, C.POINTER(C.c_int32), C.POINTER(C.c_double)]),
+    "ia_advect_momentum": (C.c_int, [C.c_void_p] * 5 + [C.c_double, C.c_int64, C.POINTER(Status)]),
+    "ia_visc_surften": (C.c_int, [C.c_void_p, C.c_void_p]),
 }
 
 _lib = None

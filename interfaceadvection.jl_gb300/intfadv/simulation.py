@@ -1,0 +1,109 @@
+"""TwoPhaseSimulation, sim_step!, MPFMomStep!, MPCFL — host mirror of
+src/InterfaceAdvection.jl:64-107 and src/flow.jl:60-109, 262-281.
+
+The Flow and cVOF fields live on the device in the reference layout and are
+bound to one library handle; every compute call is a C-ABI call.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import math
+import warnings
+
+import torch
+
+from . import _lib
+from .core import FP64, Flow, Handle, _raise_or_warn, apply_vof, cVOF, make_config
+from .fields import ptr
+
+
+class NoBody:
+    """Placeholder of WaterLily.NoBody (BDIM bodies are not supported by the reference's step either)."""
+
+
+class TwoPhaseSimulation:
+    """TwoPhaseSimulation(dims, u_BC, L; U, Δt, ν, g, u0, perdir, λμ, λρ, η, InterfaceSDF, λ,
+    normalScheme) — src/InterfaceAdvection.jl:64-85.
+
+    ``u0(i, x)`` initialises the face velocities (0-based component, coordinate tensors at
+    WaterLily loc(i,I)); ``g`` is a constant gravity vector; ``InterfaceSDF`` a vectorised
+    SDF (dark fluid where negative).  ``poisson`` selects "fp64" (FP64 V-cycles) or "mixed"
+    (FP32 V-cycles inside FP64 flexible CG); ``poisson_tol`` is the L∞ residual of the
+    dt-scaled pressure system (the reference passes tol=1e-4 to WaterLily's solver!).
+    """
+
+    def __init__(self, dims, u_BC, L, *, U=None, Δt=0.25, ν=0.0, g=None, u0=None, perdir=(), exitBC=False,
+                 λμ=1e-2, λρ=1e-3, η=None, InterfaceSDF=None, λ="Koren", normalScheme="WH", T=FP64,
+                 poisson="fp64", poisson_tol=1e-4, poisson_itmx=200, device="cuda", body=None, ϵ=1):
+        if T != FP64:
+            raise NotImplementedError("the GB300 path computes in FP64 (Poisson V-cycles optionally FP32)")
+        if exitBC:
+            raise NotImplementedError("exitBC is not supported")
+        if body is not None and not isinstance(body, NoBody):
+            raise NotImplementedError("BDIM bodies are not supported (the reference's sim_step! ignores them)")
+        dims = tuple(int(n) for n in dims)
+        self.L = float(L)
+        self.U = math.sqrt(sum(float(x) ** 2 for x in u_BC)) if U is None else float(U)
+        self.ϵ = ϵ
+        self.body = NoBody()
+        self.flow = Flow(dims, u_BC, Δt=Δt, ν=ν, g=g, u0fn=u0, perdir=perdir, device=device)
+        cfg = make_config(dims, perdir=perdir, lrho=λρ, lmu=λμ, mu=(None if ν == 0 else ν),
+                          eta=(None if (η is None or η == 0) else η), nu=ν, g=g, uBC=u_BC,
+                          normalScheme=normalScheme, limiter=λ, poisson=poisson, poisson_tol=poisson_tol,
+                          poisson_itmx=poisson_itmx)
+        # cVOF(dims; μ=flow.ν, ...) (src/InterfaceAdvection.jl:78)
+        self.intf = cVOF(dims, device=device, InterfaceSDF=InterfaceSDF, mu=ν, lmu=λμ, lrho=λρ, eta=η,
+                         normalScheme=normalScheme, perdir=perdir, _config=cfg)
+        self.handle: Handle = self.intf.handle
+        fl, it = self.flow, self.intf
+        self.handle.bind(u=fl.u, u0=fl.u0, force=fl.f, sigma=fl.sigma, p=fl.p, mu0=fl.mu0, f=it.f, f0=it.f0,
+                         alpha=it.alpha, nhat=it.nhat, fF=it.fF, rhou=it.rhou, rhouf=it.rhouf, drho=it.drho,
+                         cbar=it.cbar)
+        _lib.check(self.handle.call("ia_bc_velocity", ptr(fl.u)), "ia_bc_velocity")   # Flow: BC!(u)
+        fl.u0.copy_(fl.u)
+        fl.Δt[-1] = min(fl.Δt[-1], MPCFL(self))                                       # :81
+        self.pois = None
+        self.last_status = None
+
+    # property forwarding of the Julia wrapper (src/InterfaceAdvection.jl:86-87)
+    @property
+    def sim(self):
+        return self
+
+    def sim_time(self) -> float:
+        return sum(self.flow.Δt[:-1]) * (self.U / self.L if self.L else 1.0)
+
+
+def MPCFL(sim) -> float:
+    """MPCFL(flow, intf) — src/flow.jl:262-281."""
+    out = C.c_double()
+    _lib.check(sim.handle.call("ia_cfl", C.byref(out)), "ia_cfl")
+    return out.value
+
+
+def MPFMomStep(sim, δt=None) -> _lib.Status:
+    """MPFMomStep!(flow, pois, intf, body; δt=last(Δt)) — src/flow.jl:60-109 (push!(Δt, ...) included)."""
+    fl = sim.flow
+    dt = fl.Δt[-1] if δt is None else float(δt)
+    st = _lib.Status()
+    code = sim.handle.call("ia_mom_step", C.c_double(dt), C.c_int64(len(fl.Δt)), C.c_double(sum(fl.Δt)),
+                           C.byref(st))
+    sim.last_status = st
+    if code in (_lib.IA_ERR_NAN, _lib.IA_ERR_DIVERGENCE):
+        _raise_or_warn(st, "ia_mom_step")
+    _lib.check(code, "ia_mom_step", allow=(_lib.IA_OK, _lib.IA_WARN_FILL, _lib.IA_WARN_NOT_CONVERGED))
+    if code == _lib.IA_WARN_FILL:
+        _raise_or_warn(st, "ia_mom_step")
+    fl.Δt.append(st.dt_next)
+    return st
+
+
+def sim_step(sim, *, remeasure=False, udf=None):
+    """sim_step!(sim::TwoPhaseSimulation; remeasure, udf) — src/InterfaceAdvection.jl:100-103."""
+    if udf is not None:
+        raise NotImplementedError("udf is not supported")
+    return MPFMomStep(sim)
+
+
+def sim_info(sim):
+    print(f"    tU/L={sim.sim_time():10.6f}, ΔtU/L={sim.flow.Δt[-1] * sim.U / sim.L:.10f}")
