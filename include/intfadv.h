@@ -136,6 +136,25 @@ int ia_bind_fields(ia_handle* h, const ia_fields* fields);
 int ia_advect_vof(ia_handle* h, double* f, const double* u1, const double* u2,
                   double dt, int64_t n_dt, ia_status* status);
 
+/* Allocation-free variant of ia_advect_vof for callers that cannot let a
+ * library allocate device memory at run time (frameworks that reserve the
+ * device memory up front for their own pool, time-stepping loops that forbid
+ * the device-wide synchronisation of cudaMalloc/cudaFree after set-up).  It has
+ * no counterpart in the reference.  It needs no handle: the caller passes the
+ * configuration, a cudaStream_t (NULL = legacy default), the fields (f updated
+ * in place, c̄ written, ρuf written when not NULL) and gets the same results as
+ * ia_advect_vof.  Its scratch is one fixed-size device array inside the library
+ * (24 MiB + 1 KiB, held by every GPU that loads the library until exit):
+ * grids above IA_NOALLOC_MAX_CELLS ghost-inclusive cells return
+ * IA_ERR_TOO_LARGE; every call reuses the array (status and counters are
+ * cleared at the start of each call), so calls whose GPU work overlaps race and
+ * must be serialised by the caller; the first call on a device looks up the
+ * array's address and should come before any stream capture on that device. */
+#define IA_NOALLOC_MAX_CELLS 1048576
+int ia_advect_vof_noalloc(const ia_config* cfg, void* stream, double* f, const double* u1,
+                          const double* u2, double dt, int64_t n_dt, int8_t* cbar, double* rhouf,
+                          ia_status* status);
+
 /* reconstructInterface!(f, α, n̂, normalScheme) — src/normalEstimation.jl:10-28,
  * including BCVOF! src/VOFutil.jl:44-55 (f ghosts updated in place). */
 int ia_reconstruct(ia_handle* h, double* f, double* alpha, double* nhat);

@@ -75,6 +75,8 @@ _SIGS = {
     "ia_project": (C.c_int, [C.c_void_p, C.c_void_p, C.c_double, C.POINTER(C.c_int32), C.POINTER(C.c_double)]),
     "ia_advect_momentum": (C.c_int, [C.c_void_p] * 5 + [C.c_double, C.c_int64, C.POINTER(Status)]),
     "ia_visc_surften": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "ia_advect_vof_noalloc": (C.c_int, [C.POINTER(Config), C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                        C.c_double, C.c_int64, C.c_void_p, C.c_void_p, C.POINTER(Status)]),
 }
 
 _lib = None
