@@ -220,6 +220,10 @@ int ia_mass(ia_handle* h, const double* f, double* mass_out);
  * the totals and switches recording on (1) or off (0). */
 int ia_timing(ia_handle* h, int32_t enable, double* ms_out, int64_t* launches_out, int32_t n);
 
+/* Number of CUDA kernels this library has launched in the process so far
+ * (instrumentation, no reference counterpart; used for launch accounting). */
+int64_t ia_launch_count(void);
+
 const char* ia_error_string(int code);
 
 #ifdef __cplusplus

@@ -2,6 +2,7 @@
 // cycle, field binding, the VOF entry points and status read-back.
 #include <cuda_runtime.h>
 
+#include <atomic>
 #include <cmath>
 #include <cstring>
 #include <new>
@@ -26,12 +27,16 @@ __global__ void status_reset_k(DevStatus* s) {
 
 namespace ia {
 
+static std::atomic<long long> g_launches{0};
+void note_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
+long long launch_count() { return g_launches.load(std::memory_order_relaxed); }
+
 int cuda_fail(cudaError_t e) {
     return e == cudaSuccess ? IA_OK : IA_ERR_CUDA;
 }
 
 int status_reset(ia_handle* h) {
-    status_reset_k<<<1, 1, 0, h->stream>>>(h->dst);
+    { status_reset_k<<<1, 1, 0, h->stream>>>(h->dst); ia::note_launch(); }
     return cuda_fail(cudaGetLastError());
 }
 
@@ -200,6 +205,8 @@ int ia_timing(ia_handle* h, int32_t enable, double* ms_out, int64_t* launches_ou
     }
     return IA_OK;
 }
+
+int64_t ia_launch_count(void) { return (int64_t)launch_count(); }
 
 const char* ia_error_string(int code) {
     switch (code) {

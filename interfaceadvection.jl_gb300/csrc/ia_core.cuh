@@ -53,6 +53,11 @@ __device__ __forceinline__ long long lin(const Grid& g, int x, int y, int z) {
     return x + g.s[1] * y + g.s[2] * z;
 }
 
+// Host-side count of kernel launches issued by this library (every launch site
+// calls note_launch after issuing its kernel).
+void note_launch();
+long long launch_count();
+
 // Order-preserving map of a double onto uint64 (for atomicMax / atomicMin).
 __device__ __forceinline__ unsigned long long ord_enc(double v) {
     unsigned long long b = __double_as_longlong(v);

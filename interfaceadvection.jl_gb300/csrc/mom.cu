@@ -537,15 +537,15 @@ __global__ void cfl_kern(Grid g, const double* __restrict__ u, unsigned long lon
 }  // namespace
 
 cudaError_t k_ustar(const MomConsts& k, const double* rhou, const double* f, double* ustar, cudaStream_t s) {
-    ustar_kern<<<grd(k.g), blk(), 0, s>>>(k, rhou, f, ustar);
+    { ustar_kern<<<grd(k.g), blk(), 0, s>>>(k, rhou, f, ustar); ia::note_launch(); }
     return cudaGetLastError();
 }
 cudaError_t k_u2rhou(const MomConsts& k, double* rhou, const double* u, const double* f, cudaStream_t s) {
-    u2rhou_kern<<<grd(k.g), blk(), 0, s>>>(k, rhou, u, f);
+    { u2rhou_kern<<<grd(k.g), blk(), 0, s>>>(k, rhou, u, f); ia::note_launch(); }
     return cudaGetLastError();
 }
 cudaError_t k_bc_vel(const MomConsts& k, double* a, const double* A, cudaStream_t s) {
-    bcvel_kern<<<grd(k.g), blk(), 0, s>>>(k, a, A[0], A[1], A[2]);
+    { bcvel_kern<<<grd(k.g), blk(), 0, s>>>(k, a, A[0], A[1], A[2]); ia::note_launch(); }
     return cudaGetLastError();
 }
 cudaError_t k_momflux(const MomConsts& k, int j, int limiter, const double* ustar, const double* rhouf_j,
@@ -559,12 +559,12 @@ cudaError_t k_momflux(const MomConsts& k, int j, int limiter, const double* usta
     F.fold = fold;
     F.dt = dt;
     F.inv_dt = 1.0 / dt;
-    momflux_kern<<<grd(k.g), blk(), 0, s>>>(F, Phi);
+    { momflux_kern<<<grd(k.g), blk(), 0, s>>>(F, Phi); ia::note_launch(); }
     return cudaGetLastError();
 }
 cudaError_t k_momupdate(const MomConsts& k, int j, const double* Phi, const double* uOld, const double* u1,
                         const double* u2, const int8_t* cbar, double dt, double* rhou, cudaStream_t s) {
-    momupdate_kern<<<grd(k.g), blk(), 0, s>>>(k, j, Phi, uOld, u1 + j * k.g.N, u2 + j * k.g.N, cbar, dt, rhou);
+    { momupdate_kern<<<grd(k.g), blk(), 0, s>>>(k, j, Phi, uOld, u1 + j * k.g.N, u2 + j * k.g.N, cbar, dt, rhou); ia::note_launch(); }
     return cudaGetLastError();
 }
 cudaError_t k_visc(const MomConsts& k, const double* u, const double* f, double lmu, double mu, double* Phi6,
@@ -585,45 +585,45 @@ cudaError_t k_visc(const MomConsts& k, const double* u, const double* f, double 
     };
     V.mu_face0 = mu_at(0.0);
     V.mu_face1 = mu_at(1.0);
-    viscflux_kern<<<grd(k.g), blk(), 0, s>>>(V, Phi6);
-    viscacc_kern<<<grd(k.g), blk(), 0, s>>>(k.g, Phi6, r);
+    { viscflux_kern<<<grd(k.g), blk(), 0, s>>>(V, Phi6); ia::note_launch(); }
+    { viscacc_kern<<<grd(k.g), blk(), 0, s>>>(k.g, Phi6, r); ia::note_launch(); }
     return cudaGetLastError();
 }
 cudaError_t k_zero(double* a, long long n, cudaStream_t s) {
-    zero_kern<<<1216, 256, 0, s>>>(a, n);
+    { zero_kern<<<1216, 256, 0, s>>>(a, n); ia::note_launch(); }
     return cudaGetLastError();
 }
 cudaError_t k_surften(const MomConsts& k, int d, const double* f, double eta, double* fb, double* r, cudaStream_t s) {
-    fbuffer_kern<<<grd(k.g), blk(), 0, s>>>(k, d, f, fb);
-    if (k.g.D == 2) surften_kern<2><<<grd(k.g), blk(), 0, s>>>(k, d, f, fb, eta, r);
-    else surften_kern<3><<<grd(k.g), blk(), 0, s>>>(k, d, f, fb, eta, r);
+    { fbuffer_kern<<<grd(k.g), blk(), 0, s>>>(k, d, f, fb); ia::note_launch(); }
+    if (k.g.D == 2) { surften_kern<2><<<grd(k.g), blk(), 0, s>>>(k, d, f, fb, eta, r); ia::note_launch(); }
+    else { surften_kern<3><<<grd(k.g), blk(), 0, s>>>(k, d, f, fb, eta, r); ia::note_launch(); }
     return cudaGetLastError();
 }
 cudaError_t k_updateu(const MomConsts& k, double* u, double* rhou, const double* u0, const double* F, double dt,
                       const double* fref, const double* fupd, double w, bool write_rhou, cudaStream_t s) {
     const double a = 1.0 / w - 1.0;
-    updateu_kern<<<grd(k.g), blk(), 0, s>>>(k, u, rhou, u0, F, dt, fref, fupd, w, a, write_rhou);
+    { updateu_kern<<<grd(k.g), blk(), 0, s>>>(k, u, rhou, u0, F, dt, fref, fupd, w, a, write_rhou); ia::note_launch(); }
     return cudaGetLastError();
 }
 cudaError_t k_updatel(const MomConsts& k, double* mu0, const double* f, cudaStream_t s) {
-    updatel_kern<<<grd(k.g), blk(), 0, s>>>(k, mu0, f);
+    { updatel_kern<<<grd(k.g), blk(), 0, s>>>(k, mu0, f); ia::note_launch(); }
     return cudaGetLastError();
 }
 cudaError_t k_div_scale(const MomConsts& k, const double* u, double* zz, double* xx, double dt, cudaStream_t s) {
-    div_scale_kern<<<grd(k.g), blk(), 0, s>>>(k.g, u, zz, xx, dt);
+    { div_scale_kern<<<grd(k.g), blk(), 0, s>>>(k.g, u, zz, xx, dt); ia::note_launch(); }
     return cudaGetLastError();
 }
 cudaError_t k_correct(const MomConsts& k, double* u, const double* L, double* xx, double dt, cudaStream_t s) {
-    correct_kern<<<grd(k.g), blk(), 0, s>>>(k.g, u, L, xx);
-    scale_kern<<<1216, 256, 0, s>>>(xx, k.g.N, 1.0 / dt);
+    { correct_kern<<<grd(k.g), blk(), 0, s>>>(k.g, u, L, xx); ia::note_launch(); }
+    { scale_kern<<<1216, 256, 0, s>>>(xx, k.g.N, 1.0 / dt); ia::note_launch(); }
     return cudaGetLastError();
 }
 cudaError_t k_cfl(const MomConsts& k, const double* u, unsigned long long* out2, cudaStream_t s) {
-    cfl_kern<<<grd(k.g), blk(), 0, s>>>(k.g, u, out2);
+    { cfl_kern<<<grd(k.g), blk(), 0, s>>>(k.g, u, out2); ia::note_launch(); }
     return cudaGetLastError();
 }
 cudaError_t k_average(double* a, const double* b, long long n, cudaStream_t s) {
-    average_kern<<<1216, 256, 0, s>>>(a, b, n);
+    { average_kern<<<1216, 256, 0, s>>>(a, b, n); ia::note_launch(); }
     return cudaGetLastError();
 }
 

@@ -370,7 +370,7 @@ __global__ void zero_k(long long n, T* a) {
 // ------------------------------------------------------------------ host side
 
 template <class T>
-static cudaError_t vcycle(PoissonMG* mg, int l, cudaStream_t st, int nu1, int nu2, int nuc) {
+static cudaError_t vcycle(ia_handle* h, PoissonMG* mg, int l, cudaStream_t st, int nu1, int nu2, int nuc) {
     auto& L = mg->lev[l];
     T* x = L.template x_<T>();
     T* b = L.template b_<T>();
@@ -378,24 +378,29 @@ static cudaError_t vcycle(PoissonMG* mg, int l, cudaStream_t st, int nu1, int nu
     const T* Lc = L.template L_<T>();
     const T* iD = L.template iD_<T>();
     if (l == mg->nlev - 1) {
-        coarse_k<T><<<1, 1024, 0, st>>>(L.g, Lc, iD, b, x, nuc);
+        { coarse_k<T><<<1, 1024, 0, st>>>(L.g, Lc, iD, b, x, nuc); ia::note_launch(); }
         return cudaGetLastError();
     }
-    rb_first_k<T><<<grd(L.g), blk(), 0, st>>>(L.g, iD, b, x);
-    rbgs_k<T><<<grd(L.g), blk(), 0, st>>>(L.g, Lc, iD, b, x, 1);
+    auto half = [&](int color) {
+        const int tk = (l == 0) ? timing_begin(h, TK_MG_FINE) : -1;
+        { rbgs_k<T><<<grd(L.g), blk(), 0, st>>>(L.g, Lc, iD, b, x, color); ia::note_launch(); }
+        timing_end(h, tk);
+    };
+    { rb_first_k<T><<<grd(L.g), blk(), 0, st>>>(L.g, iD, b, x); ia::note_launch(); }
+    half(1);
     for (int k = 1; k < nu1; ++k) {
-        rbgs_k<T><<<grd(L.g), blk(), 0, st>>>(L.g, Lc, iD, b, x, 0);
-        rbgs_k<T><<<grd(L.g), blk(), 0, st>>>(L.g, Lc, iD, b, x, 1);
+        half(0);
+        half(1);
     }
-    residual_k<T><<<grd(L.g), blk(), 0, st>>>(L.g, Lc, b, x, r);
+    { residual_k<T><<<grd(L.g), blk(), 0, st>>>(L.g, Lc, b, x, r); ia::note_launch(); }
     auto& C = mg->lev[l + 1];
-    restrict_k<T><<<grd(C.g), blk(), 0, st>>>(C.g, L.g, r, C.template b_<T>());
-    cudaError_t e = vcycle<T>(mg, l + 1, st, nu1, nu2, nuc);
+    { restrict_k<T><<<grd(C.g), blk(), 0, st>>>(C.g, L.g, r, C.template b_<T>()); ia::note_launch(); }
+    cudaError_t e = vcycle<T>(h, mg, l + 1, st, nu1, nu2, nuc);
     if (e != cudaSuccess) return e;
-    prolong_k<T><<<grd(L.g), blk(), 0, st>>>(L.g, C.g, C.template x_<T>(), x);
+    { prolong_k<T><<<grd(L.g), blk(), 0, st>>>(L.g, C.g, C.template x_<T>(), x); ia::note_launch(); }
     for (int k = 0; k < nu2; ++k) {
-        rbgs_k<T><<<grd(L.g), blk(), 0, st>>>(L.g, Lc, iD, b, x, 1);
-        rbgs_k<T><<<grd(L.g), blk(), 0, st>>>(L.g, Lc, iD, b, x, 0);
+        half(1);
+        half(0);
     }
     return cudaGetLastError();
 }
@@ -498,19 +503,19 @@ static cudaError_t mg_setup(ia_handle* h, const double* L0) {
     const long long nv = F.g.N * F.g.D;
     if (!mixed) {
         cudaMemcpyAsync(F.L, L0, 8 * nv, cudaMemcpyDeviceToDevice, st);
-        set_diag_k<double><<<grd(F.g), blk(), 0, st>>>(F.g, F.L, F.iD);
+        { set_diag_k<double><<<grd(F.g), blk(), 0, st>>>(F.g, F.L, F.iD); ia::note_launch(); }
         for (int l = 1; l < mg->nlev; ++l) {
-            restrict_L_k<double><<<grd(mg->lev[l].g), blk(), 0, st>>>(mg->lev[l].g, mg->lev[l - 1].g,
-                                                                       mg->lev[l - 1].L, mg->lev[l].L);
-            set_diag_k<double><<<grd(mg->lev[l].g), blk(), 0, st>>>(mg->lev[l].g, mg->lev[l].L, mg->lev[l].iD);
+            { restrict_L_k<double><<<grd(mg->lev[l].g), blk(), 0, st>>>(mg->lev[l].g, mg->lev[l - 1].g,
+                                                                       mg->lev[l - 1].L, mg->lev[l].L); ia::note_launch(); }
+            { set_diag_k<double><<<grd(mg->lev[l].g), blk(), 0, st>>>(mg->lev[l].g, mg->lev[l].L, mg->lev[l].iD); ia::note_launch(); }
         }
     } else {
-        to_f32_k<<<1216, 256, 0, st>>>(nv, L0, F.L32);
-        set_diag_k<float><<<grd(F.g), blk(), 0, st>>>(F.g, F.L32, F.iD32);
+        { to_f32_k<<<1216, 256, 0, st>>>(nv, L0, F.L32); ia::note_launch(); }
+        { set_diag_k<float><<<grd(F.g), blk(), 0, st>>>(F.g, F.L32, F.iD32); ia::note_launch(); }
         for (int l = 1; l < mg->nlev; ++l) {
-            restrict_L_k<float><<<grd(mg->lev[l].g), blk(), 0, st>>>(mg->lev[l].g, mg->lev[l - 1].g,
-                                                                      mg->lev[l - 1].L32, mg->lev[l].L32);
-            set_diag_k<float><<<grd(mg->lev[l].g), blk(), 0, st>>>(mg->lev[l].g, mg->lev[l].L32, mg->lev[l].iD32);
+            { restrict_L_k<float><<<grd(mg->lev[l].g), blk(), 0, st>>>(mg->lev[l].g, mg->lev[l - 1].g,
+                                                                      mg->lev[l - 1].L32, mg->lev[l].L32); ia::note_launch(); }
+            { set_diag_k<float><<<grd(mg->lev[l].g), blk(), 0, st>>>(mg->lev[l].g, mg->lev[l].L32, mg->lev[l].iD32); ia::note_launch(); }
         }
     }
     return cudaGetLastError();
@@ -525,17 +530,17 @@ static cudaError_t mg_precondition(ia_handle* h) {
     cudaError_t e;
     if (h->cfg.poisson_mode == IA_POISSON_MIXED) {
         int tk = timing_begin(h, TK_MG_TRANSFER);
-        to_f32_k<<<1216, 256, 0, st>>>(N, mg->r, F.b32);
+        { to_f32_k<<<1216, 256, 0, st>>>(N, mg->r, F.b32); ia::note_launch(); }
         timing_end(h, tk);
         tk = timing_begin(h, TK_MG_SMOOTH);
-        e = vcycle<float>(mg, 0, st, mg->nu1, mg->nu2, mg->nuc);
+        e = vcycle<float>(h, mg, 0, st, mg->nu1, mg->nu2, mg->nuc);
         timing_end(h, tk);
         if (e != cudaSuccess) return e;
-        to_f64_k<<<1216, 256, 0, st>>>(N, F.x32, mg->s);
+        { to_f64_k<<<1216, 256, 0, st>>>(N, F.x32, mg->s); ia::note_launch(); }
     } else {
         cudaMemcpyAsync(F.b, mg->r, 8 * N, cudaMemcpyDeviceToDevice, st);
         int tk = timing_begin(h, TK_MG_SMOOTH);
-        e = vcycle<double>(mg, 0, st, mg->nu1, mg->nu2, mg->nuc);
+        e = vcycle<double>(h, mg, 0, st, mg->nu1, mg->nu2, mg->nuc);
         timing_end(h, tk);
         if (e != cudaSuccess) return e;
         cudaMemcpyAsync(mg->s, F.x, 8 * N, cudaMemcpyDeviceToDevice, st);
@@ -566,7 +571,7 @@ int poisson_solve(ia_handle* h, double* xv, const double* zz, const double* L, d
     double* dots = mg->dsc;
     cudaMemsetAsync(dlinf, 0, 8, st);
     int tk = timing_begin(h, TK_KRYLOV);
-    true_resid_k<<<gb, blk(), 0, st>>>(g, L, zz, xv, mg->r, dlinf);
+    { true_resid_k<<<gb, blk(), 0, st>>>(g, L, zz, xv, mg->r, dlinf); ia::note_launch(); }
     timing_end(h, tk);
     double res = read_linf(h, dlinf);
     int it = 0;
@@ -574,8 +579,8 @@ int poisson_solve(ia_handle* h, double* xv, const double* zz, const double* L, d
     while (!(res <= tol) && it < itmx) {
         if (mg_precondition(h) != cudaSuccess) return IA_ERR_CUDA;
         tk = timing_begin(h, TK_KRYLOV);
-        dot2_k<<<gb, blk(), 0, st>>>(g, mg->s, mg->q, mg->r, mg->partial, mg->nblocks);
-        finalize_k<<<1, 1024, 0, st>>>(mg->partial, mg->nblocks, 2, dots);
+        { dot2_k<<<gb, blk(), 0, st>>>(g, mg->s, mg->q, mg->r, mg->partial, mg->nblocks); ia::note_launch(); }
+        { finalize_k<<<1, 1024, 0, st>>>(mg->partial, mg->nblocks, 2, dots); ia::note_launch(); }
         timing_end(h, tk);
         cudaMemcpyAsync(mg->hsc + 2, dots, 16, cudaMemcpyDeviceToHost, st);
         if (cudaStreamSynchronize(st) != cudaSuccess) return IA_ERR_CUDA;
@@ -584,9 +589,9 @@ int poisson_solve(ia_handle* h, double* xv, const double* zz, const double* L, d
         const double beta = (it == 0) ? 0.0 : (-alpha_prev * sq) / rho_prev;
         const double rho = sr;
         tk = timing_begin(h, TK_KRYLOV);
-        xpby_k<<<gb, blk(), 0, st>>>(g, mg->s, beta, mg->p);
-        matvec_dot_k<<<gb, blk(), 0, st>>>(g, L, mg->p, mg->q, mg->partial);
-        finalize_k<<<1, 1024, 0, st>>>(mg->partial, mg->nblocks, 1, dots);
+        { xpby_k<<<gb, blk(), 0, st>>>(g, mg->s, beta, mg->p); ia::note_launch(); }
+        { matvec_dot_k<<<gb, blk(), 0, st>>>(g, L, mg->p, mg->q, mg->partial); ia::note_launch(); }
+        { finalize_k<<<1, 1024, 0, st>>>(mg->partial, mg->nblocks, 1, dots); ia::note_launch(); }
         timing_end(h, tk);
         cudaMemcpyAsync(mg->hsc + 2, dots, 8, cudaMemcpyDeviceToHost, st);
         if (cudaStreamSynchronize(st) != cudaSuccess) return IA_ERR_CUDA;
@@ -595,14 +600,14 @@ int poisson_solve(ia_handle* h, double* xv, const double* zz, const double* L, d
         const double alpha = rho / pq;
         cudaMemsetAsync(dlinf, 0, 8, st);
         tk = timing_begin(h, TK_KRYLOV);
-        update_k<<<gb, blk(), 0, st>>>(g, alpha, mg->p, mg->q, xv, mg->r, dlinf);
+        { update_k<<<gb, blk(), 0, st>>>(g, alpha, mg->p, mg->q, xv, mg->r, dlinf); ia::note_launch(); }
         timing_end(h, tk);
         res = read_linf(h, dlinf);
         rho_prev = rho;
         alpha_prev = alpha;
         ++it;
     }
-    perbc_k<<<gb, blk(), 0, st>>>(g, xv);
+    { perbc_k<<<gb, blk(), 0, st>>>(g, xv); ia::note_launch(); }
     if (cudaGetLastError() != cudaSuccess) return IA_ERR_CUDA;
     *iters = it;
     *resid = res;

@@ -101,10 +101,12 @@ static int advect_fq(ia_handle* h, double* f, const double* u1, const double* u2
         timing_end(h, tk);
         int rc = vof_sweep(h, fin, fout, u1, u2, dt, d, q == 0, cbar, h->fld.rhouf, 10.0 * tol, counter_base + q);
         if (rc != IA_OK) return rc;
-        tk = timing_begin(h, TK_MOM);
+        tk = timing_begin(h, TK_MOM_FLUX);
         if (k_momflux(k, d, h->cfg.limiter, m->ustar, h->fld.rhouf + (long long)d * g.N, fin, dt, m->Phi, st) !=
             cudaSuccess)
             return IA_ERR_CUDA;
+        timing_end(h, tk);
+        tk = timing_begin(h, TK_MOM_UPDATE);
         if (k_momupdate(k, d, m->Phi, uOld, u1, u2, cbar, dt, h->fld.rhou, st) != cudaSuccess) return IA_ERR_CUDA;
         timing_end(h, tk);
     }
@@ -133,14 +135,14 @@ static int visc_surften(ia_handle* h, const double* f) {
 static int project(ia_handle* h, const double* f, double dtp, int* iters, double* resid) {
     const MomConsts k = consts(h);
     cudaStream_t st = h->stream;
-    int tk = timing_begin(h, TK_FORCE);
+    int tk = timing_begin(h, TK_UPDATE);
     if (k_updatel(k, h->fld.mu0, f, st) != cudaSuccess) return IA_ERR_CUDA;
     if (k_div_scale(k, h->fld.u, h->fld.sigma, h->fld.p, dtp, st) != cudaSuccess) return IA_ERR_CUDA;
     timing_end(h, tk);
     int rc = poisson_solve(h, h->fld.p, h->fld.sigma, h->fld.mu0, h->cfg.poisson_tol, h->cfg.poisson_itmx, iters,
                            resid);
     if (rc != IA_OK && rc != IA_WARN_NOT_CONVERGED) return rc;
-    tk = timing_begin(h, TK_FORCE);
+    tk = timing_begin(h, TK_UPDATE);
     if (k_correct(k, h->fld.u, h->fld.mu0, h->fld.p, dtp, st) != cudaSuccess) return IA_ERR_CUDA;
     const double zero[3] = {h->cfg.uBC[0], h->cfg.uBC[1], h->cfg.uBC[2]};
     if (k_bc_vel(k, h->fld.u, zero, st) != cudaSuccess) return IA_ERR_CUDA;

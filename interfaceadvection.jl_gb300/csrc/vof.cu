@@ -282,7 +282,7 @@ template <int D, bool FIRST>
 void launch_bulk(const SweepArgs& a, cudaStream_t st) {
     dim3 blk(32, 8, 1);
     dim3 grd((a.g.n[0] + 31) / 32, (a.g.n[1] + 7) / 8, a.g.n[2]);
-    vof_bulk<D, FIRST><<<grd, blk, 0, st>>>(a);
+    { vof_bulk<D, FIRST><<<grd, blk, 0, st>>>(a); ia::note_launch(); }
 }
 
 }  // namespace
@@ -294,23 +294,23 @@ cudaError_t vof_sweep_bulk(const SweepArgs& a, cudaStream_t st) {
 }
 
 cudaError_t vof_sweep_faces(const SweepArgs& a, cudaStream_t st, int list_blocks) {
-    if (a.g.D == 2) vof_faces<2><<<list_blocks, 128, 0, st>>>(a);
-    else vof_faces<3><<<list_blocks, 128, 0, st>>>(a);
+    if (a.g.D == 2) { vof_faces<2><<<list_blocks, 128, 0, st>>>(a); ia::note_launch(); }
+    else { vof_faces<3><<<list_blocks, 128, 0, st>>>(a); ia::note_launch(); }
     return cudaGetLastError();
 }
 
 cudaError_t vof_sweep_scatter(const SweepArgs& a, cudaStream_t st, int list_blocks) {
-    vof_scatter<<<list_blocks / 2, 256, 0, st>>>(a);
+    { vof_scatter<<<list_blocks / 2, 256, 0, st>>>(a); ia::note_launch(); }
     return cudaGetLastError();
 }
 
 cudaError_t vof_sweep_cells(const SweepArgs& a, cudaStream_t st, int list_blocks) {
     if (a.g.D == 2) {
-        if (a.first) vof_cells<2, true><<<list_blocks, 128, 0, st>>>(a);
-        else vof_cells<2, false><<<list_blocks, 128, 0, st>>>(a);
+        if (a.first) { vof_cells<2, true><<<list_blocks, 128, 0, st>>>(a); ia::note_launch(); }
+        else { vof_cells<2, false><<<list_blocks, 128, 0, st>>>(a); ia::note_launch(); }
     } else {
-        if (a.first) vof_cells<3, true><<<list_blocks, 128, 0, st>>>(a);
-        else vof_cells<3, false><<<list_blocks, 128, 0, st>>>(a);
+        if (a.first) { vof_cells<3, true><<<list_blocks, 128, 0, st>>>(a); ia::note_launch(); }
+        else { vof_cells<3, false><<<list_blocks, 128, 0, st>>>(a); ia::note_launch(); }
     }
     return cudaGetLastError();
 }

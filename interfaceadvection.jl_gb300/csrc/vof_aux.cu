@@ -158,39 +158,39 @@ inline dim3 grd3(const Grid& g) { return dim3((g.n[0] + 31) / 32, (g.n[1] + 7) /
 }  // namespace
 
 cudaError_t fill_ghosts_scalar(const Grid& g, double* f, cudaStream_t st) {
-    ghosts_k<<<grd3(g), blk3(), 0, st>>>(g, f);
+    { ghosts_k<<<grd3(g), blk3(), 0, st>>>(g, f); ia::note_launch(); }
     return cudaGetLastError();
 }
 
 cudaError_t apply_vof(const Grid& g, const double* sdf, double* f, double* alpha, double* nhat, cudaStream_t st) {
-    if (g.D == 2) apply_vof_k<2><<<grd3(g), blk3(), 0, st>>>(g, sdf, f, alpha, nhat);
-    else apply_vof_k<3><<<grd3(g), blk3(), 0, st>>>(g, sdf, f, alpha, nhat);
+    if (g.D == 2) { apply_vof_k<2><<<grd3(g), blk3(), 0, st>>>(g, sdf, f, alpha, nhat); ia::note_launch(); }
+    else { apply_vof_k<3><<<grd3(g), blk3(), 0, st>>>(g, sdf, f, alpha, nhat); ia::note_launch(); }
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
     return fill_ghosts_scalar(g, f, st);
 }
 
 cudaError_t reconstruct(const Grid& g, int scheme, double* f, double* alpha, double* nhat, cudaStream_t st) {
-    if (g.D == 2) reconstruct_k<2><<<grd3(g), blk3(), 0, st>>>(g, scheme, f, alpha, nhat);
-    else reconstruct_k<3><<<grd3(g), blk3(), 0, st>>>(g, scheme, f, alpha, nhat);
+    if (g.D == 2) { reconstruct_k<2><<<grd3(g), blk3(), 0, st>>>(g, scheme, f, alpha, nhat); ia::note_launch(); }
+    else { reconstruct_k<3><<<grd3(g), blk3(), 0, st>>>(g, scheme, f, alpha, nhat); ia::note_launch(); }
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
-    bcvof_ghosts_k<<<grd3(g), blk3(), 0, st>>>(g, f, alpha, nhat);
+    { bcvof_ghosts_k<<<grd3(g), blk3(), 0, st>>>(g, f, alpha, nhat); ia::note_launch(); }
     return cudaGetLastError();
 }
 
 cudaError_t vof_flux(const Grid& g, double* fF, const double* f, const double* alpha, const double* nhat,
                      const double* u, const double* u0, double dt, int d, double* rhouf, double lrho,
                      cudaStream_t st) {
-    if (g.D == 2) vof_flux_k<2><<<grd3(g), blk3(), 0, st>>>(g, fF, f, alpha, nhat, u, u0, dt, d, rhouf, lrho);
-    else vof_flux_k<3><<<grd3(g), blk3(), 0, st>>>(g, fF, f, alpha, nhat, u, u0, dt, d, rhouf, lrho);
+    if (g.D == 2) { vof_flux_k<2><<<grd3(g), blk3(), 0, st>>>(g, fF, f, alpha, nhat, u, u0, dt, d, rhouf, lrho); ia::note_launch(); }
+    else { vof_flux_k<3><<<grd3(g), blk3(), 0, st>>>(g, fF, f, alpha, nhat, u, u0, dt, d, rhouf, lrho); ia::note_launch(); }
     return cudaGetLastError();
 }
 
 cudaError_t interior_sum(const Grid& g, const double* f, double* partial, double* out, cudaStream_t st) {
     const int nb = 1024;
-    sum_rows_k<<<nb, 256, 0, st>>>(g, f, partial);
-    sum_partials_k<<<1, 1024, 0, st>>>(partial, nb, out);
+    { sum_rows_k<<<nb, 256, 0, st>>>(g, f, partial); ia::note_launch(); }
+    { sum_partials_k<<<1, 1024, 0, st>>>(partial, nb, out); ia::note_launch(); }
     return cudaGetLastError();
 }
 

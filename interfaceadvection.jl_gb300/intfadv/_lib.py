@@ -30,8 +30,8 @@ NORMAL_SCHEMES = {"WH": 0, "WY": 1, "MYC": 2, "Y": 3, "Column": 4, "PCD": 5, "SL
 LIMITERS = {"Koren": 0, "upwind": 1, "minmod": 2, "vanAlbada1": 3, "Sweby": 4, "superbee": 5,
             "TVDcen": 6, "TVDdown": 7}
 POISSON_MODES = {"fp64": 0, "mixed": 1}
-TIMED_KERNELS = ["vof_bulk", "vof_list", "momentum", "forcing", "mg_smooth", "mg_residual", "mg_transfer",
-                 "krylov", "other"]
+TIMED_KERNELS = ["vof_bulk", "vof_cells", "ustar", "forcing", "mg_vcycle", "mg_residual", "mg_transfer",
+                 "krylov", "other", "vof_faces", "momflux", "momupdate", "update_project", "mg_fine_rbgs"]
 
 
 class Config(C.Structure):
@@ -66,6 +66,7 @@ _SIGS = {
     "ia_apply_vof": (C.c_int, [C.c_void_p] * 5),
     "ia_mass": (C.c_int, [C.c_void_p, C.c_void_p, C.POINTER(C.c_double)]),
     "ia_error_string": (C.c_char_p, [C.c_int]),
+    "ia_launch_count": (C.c_int64, []),
     "ia_timing": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p, C.c_int32]),
     "ia_mom_step": (C.c_int, [C.c_void_p, C.c_double, C.c_int64, C.c_double, C.POINTER(Status)]),
     "ia_cfl": (C.c_int, [C.c_void_p, C.POINTER(C.c_double)]),
