@@ -341,6 +341,110 @@ __global__ void update_k(Grid g, double alpha, const double* __restrict__ pv, co
     if (t == 0) atomicMax(linf, sm[0]);
 }
 
+// ---- FP32 inner Krylov kernels (mixed mode): products and block sums in FP32,
+// one FP64 partial per block, reduced across blocks in FP64.
+__device__ __forceinline__ float block_sum_f(float v, float* sm, int t) {
+    sm[t] = v;
+    __syncthreads();
+    for (int w = 128; w > 0; w >>= 1) {
+        if (t < w) sm[t] += sm[t + w];
+        __syncthreads();
+    }
+    return sm[0];
+}
+
+__global__ void matvec32_dot_k(Grid g, const float* __restrict__ L, const float* __restrict__ pv,
+                               float* __restrict__ q, double* __restrict__ partial) {
+    __shared__ float sm[256];
+    const int t = threadIdx.y * blockDim.x + threadIdx.x;
+    float acc = 0.f;
+    {
+        const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y;
+        const int z = blockIdx.z;
+        const int c[3] = {x, y, z};
+        if (x < g.n[0] && y < g.n[1] && is_interior(g, c)) {
+            const long long I = lin(g, x, y, z);
+            float dd = 0.f;
+            for (int i = 0; i < g.D; ++i) dd -= L[I + i * g.N] + L[I + g.s[i] + i * g.N];
+            const float v = offdiag(g, L, pv, I, c) + dd * pv[I];
+            q[I] = v;
+            acc = pv[I] * v;
+        }
+    }
+    const float b = block_sum_f(acc, sm, t);
+    if (t == 0) partial[(blockIdx.z * gridDim.y + blockIdx.y) * gridDim.x + blockIdx.x] = double(b);
+}
+
+__global__ void dot2_32_k(Grid g, const float* __restrict__ sv, const float* __restrict__ q,
+                          const float* __restrict__ r, double* __restrict__ partial, long long nblocks) {
+    __shared__ float s1[256], s2[256];
+    const int t = threadIdx.y * blockDim.x + threadIdx.x;
+    float a1 = 0.f, a2 = 0.f;
+    {
+        const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y;
+        const int z = blockIdx.z;
+        const int c[3] = {x, y, z};
+        if (x < g.n[0] && y < g.n[1] && is_interior(g, c)) {
+            const long long I = lin(g, x, y, z);
+            a1 = sv[I] * q[I];
+            a2 = sv[I] * r[I];
+        }
+    }
+    s1[t] = a1;
+    s2[t] = a2;
+    __syncthreads();
+    for (int w = 128; w > 0; w >>= 1) {
+        if (t < w) {
+            s1[t] += s1[t + w];
+            s2[t] += s2[t + w];
+        }
+        __syncthreads();
+    }
+    if (t == 0) {
+        const long long b = (blockIdx.z * gridDim.y + blockIdx.y) * gridDim.x + blockIdx.x;
+        partial[b] = double(s1[0]);
+        partial[nblocks + b] = double(s2[0]);
+    }
+}
+
+__global__ void xpby32_k(Grid g, const float* __restrict__ sv, float beta, float* __restrict__ pv) {
+    INTERIOR_XYZ
+    pv[I] = sv[I] + beta * pv[I];
+}
+
+// e += α p ; r -= α q ; L∞(r) as float bits
+__global__ void update32_k(Grid g, float alpha, const float* __restrict__ pv, const float* __restrict__ q,
+                           float* __restrict__ e, float* __restrict__ r, unsigned int* linf) {
+    __shared__ unsigned int sm[256];
+    const int t = threadIdx.y * blockDim.x + threadIdx.x;
+    unsigned int m = 0u;
+    {
+        const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y;
+        const int z = blockIdx.z;
+        const int c[3] = {x, y, z};
+        if (x < g.n[0] && y < g.n[1] && is_interior(g, c)) {
+            const long long I = lin(g, x, y, z);
+            e[I] += alpha * pv[I];
+            const float v = r[I] - alpha * q[I];
+            r[I] = v;
+            m = __float_as_uint(v) & 0x7FFFFFFFu;
+        }
+    }
+    sm[t] = m;
+    __syncthreads();
+    for (int w = 128; w > 0; w >>= 1) {
+        if (t < w) sm[t] = sm[t] > sm[t + w] ? sm[t] : sm[t + w];
+        __syncthreads();
+    }
+    if (t == 0) atomicMax(linf, sm[0]);
+}
+
+// x += e (FP64 += FP32), interior cells
+__global__ void add_correction_k(Grid g, const float* __restrict__ e, double* __restrict__ xv) {
+    INTERIOR_XYZ
+    xv[I] += double(e[I]);
+}
+
 // periodic ghosts of a scalar (WaterLily perBC!)
 __global__ void perbc_k(Grid g, double* a) {
     const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y;
@@ -466,6 +570,16 @@ int mg_create(ia_handle* h) {
     const dim3 gb = grd(g0);
     mg->nblocks = (long long)gb.x * gb.y * gb.z;
     e = e ? e : cudaMalloc(&mg->partial, 8 * 2 * (size_t)mg->nblocks);
+    if (mixed) {
+        e = e ? e : cudaMalloc(&mg->p32, 4 * N);
+        e = e ? e : cudaMalloc(&mg->q32, 4 * N);
+        e = e ? e : cudaMalloc(&mg->e32, 4 * N);
+        if (!e) {
+            cudaMemset(mg->p32, 0, 4 * N);
+            cudaMemset(mg->q32, 0, 4 * N);
+            cudaMemset(mg->e32, 0, 4 * N);
+        }
+    }
     e = e ? e : cudaMalloc(&mg->dsc, 8 * 16);
     e = e ? e : cudaMallocHost(&mg->hsc, 8 * 16);
     if (e != cudaSuccess) return IA_ERR_CUDA;
@@ -488,6 +602,7 @@ void mg_destroy(ia_handle* h) {
         cudaFree(L.x32); cudaFree(L.b32); cudaFree(L.r32); cudaFree(L.L32); cudaFree(L.iD32);
     }
     cudaFree(mg->r); cudaFree(mg->s); cudaFree(mg->p); cudaFree(mg->q);
+    cudaFree(mg->p32); cudaFree(mg->q32); cudaFree(mg->e32);
     cudaFree(mg->partial); cudaFree(mg->dsc);
     if (mg->hsc) cudaFreeHost(mg->hsc);
     delete mg;
@@ -558,11 +673,102 @@ static double read_linf(ia_handle* h, unsigned long long* dlinf) {
     return d;
 }
 
+static double read_linf32(ia_handle* h, unsigned int* d) {
+    unsigned int v = 0;
+    cudaMemcpyAsync(&h->mg->hsc[0], d, 4, cudaMemcpyDeviceToHost, h->stream);
+    cudaStreamSynchronize(h->stream);
+    std::memcpy(&v, &h->mg->hsc[0], 4);
+    float f;
+    std::memcpy(&f, &v, 4);
+    return double(f);
+}
+
+// Mixed precision: FP64 defect correction x += e, e from an inner flexible CG run
+// entirely in FP32 (operator, V-cycle, vectors) on A e = r, started from the FP64
+// true residual; inner dot products are block sums in FP32 reduced across blocks in
+// FP64 and the CG scalars are FP64.
+static int poisson_solve_mixed(ia_handle* h, double* xv, const double* zz, const double* L, double tol, int itmx,
+                               int* iters, double* resid) {
+    PoissonMG* mg = h->mg;
+    cudaStream_t st = h->stream;
+    const Grid& g = h->g;
+    const dim3 gb = grd(g);
+    MGLevel& F = mg->lev[0];
+    const long long N = g.N;
+    unsigned long long* dlinf = reinterpret_cast<unsigned long long*>(mg->dsc + 8);
+    unsigned int* dlinf32 = reinterpret_cast<unsigned int*>(mg->dsc + 9);
+    double* dots = mg->dsc;
+    float* rr = F.b32;    // inner residual (the V-cycle reads its right-hand side here)
+    float* sv = F.x32;    // V-cycle output = preconditioned residual
+    int total = 0;
+    cudaMemsetAsync(dlinf, 0, 8, st);
+    int tk = timing_begin(h, TK_KRYLOV);
+    { true_resid_k<<<gb, blk(), 0, st>>>(g, L, zz, xv, mg->r, dlinf); ia::note_launch(); }
+    timing_end(h, tk);
+    double res = read_linf(h, dlinf);
+    while (!(res <= tol) && total < itmx) {
+        tk = timing_begin(h, TK_MG_TRANSFER);
+        { to_f32_k<<<1216, 256, 0, st>>>(N, mg->r, rr); ia::note_launch(); }
+        { zero_k<float><<<1216, 256, 0, st>>>(N, mg->e32); ia::note_launch(); }
+        timing_end(h, tk);
+        const double target = std::fmax(0.5 * tol / res, mg->inner_rtol) * res;
+        double rho_prev = 0.0, alpha_prev = 0.0;
+        for (int it = 0; it < mg->inner_max && total < itmx; ++it) {
+            tk = timing_begin(h, TK_MG_SMOOTH);
+            cudaError_t e = vcycle<float>(h, mg, 0, st, mg->nu1, mg->nu2, mg->nuc);
+            timing_end(h, tk);
+            if (e != cudaSuccess) return IA_ERR_CUDA;
+            tk = timing_begin(h, TK_KRYLOV);
+            { dot2_32_k<<<gb, blk(), 0, st>>>(g, sv, mg->q32, rr, mg->partial, mg->nblocks); ia::note_launch(); }
+            { finalize_k<<<1, 1024, 0, st>>>(mg->partial, mg->nblocks, 2, dots); ia::note_launch(); }
+            timing_end(h, tk);
+            cudaMemcpyAsync(mg->hsc + 2, dots, 16, cudaMemcpyDeviceToHost, st);
+            if (cudaStreamSynchronize(st) != cudaSuccess) return IA_ERR_CUDA;
+            const double sq = mg->hsc[2], sr = mg->hsc[3];
+            const double beta = (it == 0) ? 0.0 : (-alpha_prev * sq) / rho_prev;
+            tk = timing_begin(h, TK_KRYLOV);
+            { xpby32_k<<<gb, blk(), 0, st>>>(g, sv, float(beta), mg->p32); ia::note_launch(); }
+            { matvec32_dot_k<<<gb, blk(), 0, st>>>(g, F.L32, mg->p32, mg->q32, mg->partial); ia::note_launch(); }
+            { finalize_k<<<1, 1024, 0, st>>>(mg->partial, mg->nblocks, 1, dots); ia::note_launch(); }
+            timing_end(h, tk);
+            cudaMemcpyAsync(mg->hsc + 2, dots, 8, cudaMemcpyDeviceToHost, st);
+            if (cudaStreamSynchronize(st) != cudaSuccess) return IA_ERR_CUDA;
+            const double pq = mg->hsc[2];
+            ++total;
+            if (!(pq != 0.0) || !std::isfinite(pq)) break;
+            const double alpha = sr / pq;
+            cudaMemsetAsync(dlinf32, 0, 4, st);
+            tk = timing_begin(h, TK_KRYLOV);
+            { update32_k<<<gb, blk(), 0, st>>>(g, float(alpha), mg->p32, mg->q32, mg->e32, rr, dlinf32); ia::note_launch(); }
+            timing_end(h, tk);
+            const double rin = read_linf32(h, dlinf32);
+            rho_prev = sr;
+            alpha_prev = alpha;
+            if (rin <= target) break;
+        }
+        tk = timing_begin(h, TK_KRYLOV);
+        { add_correction_k<<<gb, blk(), 0, st>>>(g, mg->e32, xv); ia::note_launch(); }
+        cudaMemsetAsync(dlinf, 0, 8, st);
+        { true_resid_k<<<gb, blk(), 0, st>>>(g, L, zz, xv, mg->r, dlinf); ia::note_launch(); }
+        timing_end(h, tk);
+        res = read_linf(h, dlinf);
+    }
+    { perbc_k<<<gb, blk(), 0, st>>>(g, xv); ia::note_launch(); }
+    if (cudaGetLastError() != cudaSuccess) return IA_ERR_CUDA;
+    *iters = total;
+    *resid = res;
+    return (res <= tol) ? IA_OK : IA_WARN_NOT_CONVERGED;
+}
+
 // Solve A x = z to L∞(z - A x) <= tol (x holds the initial guess); L = μ₀.
 int poisson_solve(ia_handle* h, double* xv, const double* zz, const double* L, double tol, int itmx, int* iters,
                   double* resid) {
     PoissonMG* mg = h->mg;
     if (!mg) return IA_ERR_INVALID;
+    if (h->cfg.poisson_mode == IA_POISSON_MIXED) {
+        if (mg_setup(h, L) != cudaSuccess) return IA_ERR_CUDA;
+        return poisson_solve_mixed(h, xv, zz, L, tol, itmx, iters, resid);
+    }
     cudaStream_t st = h->stream;
     const Grid& g = h->g;
     const dim3 gb = grd(g);

@@ -39,6 +39,9 @@ struct PoissonMG {
     int nlev = 0;
     ia::MGLevel lev[ia::MG_MAX_LEVELS];
     double *r = nullptr, *s = nullptr, *p = nullptr, *q = nullptr;   // fine-level Krylov vectors (FP64)
+    float *p32 = nullptr, *q32 = nullptr, *e32 = nullptr;             // inner FP32 Krylov vectors (mixed)
+    int inner_max = 30;                                               // inner FCG iterations per correction
+    double inner_rtol = 1e-4;                                         // inner relative residual target
     double* partial = nullptr;                                        // per-block dot partials
     long long nblocks = 0;
     double* dsc = nullptr;                                            // device scalars

@@ -158,3 +158,23 @@ def test_mpcfl_matches_oracle(cuda):
     ia.sim_step(sim)
     orc.step()
     assert abs(ia.MPCFL(sim) - orc.mpcfl()) < 1e-12 * orc.mpcfl()
+
+
+@pytest.mark.parametrize("limiter", ["upwind", "minmod", "vanAlbada1", "Sweby", "superbee", "TVDcen", "TVDdown"])
+def test_every_limiter_matches_oracle(cuda, limiter):
+    # the λ(u,c,d) keyword of TwoPhaseSimulation (src/flow.jl:5-15), on a sheared 2D droplet
+    N = 24
+    k = 2 * math.pi / N
+    u0_t = lambda i, x: 0.3 * torch.sin(x[1] * k) if i == 0 else 0.2 * torch.cos(x[0] * k)
+    u0_n = lambda i, x: 0.3 * np.sin(x[1] * k) if i == 0 else 0.2 * np.cos(x[0] * k)
+    sdf_t = lambda x: torch.sqrt((x[0] - 10) ** 2 + (x[1] - 12) ** 2) - 5
+    sdf_n = lambda x: np.sqrt((x[0] - 10) ** 2 + (x[1] - 12) ** 2) - 5
+    sim = ia.TwoPhaseSimulation((N, N), (0.0, 0.0), float(N), λρ=0.05, λμ=0.1, InterfaceSDF=sdf_t, u0=u0_t,
+                                perdir=(0, 1), λ=limiter, poisson_tol=PTOL, poisson_itmx=500)
+    orc = OracleSim((N, N), (0.0, 0.0), sdf=sdf_n, u0=u0_n, perdir=(0, 1), lrho=0.05, lmu=0.1, limiter=limiter,
+                    ptol=PTOL)
+    for _ in range(3):
+        ia.sim_step(sim)
+        orc.step()
+    ef, eu, ep = compare(sim, orc, 2)
+    assert ef < 1e-10 and eu < 1e-10 and ep < 1e-6, (limiter, ef, eu, ep)
