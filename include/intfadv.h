@@ -68,6 +68,13 @@ extern "C" {
 /* Poisson solver modes */
 #define IA_POISSON_FP64    0   /* FP64 V-cycle preconditioned CG                     */
 #define IA_POISSON_MIXED   1   /* FP32 V-cycles inside FP64 defect-correction CG     */
+#define IA_POISSON_LEARNED 2   /* as MIXED, inner FCG preconditioned by the conv net  */
+
+/* Inner preconditioner of IA_POISSON_LEARNED (ia_poisson_precond) */
+#define IA_PRECOND_HYBRID  0   /* s1 = ω·net(r); s = s1 + Vcycle(r - A s1), ω least squares */
+#define IA_PRECOND_NET     1   /* s = net(r)                                           */
+#define IA_PRECOND_NONE    2   /* s = r (plain CG; the ablation baseline)               */
+#define IA_PRECOND_VCYCLE  3   /* s = Vcycle(r) (the fallback)                          */
 
 typedef struct ia_handle ia_handle;
 
@@ -225,6 +232,39 @@ int ia_timing(ia_handle* h, int32_t enable, double* ms_out, int64_t* launches_ou
 int64_t ia_launch_count(void);
 
 const char* ia_error_string(int code);
+
+/* ---------------------------------------------------------------------------
+ * Learned Poisson preconditioner (no reference counterpart).
+ *
+ * Network: 3-level 3D conv encoder-decoder, 3x3x3 kernels, channels
+ * 4-16-32-32-32-16-1 (see csrc/nn.cuh), input channels r/max|r| and λρ·L_{x,y,z},
+ * output ∝ A⁻¹ r.  Parameters: FP32 vector of ia_nn_param_count() floats, per
+ * layer W[27][Cout][Cin] (tap = (dz+1)*9 + (dy+1)*3 + (dx+1)) then b[Cout].
+ * Training tensors (device, FP32): channels-last with a one-cell zero halo,
+ * x0 [B][nz+2][ny+2][nx+2][4], target and out [B][nz+2][ny+2][nx+2];
+ * nx, ny, nz multiples of 4.  A handle of any grid carries the net state.
+ * ------------------------------------------------------------------------- */
+int64_t ia_nn_param_count(void);
+/* copy host parameters into / out of the handle's net (set resets the Adam moments) */
+int ia_nn_set_params(ia_handle* h, const float* params);
+int ia_nn_get_params(ia_handle* h, float* params);
+/* forward pass on the handle's stream: tensor_cores = 0 FP32 training kernels, 1 BF16 tcgen05
+ * inference kernels */
+int ia_nn_forward(ia_handle* h, const float* x0, float* out, int32_t B, int32_t nx, int32_t ny, int32_t nz,
+                  int32_t tensor_cores);
+/* MSE loss (mean over interior cells) and its gradient (device, NULL = keep in the handle) */
+int ia_nn_loss_grad(ia_handle* h, const float* x0, const float* target, int32_t B, int32_t nx, int32_t ny,
+                    int32_t nz, float* grad, double* loss);
+/* one Adam step (β1 0.9, β2 0.999, ε 1e-8) on the MSE loss of the handle's net; loss before
+ * the step */
+int ia_nn_train_step(ia_handle* h, const float* x0, const float* target, int32_t B, int32_t nx, int32_t ny,
+                     int32_t nz, float lr, double* loss);
+/* inner preconditioner of an IA_POISSON_LEARNED handle and the inner FCG limits
+ * (inner_max iterations, relative inner residual target) */
+int ia_poisson_precond(ia_handle* h, int32_t precond, int32_t inner_max, double inner_rtol);
+/* counters since the handle's creation: [0] net applications, [1] V-cycles, [2] fallbacks
+ * to the V-cycle, [3] inner FCG iterations, [4] outer corrections */
+int ia_poisson_stats(ia_handle* h, int64_t* out5);
 
 #ifdef __cplusplus
 }

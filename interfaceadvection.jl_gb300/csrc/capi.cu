@@ -233,6 +233,12 @@ int ia_create(const ia_config* cfg, ia_handle** out) {
         if (cfg->N[d] < 2) return IA_ERR_INVALID;
     if (cfg->normal_scheme < 0 || cfg->normal_scheme > IA_NORMAL_XYLIC) return IA_ERR_INVALID;
     if (cfg->limiter < 0 || cfg->limiter > IA_LIMITER_TVDDOWN) return IA_ERR_INVALID;
+    if (cfg->poisson_mode < IA_POISSON_FP64 || cfg->poisson_mode > IA_POISSON_LEARNED) return IA_ERR_INVALID;
+    if (cfg->poisson_mode == IA_POISSON_LEARNED) {   // the net pools twice in 3D
+        if (cfg->D != 3) return IA_ERR_UNSUPPORTED;
+        for (int d = 0; d < 3; ++d)
+            if (cfg->N[d] % 4 != 0) return IA_ERR_UNSUPPORTED;
+    }
     int ndev = 0;
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return IA_ERR_NO_DEVICE;
     ia_handle* h = new (std::nothrow) ia_handle();

@@ -10,7 +10,8 @@
 // Kernel families timed by the optional per-launch event instrumentation.
 enum TimedKernel { TK_VOF_BULK = 0, TK_VOF_LIST = 1, TK_MOM = 2, TK_FORCE = 3, TK_MG_SMOOTH = 4,
                    TK_MG_RESID = 5, TK_MG_TRANSFER = 6, TK_KRYLOV = 7, TK_OTHER = 8, TK_VOF_FACES = 9,
-                   TK_MOM_FLUX = 10, TK_MOM_UPDATE = 11, TK_UPDATE = 12, TK_MG_FINE = 13, TK_COUNT = 16 };
+                   TK_MOM_FLUX = 10, TK_MOM_UPDATE = 11, TK_UPDATE = 12, TK_MG_FINE = 13, TK_NN = 14,
+                   TK_COUNT = 16 };
 
 struct Timing {
     bool on = false;
@@ -23,6 +24,7 @@ struct Timing {
 
 struct MomScratch;    // momentum / projection scratch (momentum.cu)
 struct PoissonMG;     // multigrid hierarchy (poisson.cu)
+namespace ia { struct NNState; }   // learned preconditioner: weights, Adam state, buffers (nn.cu)
 
 struct ia_handle {
     ia_config cfg;
@@ -44,6 +46,7 @@ struct ia_handle {
     Timing timing;
     MomScratch* mom = nullptr;
     PoissonMG* mg = nullptr;
+    ia::NNState* nn = nullptr;
 };
 
 namespace ia {
@@ -62,4 +65,8 @@ int timing_begin(ia_handle* h, int family);
 void timing_end(ia_handle* h, int token);
 int extra_create(ia_handle* h);
 void extra_destroy(ia_handle* h);
+// learned preconditioner (nn.cu): out = net(r / max|r|, λρ·L) on a 3D grid, interior written
+int nn_apply(ia_handle* h, const float* r, const float* L32, float* out, int nx, int ny, int nz, long long ncomp);
+int nn_error_flag(ia_handle* h);
+void nn_destroy(ia_handle* h);
 }  // namespace ia

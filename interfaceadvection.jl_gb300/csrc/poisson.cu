@@ -19,7 +19,10 @@
 //
 // IA_POISSON_FP64 runs the V-cycle in FP64; IA_POISSON_MIXED runs it in FP32
 // (FP32 copies of every level's operator), the defect correction, matvec,
-// dot products and updates staying FP64.
+// dot products and updates staying FP64.  IA_POISSON_LEARNED keeps the MIXED
+// structure and preconditions the inner FCG with the conv net (nn.cu), composed
+// with the V-cycle (hybrid) or alone; an outer correction that fails to halve
+// the FP64 true residual switches the rest of the solve to the plain V-cycle.
 #include <cuda_runtime.h>
 
 #include <cmath>
@@ -439,6 +442,63 @@ __global__ void update32_k(Grid g, float alpha, const float* __restrict__ pv, co
     if (t == 0) atomicMax(linf, sm[0]);
 }
 
+// ---- learned hybrid preconditioner: t = A v with partial dots r·t and t·t
+__global__ void matvec32_dot2_k(Grid g, const float* __restrict__ L, const float* __restrict__ v,
+                                float* __restrict__ t, const float* __restrict__ r, double* __restrict__ partial,
+                                long long nblocks) {
+    __shared__ float s1[256], s2[256];
+    const int tt = threadIdx.y * blockDim.x + threadIdx.x;
+    float a1 = 0.f, a2 = 0.f;
+    {
+        const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y;
+        const int z = blockIdx.z;
+        const int c[3] = {x, y, z};
+        if (x < g.n[0] && y < g.n[1] && is_interior(g, c)) {
+            const long long I = lin(g, x, y, z);
+            float dd = 0.f;
+            for (int i = 0; i < g.D; ++i) dd -= L[I + i * g.N] + L[I + g.s[i] + i * g.N];
+            const float w = offdiag(g, L, v, I, c) + dd * v[I];
+            t[I] = w;
+            a1 = r[I] * w;
+            a2 = w * w;
+        }
+    }
+    s1[tt] = a1;
+    s2[tt] = a2;
+    __syncthreads();
+    for (int w = 128; w > 0; w >>= 1) {
+        if (tt < w) {
+            s1[tt] += s1[tt + w];
+            s2[tt] += s2[tt + w];
+        }
+        __syncthreads();
+    }
+    if (tt == 0) {
+        const long long b = (blockIdx.z * gridDim.y + blockIdx.y) * gridDim.x + blockIdx.x;
+        partial[b] = double(s1[0]);
+        partial[nblocks + b] = double(s2[0]);
+    }
+}
+
+// ω = (r·t)/(t·t) (0 unless t·t is positive and finite); b = r - ω t; ω stored for the sum
+__device__ __forceinline__ float hybrid_omega(const double* dots) {
+    const double rt = dots[0], t2 = dots[1];
+    const double w = (t2 > 0.0 && t2 < 1e300 && rt == rt) ? rt / t2 : 0.0;
+    return float(w);
+}
+__global__ void hybrid_resid_k(Grid g, const double* __restrict__ dots, const float* __restrict__ r,
+                               const float* __restrict__ t, float* __restrict__ b, float* __restrict__ om) {
+    INTERIOR_XYZ
+    const float w = hybrid_omega(dots);
+    if (x == 1 && y == 1 && (g.D == 2 || z == 1)) *om = w;
+    b[I] = r[I] - w * t[I];
+}
+// s += ω n
+__global__ void add_scaled_k(Grid g, const float* __restrict__ om, const float* __restrict__ nv, float* __restrict__ sv) {
+    INTERIOR_XYZ
+    sv[I] += (*om) * nv[I];
+}
+
 // x += e (FP64 += FP32), interior cells
 __global__ void add_correction_k(Grid g, const float* __restrict__ e, double* __restrict__ xv) {
     INTERIOR_XYZ
@@ -514,7 +574,7 @@ int mg_create(ia_handle* h) {
     h->mg = mg;
     const Grid& g0 = h->g;
     long long Nint[3] = {g0.n[0] - 2, g0.n[1] - 2, g0.D == 3 ? g0.n[2] - 2 : 1};
-    const bool mixed = h->cfg.poisson_mode == IA_POISSON_MIXED;
+    const bool mixed = h->cfg.poisson_mode != IA_POISSON_FP64;
     int nl = 0;
     while (nl < MG_MAX_LEVELS) {
         int64_t N[3] = {Nint[0], Nint[1], Nint[2]};
@@ -580,6 +640,16 @@ int mg_create(ia_handle* h) {
             cudaMemset(mg->e32, 0, 4 * N);
         }
     }
+    if (h->cfg.poisson_mode == IA_POISSON_LEARNED) {
+        e = e ? e : cudaMalloc(&mg->rl32, 4 * N);
+        e = e ? e : cudaMalloc(&mg->nl32, 4 * N);
+        e = e ? e : cudaMalloc(&mg->t32, 4 * N);
+        if (!e) {   // ghosts stay zero: only interior cells are written
+            cudaMemset(mg->rl32, 0, 4 * N);
+            cudaMemset(mg->nl32, 0, 4 * N);
+            cudaMemset(mg->t32, 0, 4 * N);
+        }
+    }
     e = e ? e : cudaMalloc(&mg->dsc, 8 * 16);
     e = e ? e : cudaMallocHost(&mg->hsc, 8 * 16);
     if (e != cudaSuccess) return IA_ERR_CUDA;
@@ -603,6 +673,7 @@ void mg_destroy(ia_handle* h) {
     }
     cudaFree(mg->r); cudaFree(mg->s); cudaFree(mg->p); cudaFree(mg->q);
     cudaFree(mg->p32); cudaFree(mg->q32); cudaFree(mg->e32);
+    cudaFree(mg->rl32); cudaFree(mg->nl32); cudaFree(mg->t32);
     cudaFree(mg->partial); cudaFree(mg->dsc);
     if (mg->hsc) cudaFreeHost(mg->hsc);
     delete mg;
@@ -613,7 +684,7 @@ void mg_destroy(ia_handle* h) {
 static cudaError_t mg_setup(ia_handle* h, const double* L0) {
     PoissonMG* mg = h->mg;
     cudaStream_t st = h->stream;
-    const bool mixed = h->cfg.poisson_mode == IA_POISSON_MIXED;
+    const bool mixed = h->cfg.poisson_mode != IA_POISSON_FP64;
     MGLevel& F = mg->lev[0];
     const long long nv = F.g.N * F.g.D;
     if (!mixed) {
@@ -643,7 +714,7 @@ static cudaError_t mg_precondition(ia_handle* h) {
     MGLevel& F = mg->lev[0];
     const long long N = F.g.N;
     cudaError_t e;
-    if (h->cfg.poisson_mode == IA_POISSON_MIXED) {
+    if (h->cfg.poisson_mode != IA_POISSON_FP64) {
         int tk = timing_begin(h, TK_MG_TRANSFER);
         { to_f32_k<<<1216, 256, 0, st>>>(N, mg->r, F.b32); ia::note_launch(); }
         timing_end(h, tk);
@@ -684,9 +755,10 @@ static double read_linf32(ia_handle* h, unsigned int* d) {
 }
 
 // Mixed precision: FP64 defect correction x += e, e from an inner flexible CG run
-// entirely in FP32 (operator, V-cycle, vectors) on A e = r, started from the FP64
+// entirely in FP32 (operator, preconditioner, vectors) on A e = r, started from the FP64
 // true residual; inner dot products are block sums in FP32 reduced across blocks in
-// FP64 and the CG scalars are FP64.
+// FP64 and the CG scalars are FP64.  The inner preconditioner is the FP32 V-cycle
+// (IA_POISSON_MIXED) or, for IA_POISSON_LEARNED, the mode set by ia_poisson_precond.
 static int poisson_solve_mixed(ia_handle* h, double* xv, const double* zz, const double* L, double tol, int itmx,
                                int* iters, double* resid) {
     PoissonMG* mg = h->mg;
@@ -698,8 +770,55 @@ static int poisson_solve_mixed(ia_handle* h, double* xv, const double* zz, const
     unsigned long long* dlinf = reinterpret_cast<unsigned long long*>(mg->dsc + 8);
     unsigned int* dlinf32 = reinterpret_cast<unsigned int*>(mg->dsc + 9);
     double* dots = mg->dsc;
-    float* rr = F.b32;    // inner residual (the V-cycle reads its right-hand side here)
-    float* sv = F.x32;    // V-cycle output = preconditioned residual
+    double* hdots = mg->dsc + 12;                                  // hybrid r·t, t·t
+    float* omega = reinterpret_cast<float*>(mg->dsc + 14);
+    const bool learned = h->cfg.poisson_mode == IA_POISSON_LEARNED;
+    // inner residual: the V-cycle reads its right-hand side from F.b32, so the plain mixed
+    // mode keeps the residual there; the learned modes keep it apart
+    float* rr = learned ? mg->rl32 : F.b32;
+    int mode = learned ? mg->precond : IA_PRECOND_VCYCLE;
+    auto vcyc = [&]() -> cudaError_t {
+        const int tk = timing_begin(h, TK_MG_SMOOTH);
+        const cudaError_t e = vcycle<float>(h, mg, 0, st, mg->nu1, mg->nu2, mg->nuc);
+        timing_end(h, tk);
+        mg->stats[1]++;
+        return e;
+    };
+    auto net = [&]() -> bool {
+        const int tk = timing_begin(h, TK_NN);
+        const int rc = nn_apply(h, rr, F.L32, mg->nl32, g.n[0] - 2, g.n[1] - 2, g.n[2] - 2, N);
+        timing_end(h, tk);
+        mg->stats[0]++;
+        return rc == IA_OK;
+    };
+    // sv ≈ A⁻¹ rr
+    auto precond = [&](float*& sv) -> bool {
+        if (mode == IA_PRECOND_NONE) {
+            sv = rr;
+            return true;
+        }
+        if (mode == IA_PRECOND_NET) {
+            sv = mg->nl32;
+            return net();
+        }
+        if (mode == IA_PRECOND_HYBRID) {
+            if (!net()) return false;
+            int tk = timing_begin(h, TK_KRYLOV);
+            { matvec32_dot2_k<<<gb, blk(), 0, st>>>(g, F.L32, mg->nl32, mg->t32, rr, mg->partial, mg->nblocks); ia::note_launch(); }
+            { finalize_k<<<1, 1024, 0, st>>>(mg->partial, mg->nblocks, 2, hdots); ia::note_launch(); }
+            { hybrid_resid_k<<<gb, blk(), 0, st>>>(g, hdots, rr, mg->t32, F.b32, omega); ia::note_launch(); }
+            timing_end(h, tk);
+            if (vcyc() != cudaSuccess) return false;
+            tk = timing_begin(h, TK_KRYLOV);
+            { add_scaled_k<<<gb, blk(), 0, st>>>(g, omega, mg->nl32, F.x32); ia::note_launch(); }
+            timing_end(h, tk);
+            sv = F.x32;
+            return cudaGetLastError() == cudaSuccess;
+        }
+        if (rr != F.b32) cudaMemcpyAsync(F.b32, rr, 4 * N, cudaMemcpyDeviceToDevice, st);
+        sv = F.x32;
+        return vcyc() == cudaSuccess;
+    };
     int total = 0;
     cudaMemsetAsync(dlinf, 0, 8, st);
     int tk = timing_begin(h, TK_KRYLOV);
@@ -714,10 +833,8 @@ static int poisson_solve_mixed(ia_handle* h, double* xv, const double* zz, const
         const double target = std::fmax(0.5 * tol / res, mg->inner_rtol) * res;
         double rho_prev = 0.0, alpha_prev = 0.0;
         for (int it = 0; it < mg->inner_max && total < itmx; ++it) {
-            tk = timing_begin(h, TK_MG_SMOOTH);
-            cudaError_t e = vcycle<float>(h, mg, 0, st, mg->nu1, mg->nu2, mg->nuc);
-            timing_end(h, tk);
-            if (e != cudaSuccess) return IA_ERR_CUDA;
+            float* sv = nullptr;
+            if (!precond(sv)) return IA_ERR_CUDA;
             tk = timing_begin(h, TK_KRYLOV);
             { dot2_32_k<<<gb, blk(), 0, st>>>(g, sv, mg->q32, rr, mg->partial, mg->nblocks); ia::note_launch(); }
             { finalize_k<<<1, 1024, 0, st>>>(mg->partial, mg->nblocks, 2, dots); ia::note_launch(); }
@@ -735,7 +852,8 @@ static int poisson_solve_mixed(ia_handle* h, double* xv, const double* zz, const
             if (cudaStreamSynchronize(st) != cudaSuccess) return IA_ERR_CUDA;
             const double pq = mg->hsc[2];
             ++total;
-            if (!(pq != 0.0) || !std::isfinite(pq)) break;
+            mg->stats[3]++;
+            if (!(pq != 0.0) || !std::isfinite(pq) || !std::isfinite(sr) || !std::isfinite(beta)) break;
             const double alpha = sr / pq;
             cudaMemsetAsync(dlinf32, 0, 4, st);
             tk = timing_begin(h, TK_KRYLOV);
@@ -751,7 +869,15 @@ static int poisson_solve_mixed(ia_handle* h, double* xv, const double* zz, const
         cudaMemsetAsync(dlinf, 0, 8, st);
         { true_resid_k<<<gb, blk(), 0, st>>>(g, L, zz, xv, mg->r, dlinf); ia::note_launch(); }
         timing_end(h, tk);
+        const double res_old = res;
         res = read_linf(h, dlinf);
+        mg->stats[4]++;
+        // fallback: a correction that fails to halve the FP64 true residual (or a net
+        // kernel that reported a timeout) hands the rest of the solve to the V-cycle
+        if (learned && mode != IA_PRECOND_VCYCLE && (!(res <= 0.5 * res_old) || nn_error_flag(h))) {
+            mode = IA_PRECOND_VCYCLE;
+            mg->stats[2]++;
+        }
     }
     { perbc_k<<<gb, blk(), 0, st>>>(g, xv); ia::note_launch(); }
     if (cudaGetLastError() != cudaSuccess) return IA_ERR_CUDA;
@@ -765,7 +891,7 @@ int poisson_solve(ia_handle* h, double* xv, const double* zz, const double* L, d
                   double* resid) {
     PoissonMG* mg = h->mg;
     if (!mg) return IA_ERR_INVALID;
-    if (h->cfg.poisson_mode == IA_POISSON_MIXED) {
+    if (h->cfg.poisson_mode != IA_POISSON_FP64) {
         if (mg_setup(h, L) != cudaSuccess) return IA_ERR_CUDA;
         return poisson_solve_mixed(h, xv, zz, L, tol, itmx, iters, resid);
     }

@@ -40,6 +40,9 @@ struct PoissonMG {
     ia::MGLevel lev[ia::MG_MAX_LEVELS];
     double *r = nullptr, *s = nullptr, *p = nullptr, *q = nullptr;   // fine-level Krylov vectors (FP64)
     float *p32 = nullptr, *q32 = nullptr, *e32 = nullptr;             // inner FP32 Krylov vectors (mixed)
+    float *rl32 = nullptr, *nl32 = nullptr, *t32 = nullptr;           // learned: residual, net output, A·net
+    int precond = 0;                                                  // IA_PRECOND_* of the learned mode
+    long long stats[5] = {0, 0, 0, 0, 0};                             // net, V-cycles, fallbacks, inner, outer
     int inner_max = 30;                                               // inner FCG iterations per correction
     double inner_rtol = 1e-4;                                         // inner relative residual target
     double* partial = nullptr;                                        // per-block dot partials

@@ -65,6 +65,7 @@ static int ensure_scratch(ia_handle* h) {
 
 void extra_destroy(ia_handle* h) {
     mg_destroy(h);
+    nn_destroy(h);
     MomScratch* m = h->mom;
     if (!m) return;
     cudaFree(m->ustar);
@@ -278,6 +279,24 @@ int ia_poisson_solve(ia_handle* h, double* x, const double* z, const double* L, 
     if (iters) *iters = it;
     if (resid) *resid = r;
     return rc;
+}
+
+int ia_poisson_precond(ia_handle* h, int32_t precond, int32_t inner_max, double inner_rtol) {
+    if (!h || precond < IA_PRECOND_HYBRID || precond > IA_PRECOND_VCYCLE || inner_max < 1 ||
+        !(inner_rtol > 0.0 && inner_rtol < 1.0))
+        return IA_ERR_INVALID;
+    if (h->cfg.poisson_mode != IA_POISSON_LEARNED) return IA_ERR_UNSUPPORTED;
+    if (ensure_scratch(h) != IA_OK) return IA_ERR_CUDA;
+    h->mg->precond = precond;
+    h->mg->inner_max = inner_max;
+    h->mg->inner_rtol = inner_rtol;
+    return IA_OK;
+}
+
+int ia_poisson_stats(ia_handle* h, int64_t* out5) {
+    if (!h || !out5) return IA_ERR_INVALID;
+    for (int i = 0; i < 5; ++i) out5[i] = h->mg ? h->mg->stats[i] : 0;
+    return IA_OK;
 }
 
 int ia_project(ia_handle* h, const double* f, double dtp, int32_t* iters, double* resid) {

@@ -9,9 +9,10 @@ from ._build import build
 from .core import (Flow, Handle, advect, advect_vof_raw, advectVOF, apply_vof, applyVOF, cVOF, get_vof_flux,
                    getVOFFlux, make_config, reconstruct_interface, reconstructInterface)
 from .fields import cell_coords, face_coords, ffrom, fones, fzeros, is_fortran
-from .simulation import MPCFL, MPFMomStep, NoBody, TwoPhaseSimulation, sim_info, sim_step
+from .simulation import (MPCFL, MPFMomStep, NoBody, TwoPhaseSimulation, poisson_stats, set_learned, sim_info,
+                         sim_step)
 
 __all__ = ["Flow", "Handle", "advect", "advect_vof_raw", "advectVOF", "apply_vof", "applyVOF", "cVOF",
            "get_vof_flux", "getVOFFlux", "make_config", "reconstruct_interface", "reconstructInterface", "build",
            "cell_coords", "face_coords", "ffrom", "fones", "fzeros", "is_fortran", "MPCFL", "MPFMomStep", "NoBody",
-           "TwoPhaseSimulation", "sim_info", "sim_step"]
+           "TwoPhaseSimulation", "sim_info", "sim_step", "poisson_stats", "set_learned"]

@@ -29,9 +29,10 @@ FLAG_NAN, FLAG_OVERFILL, FLAG_UNDERFILL, FLAG_DIVERGENCE, FLAG_POISSON = 1, 2, 4
 NORMAL_SCHEMES = {"WH": 0, "WY": 1, "MYC": 2, "Y": 3, "Column": 4, "PCD": 5, "SLIC": 6, "CD": 7, "XYLIC": 8}
 LIMITERS = {"Koren": 0, "upwind": 1, "minmod": 2, "vanAlbada1": 3, "Sweby": 4, "superbee": 5,
             "TVDcen": 6, "TVDdown": 7}
-POISSON_MODES = {"fp64": 0, "mixed": 1}
+POISSON_MODES = {"fp64": 0, "mixed": 1, "learned": 2}
+PRECONDS = {"hybrid": 0, "net": 1, "none": 2, "vcycle": 3}
 TIMED_KERNELS = ["vof_bulk", "vof_cells", "ustar", "forcing", "mg_vcycle", "mg_residual", "mg_transfer",
-                 "krylov", "other", "vof_faces", "momflux", "momupdate", "update_project", "mg_fine_rbgs"]
+                 "krylov", "other", "vof_faces", "momflux", "momupdate", "update_project", "mg_fine_rbgs", "nn_precond"]
 
 
 class Config(C.Structure):
@@ -78,6 +79,16 @@ _SIGS = {
     "ia_visc_surften": (C.c_int, [C.c_void_p, C.c_void_p]),
     "ia_advect_vof_noalloc": (C.c_int, [C.POINTER(Config), C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                         C.c_double, C.c_int64, C.c_void_p, C.c_void_p, C.POINTER(Status)]),
+    "ia_nn_param_count": (C.c_int64, []),
+    "ia_nn_set_params": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "ia_nn_get_params": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "ia_nn_forward": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p] + [C.c_int32] * 5),
+    "ia_nn_loss_grad": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p] + [C.c_int32] * 4 +
+                        [C.c_void_p, C.POINTER(C.c_double)]),
+    "ia_nn_train_step": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p] + [C.c_int32] * 4 +
+                         [C.c_float, C.POINTER(C.c_double)]),
+    "ia_poisson_precond": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.c_double]),
+    "ia_poisson_stats": (C.c_int, [C.c_void_p, C.c_void_p]),
 }
 
 _lib = None

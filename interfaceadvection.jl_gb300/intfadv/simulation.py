@@ -30,11 +30,16 @@ class TwoPhaseSimulation:
     SDF (dark fluid where negative).  ``poisson`` selects "fp64" (FP64 V-cycles) or "mixed"
     (FP32 V-cycles inside FP64 flexible CG); ``poisson_tol`` is the L∞ residual of the
     dt-scaled pressure system (the reference passes tol=1e-4 to WaterLily's solver!).
+    ``poisson="learned"`` (3D, dims multiples of 4) preconditions the inner FCG of the mixed
+    solver with the conv net: ``precond`` is "hybrid" (net then V-cycle), "net", "none" or
+    "vcycle"; ``nn_weights`` a parameter vector or a weights file (default: the trained
+    weights shipped with the package).
     """
 
     def __init__(self, dims, u_BC, L, *, U=None, Δt=0.25, ν=0.0, g=None, u0=None, perdir=(), exitBC=False,
                  λμ=1e-2, λρ=1e-3, η=None, InterfaceSDF=None, λ="Koren", normalScheme="WH", T=FP64,
-                 poisson="fp64", poisson_tol=1e-4, poisson_itmx=200, device="cuda", body=None, ϵ=1):
+                 poisson="fp64", poisson_tol=1e-4, poisson_itmx=200, device="cuda", body=None, ϵ=1,
+                 precond="hybrid", nn_weights=None, inner_max=30, inner_rtol=1e-4):
         if T != FP64:
             raise NotImplementedError("the GB300 path computes in FP64 (Poisson V-cycles optionally FP32)")
         if exitBC:
@@ -59,6 +64,8 @@ class TwoPhaseSimulation:
         self.handle.bind(u=fl.u, u0=fl.u0, force=fl.f, sigma=fl.sigma, p=fl.p, mu0=fl.mu0, f=it.f, f0=it.f0,
                          alpha=it.alpha, nhat=it.nhat, fF=it.fF, rhou=it.rhou, rhouf=it.rhouf, drho=it.drho,
                          cbar=it.cbar)
+        if poisson == "learned":
+            set_learned(self.handle, precond=precond, weights=nn_weights, inner_max=inner_max, inner_rtol=inner_rtol)
         _lib.check(self.handle.call("ia_bc_velocity", ptr(fl.u)), "ia_bc_velocity")   # Flow: BC!(u)
         fl.u0.copy_(fl.u)
         fl.Δt[-1] = min(fl.Δt[-1], MPCFL(self))                                       # :81
@@ -72,6 +79,33 @@ class TwoPhaseSimulation:
 
     def sim_time(self) -> float:
         return sum(self.flow.Δt[:-1]) * (self.U / self.L if self.L else 1.0)
+
+
+def set_learned(handle, precond="hybrid", weights=None, inner_max=30, inner_rtol=1e-4):
+    """Load the net parameters into a learned-mode handle and select its inner preconditioner."""
+    import os
+
+    import numpy as np
+
+    from . import learned
+    if weights is None:
+        if os.path.exists(learned.WEIGHTS):
+            weights = learned.WEIGHTS
+        else:
+            warnings.warn("no trained weights for the learned preconditioner: the net outputs zero and the "
+                          "hybrid preconditioner reduces to the V-cycle")
+    if weights is not None:
+        w = learned.load_params(weights)[0] if isinstance(weights, str) else np.asarray(weights, np.float32)
+        learned.Net(handle).set_params(w)
+    _lib.check(handle.call("ia_poisson_precond", _lib.PRECONDS[precond] if isinstance(precond, str) else int(precond),
+                           int(inner_max), float(inner_rtol)), "ia_poisson_precond")
+
+
+def poisson_stats(handle) -> dict:
+    """Counters of the Poisson solver: net applications, V-cycles, fallbacks, inner and outer iterations."""
+    out = (C.c_int64 * 5)()
+    _lib.check(handle.call("ia_poisson_stats", out), "ia_poisson_stats")
+    return dict(zip(("net", "vcycles", "fallbacks", "inner", "outer"), list(out)))
 
 
 def MPCFL(sim) -> float:

@@ -18,6 +18,7 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 SRC = os.path.join(HERE, "oracle.cpp")
+SRC_NN = os.path.join(HERE, "nn_oracle.cpp")
 LIB = os.path.join(HERE, "liboracle.so")
 
 SCHEMES = {"WH": 0, "WY": 1, "MYC": 2, "Y": 3, "Column": 4, "PCD": 5, "SLIC": 6, "CD": 7, "XYLIC": 8}
@@ -28,9 +29,9 @@ LIMITERS = {"Koren": 0, "upwind": 1, "minmod": 2, "vanAlbada1": 3, "Sweby": 4, "
 def build(force: bool = False) -> str:
     """Compile liboracle.so with g++ (OpenMP, IEEE FP64, no FMA contraction)."""
     if force or not os.path.exists(LIB) or os.path.getmtime(LIB) < max(
-            os.path.getmtime(SRC), os.path.getmtime(os.path.join(HERE, "oracle.h"))):
+            os.path.getmtime(SRC), os.path.getmtime(SRC_NN), os.path.getmtime(os.path.join(HERE, "oracle.h"))):
         cmd = ["g++", "-std=c++17", "-O2", "-fopenmp", "-ffp-contract=off", "-fPIC", "-shared",
-               SRC, "-o", LIB + ".tmp"]
+               SRC, SRC_NN, "-o", LIB + ".tmp"]
         subprocess.run(cmd, check=True)
         os.replace(LIB + ".tmp", LIB)
     return LIB
@@ -87,6 +88,10 @@ def lib():
             "orc_argabsmax": (i, [i, p]), "orc_get_xdir": (i, [i]), "orc_get_xydir": (None, [i, p, p]),
             "orc_getrho_cell": (d, [d, d]), "orc_getrho_face": (d, [p, i, i64, p, d]),
             "orc_vof_flux_face": (None, [p, p, p, p, p, d, i, i64, p, d]),
+            "orc_nn_param_count": (i64, []),
+            "orc_nn_forward": (None, [p, p, i, i, i, i, p]),
+            "orc_nn_loss_grad": (d, [p, p, p, i, i, i, i, p]),
+            "orc_nn_adam": (None, [i64, p, p, p, p, d, i64]),
         }
         for name, (res, args) in sig.items():
             fn = getattr(L, name)
@@ -179,3 +184,42 @@ def advect_vof(f, u, u0, dt, dirO, lrho=1e-3, scheme="WH", per=(), fF=None, alph
 def dir_order(n_dt: int, D: int):
     """Split order of advect!/advectfq!: dirO[i] = mod(length(Δt)+i, D) (0-based)."""
     return [(n_dt + i) % D for i in range(1, D + 1)]
+
+
+# ---- learned preconditioner network (nn_oracle.cpp) -------------------------------------------
+
+def _c64(a):
+    a = np.ascontiguousarray(a, dtype=np.float64)
+    return a, a.ctypes.data
+
+
+def nn_param_count() -> int:
+    return int(lib().orc_nn_param_count())
+
+
+def nn_forward(w, x0):
+    """x0: C-ordered [B, nz+2, ny+2, nx+2, 4]; returns [B, nz+2, ny+2, nx+2] (FP64)."""
+    B, nzp, nyp, nxp, _ = x0.shape
+    w, pw = _c64(w)
+    x0, px = _c64(x0)
+    out = np.zeros((B, nzp, nyp, nxp), dtype=np.float64)
+    lib().orc_nn_forward(pw, px, B, nxp - 2, nyp - 2, nzp - 2, out.ctypes.data)
+    return out
+
+
+def nn_loss_grad(w, x0, tgt):
+    """MSE loss over interior cells and its gradient (FP64)."""
+    B, nzp, nyp, nxp, _ = x0.shape
+    w, pw = _c64(w)
+    x0, px = _c64(x0)
+    tgt, pt = _c64(tgt)
+    g = np.zeros(w.size, dtype=np.float64)
+    loss = lib().orc_nn_loss_grad(pw, px, pt, B, nxp - 2, nyp - 2, nzp - 2, g.ctypes.data)
+    return float(loss), g
+
+
+def nn_adam(w, g, m, v, lr, t):
+    """One Adam step in place on FP64 arrays (t = step number, from 1)."""
+    for a in (w, g, m, v):
+        assert a.dtype == np.float64 and a.flags.c_contiguous
+    lib().orc_nn_adam(w.size, w.ctypes.data, g.ctypes.data, m.ctypes.data, v.ctypes.data, float(lr), int(t))
