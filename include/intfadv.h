@@ -71,7 +71,7 @@ extern "C" {
 #define IA_POISSON_LEARNED 2   /* as MIXED, inner FCG preconditioned by the conv net  */
 
 /* Inner preconditioner of IA_POISSON_LEARNED (ia_poisson_precond) */
-#define IA_PRECOND_HYBRID  0   /* s1 = ω·net(r); s = s1 + Vcycle(r - A s1), ω least squares */
+#define IA_PRECOND_HYBRID  0   /* s = Vcycle(r); s += ω·net(r - A s), ω least squares      */
 #define IA_PRECOND_NET     1   /* s = net(r)                                           */
 #define IA_PRECOND_NONE    2   /* s = r (plain CG; the ablation baseline)               */
 #define IA_PRECOND_VCYCLE  3   /* s = Vcycle(r) (the fallback)                          */
@@ -200,6 +200,11 @@ int ia_bc_velocity(ia_handle* h, double* a);
  * iterations (IA_WARN_NOT_CONVERGED). */
 int ia_poisson_solve(ia_handle* h, double* x, const double* z, const double* L, double tol,
                      int32_t itmx, int32_t* iters, double* resid);
+
+/* Residual of that pressure system, r = z - A x on interior cells, and its L-infinity norm
+ * (the quantity ia_poisson_solve's stopping test measures; src/flow.jl:343-347). */
+int ia_poisson_residual(ia_handle* h, double* r, const double* x, const double* z, const double* L,
+                        double* linf);
 
 /* updateL!(μ₀, f) + myproject!(flow, pois, w) — src/flow.jl:254-259, 328-347, with
  * dtp = w·last(Δt), on the bound u, p, sigma (source) and mu0; then BC!(u). */

@@ -410,9 +410,11 @@ __global__ void dot2_32_k(Grid g, const float* __restrict__ sv, const float* __r
     }
 }
 
+// p = s + β p; β = 0 restarts from s without reading the old direction (which a rejected
+// preconditioner output may have left non-finite)
 __global__ void xpby32_k(Grid g, const float* __restrict__ sv, float beta, float* __restrict__ pv) {
     INTERIOR_XYZ
-    pv[I] = sv[I] + beta * pv[I];
+    pv[I] = (beta == 0.f) ? sv[I] : sv[I] + beta * pv[I];
 }
 
 // e += α p ; r -= α q ; L∞(r) as float bits
@@ -480,23 +482,13 @@ __global__ void matvec32_dot2_k(Grid g, const float* __restrict__ L, const float
     }
 }
 
-// ω = (r·t)/(t·t) (0 unless t·t is positive and finite); b = r - ω t; ω stored for the sum
-__device__ __forceinline__ float hybrid_omega(const double* dots) {
-    const double rt = dots[0], t2 = dots[1];
-    const double w = (t2 > 0.0 && t2 < 1e300 && rt == rt) ? rt / t2 : 0.0;
-    return float(w);
-}
-__global__ void hybrid_resid_k(Grid g, const double* __restrict__ dots, const float* __restrict__ r,
-                               const float* __restrict__ t, float* __restrict__ b, float* __restrict__ om) {
+// s += ω n with ω = (t·An)/(An·An) from the device dots (0 unless An·An is positive and finite)
+__global__ void add_scaled_k(Grid g, const double* __restrict__ dots, const float* __restrict__ nv,
+                             float* __restrict__ sv) {
     INTERIOR_XYZ
-    const float w = hybrid_omega(dots);
-    if (x == 1 && y == 1 && (g.D == 2 || z == 1)) *om = w;
-    b[I] = r[I] - w * t[I];
-}
-// s += ω n
-__global__ void add_scaled_k(Grid g, const float* __restrict__ om, const float* __restrict__ nv, float* __restrict__ sv) {
-    INTERIOR_XYZ
-    sv[I] += (*om) * nv[I];
+    const double tn = dots[0], n2 = dots[1];
+    const float w = float((n2 > 0.0 && n2 < 1e300 && tn == tn) ? tn / n2 : 0.0);
+    sv[I] += w * nv[I];
 }
 
 // x += e (FP64 += FP32), interior cells
@@ -770,8 +762,7 @@ static int poisson_solve_mixed(ia_handle* h, double* xv, const double* zz, const
     unsigned long long* dlinf = reinterpret_cast<unsigned long long*>(mg->dsc + 8);
     unsigned int* dlinf32 = reinterpret_cast<unsigned int*>(mg->dsc + 9);
     double* dots = mg->dsc;
-    double* hdots = mg->dsc + 12;                                  // hybrid r·t, t·t
-    float* omega = reinterpret_cast<float*>(mg->dsc + 14);
+    double* hdots = mg->dsc + 12;                                  // hybrid t·An, An·An
     const bool learned = h->cfg.poisson_mode == IA_POISSON_LEARNED;
     // inner residual: the V-cycle reads its right-hand side from F.b32, so the plain mixed
     // mode keeps the residual there; the learned modes keep it apart
@@ -784,9 +775,9 @@ static int poisson_solve_mixed(ia_handle* h, double* xv, const double* zz, const
         mg->stats[1]++;
         return e;
     };
-    auto net = [&]() -> bool {
+    auto net = [&](const float* in) -> bool {
         const int tk = timing_begin(h, TK_NN);
-        const int rc = nn_apply(h, rr, F.L32, mg->nl32, g.n[0] - 2, g.n[1] - 2, g.n[2] - 2, N);
+        const int rc = nn_apply(h, in, F.L32, mg->nl32, g.n[0] - 2, g.n[1] - 2, g.n[2] - 2, N);
         timing_end(h, tk);
         mg->stats[0]++;
         return rc == IA_OK;
@@ -799,25 +790,24 @@ static int poisson_solve_mixed(ia_handle* h, double* xv, const double* zz, const
         }
         if (mode == IA_PRECOND_NET) {
             sv = mg->nl32;
-            return net();
-        }
-        if (mode == IA_PRECOND_HYBRID) {
-            if (!net()) return false;
-            int tk = timing_begin(h, TK_KRYLOV);
-            { matvec32_dot2_k<<<gb, blk(), 0, st>>>(g, F.L32, mg->nl32, mg->t32, rr, mg->partial, mg->nblocks); ia::note_launch(); }
-            { finalize_k<<<1, 1024, 0, st>>>(mg->partial, mg->nblocks, 2, hdots); ia::note_launch(); }
-            { hybrid_resid_k<<<gb, blk(), 0, st>>>(g, hdots, rr, mg->t32, F.b32, omega); ia::note_launch(); }
-            timing_end(h, tk);
-            if (vcyc() != cudaSuccess) return false;
-            tk = timing_begin(h, TK_KRYLOV);
-            { add_scaled_k<<<gb, blk(), 0, st>>>(g, omega, mg->nl32, F.x32); ia::note_launch(); }
-            timing_end(h, tk);
-            sv = F.x32;
-            return cudaGetLastError() == cudaSuccess;
+            return net(rr);
         }
         if (rr != F.b32) cudaMemcpyAsync(F.b32, rr, 4 * N, cudaMemcpyDeviceToDevice, st);
         sv = F.x32;
-        return vcyc() == cudaSuccess;
+        if (vcyc() != cudaSuccess) return false;
+        if (mode != IA_PRECOND_HYBRID) return true;
+        // hybrid: the net corrects what the V-cycle left, s += ω net(t) with t = r - A s and
+        // ω minimising |t - ω A net(t)|
+        int tk = timing_begin(h, TK_KRYLOV);
+        { residual_k<float><<<gb, blk(), 0, st>>>(g, F.L32, rr, F.x32, mg->t32); ia::note_launch(); }
+        timing_end(h, tk);
+        if (!net(mg->t32)) return false;
+        tk = timing_begin(h, TK_KRYLOV);
+        { matvec32_dot2_k<<<gb, blk(), 0, st>>>(g, F.L32, mg->nl32, F.r32, mg->t32, mg->partial, mg->nblocks); ia::note_launch(); }
+        { finalize_k<<<1, 1024, 0, st>>>(mg->partial, mg->nblocks, 2, hdots); ia::note_launch(); }
+        { add_scaled_k<<<gb, blk(), 0, st>>>(g, hdots, mg->nl32, F.x32); ia::note_launch(); }
+        timing_end(h, tk);
+        return cudaGetLastError() == cudaSuccess;
     };
     int total = 0;
     cudaMemsetAsync(dlinf, 0, 8, st);
@@ -884,6 +874,19 @@ static int poisson_solve_mixed(ia_handle* h, double* xv, const double* zz, const
     *iters = total;
     *resid = res;
     return (res <= tol) ? IA_OK : IA_WARN_NOT_CONVERGED;
+}
+
+// r = z - A x over interior cells; L∞(r) to the host
+int poisson_residual(ia_handle* h, double* r, const double* x, const double* z, const double* L, double* linf) {
+    cudaStream_t st = h->stream;
+    unsigned long long* d = reinterpret_cast<unsigned long long*>(h->dscalar + 60);
+    cudaMemsetAsync(d, 0, 8, st);
+    { true_resid_k<<<grd(h->g), blk(), 0, st>>>(h->g, L, z, x, r, d); ia::note_launch(); }
+    unsigned long long v = 0;
+    cudaMemcpyAsync(&v, d, 8, cudaMemcpyDeviceToHost, st);
+    if (cudaStreamSynchronize(st) != cudaSuccess) return IA_ERR_CUDA;
+    if (linf) std::memcpy(linf, &v, 8);
+    return IA_OK;
 }
 
 // Solve A x = z to L∞(z - A x) <= tol (x holds the initial guess); L = μ₀.

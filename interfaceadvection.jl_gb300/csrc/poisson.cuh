@@ -57,4 +57,5 @@ int mg_create(ia_handle* h);
 void mg_destroy(ia_handle* h);
 int poisson_solve(ia_handle* h, double* x, const double* z, const double* L, double tol, int itmx, int* iters,
                   double* resid);
+int poisson_residual(ia_handle* h, double* r, const double* x, const double* z, const double* L, double* linf);
 }  // namespace ia

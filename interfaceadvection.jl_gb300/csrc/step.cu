@@ -281,6 +281,11 @@ int ia_poisson_solve(ia_handle* h, double* x, const double* z, const double* L, 
     return rc;
 }
 
+int ia_poisson_residual(ia_handle* h, double* r, const double* x, const double* z, const double* L, double* linf) {
+    if (!h || !r || !x || !z || !L) return IA_ERR_INVALID;
+    return poisson_residual(h, r, x, z, L, linf);
+}
+
 int ia_poisson_precond(ia_handle* h, int32_t precond, int32_t inner_max, double inner_rtol) {
     if (!h || precond < IA_PRECOND_HYBRID || precond > IA_PRECOND_VCYCLE || inner_max < 1 ||
         !(inner_rtol > 0.0 && inner_rtol < 1.0))

@@ -177,7 +177,7 @@ def bubbles_sdf(bubbles):
 
 
 class PatchSolver:
-    """FP64 multigrid solve of a P³ patch system with walls on the patch boundary."""
+    """FP64 multigrid-preconditioned CG on a P³ patch system with walls on the patch boundary."""
 
     def __init__(self, P: int, device="cuda", tol_rel=1e-6, itmx=200):
         self.P = P
@@ -185,13 +185,14 @@ class PatchSolver:
         ng = (P + 2,) * 3
         self.x = fzeros(ng, device=device)
         self.z = fzeros(ng, device=device)
+        self.r = fzeros(ng, device=device)
         self.L = fzeros(ng + (3,), device=device)
         self.tol_rel, self.itmx = tol_rel, itmx
+        self.tol = 0.0
 
-    def solve(self, r: torch.Tensor, L: torch.Tensor):
-        """r: P³ interior residual; L: (P, P, P, 3) lower-face coefficients of the patch cells.
-        Returns the mean-free correction e (P³) and the iteration count."""
-        self.x.zero_()
+    def set_system(self, r: torch.Tensor, L: torch.Tensor) -> float:
+        """r: P³ right-hand side (made mean-free); L: (P, P, P, 3) lower-face coefficients of the
+        patch cells (the patch's own boundary faces become walls).  Returns max|r|."""
         self.z.zero_()
         self.L.zero_()
         rm = r - r.mean()
@@ -200,31 +201,48 @@ class PatchSolver:
         self.L[1, :, :, 0] = 0.0
         self.L[:, 1, :, 1] = 0.0
         self.L[:, :, 1, 2] = 0.0
+        s = float(rm.abs().max())
+        self.tol = self.tol_rel * s
+        return s
+
+    def run(self, itmx=None):
+        """CG from zero for at most itmx iterations (default: to tol_rel); returns the iterations."""
+        self.x.zero_()
         it, res = C.c_int32(), C.c_double()
-        tol = self.tol_rel * float(rm.abs().max())
-        rc = self.handle.call("ia_poisson_solve", ptr(self.x), ptr(self.z), ptr(self.L), tol, self.itmx,
-                              C.byref(it), C.byref(res))
+        rc = self.handle.call("ia_poisson_solve", ptr(self.x), ptr(self.z), ptr(self.L), self.tol,
+                              int(itmx or self.itmx), C.byref(it), C.byref(res))
         _lib.check(rc, "ia_poisson_solve", allow=(_lib.IA_OK, _lib.IA_WARN_NOT_CONVERGED))
-        e = self.x[1:-1, 1:-1, 1:-1].clone()
-        return e - e.mean(), it.value
+        return it.value
+
+    def residual(self) -> torch.Tensor:
+        """z - A x of the current iterate (interior, P³)."""
+        linf = C.c_double()
+        _lib.check(self.handle.call("ia_poisson_residual", ptr(self.r), ptr(self.x), ptr(self.z), ptr(self.L),
+                                    C.byref(linf)), "ia_poisson_residual")
+        return self.r[1:-1, 1:-1, 1:-1].clone()
 
 
 class PairGenerator:
     """(input, target) patch pairs from rising-bubble runs on an N³ box (periodic x/z, walls y).
 
     Run k uses ``bubble_layout(seed_base + k, N)``; after ``warm`` steps every step's pressure
-    system is cut into the (N/P)³ non-overlapping P³ patches.  Target = mean-free patch
-    correction e / (max|r| · scale), with ``scale`` fixed from the first snapshot."""
+    system is cut into the (N/P)³ non-overlapping P³ patches.  Each patch system is solved by
+    the multigrid-preconditioned CG (correction e*), and for every k in ``ks`` the iterate x_k
+    after k multigrid-preconditioned iterations gives one pair: input the residual
+    t = r - A x_k (as t / max|t|, with the face coefficients), target the remaining correction
+    e* - x_k (mean-free, as a fraction of its maximum) — the residuals the net meets behind the
+    V-cycle in the hybrid preconditioner.  Flexible CG and the hybrid's least-squares ω are
+    blind to the amplitude of each preconditioner output, so only its shape is learned."""
 
     def __init__(self, N=128, P=64, seed_base=1000, steps_per_run=6, warm=2, poisson="mixed", device="cuda",
-                 lrho=1e-3, lmu=1e-2):
+                 lrho=1e-3, lmu=1e-2, ks=(1, 2)):
         assert N % P == 0 and P % 4 == 0
         self.N, self.P, self.seed_base = N, P, seed_base
         self.steps_per_run, self.warm = steps_per_run, warm
         self.poisson, self.device = poisson, device
-        self.lrho, self.lmu = lrho, lmu
+        self.lrho, self.lmu, self.ks = lrho, lmu, tuple(ks)
         self.solver = PatchSolver(P, device=device)
-        self.scale = None
+        self.gains = []   # max|e| / max|t| per pair (information only)
         self.iters = []
 
     def _sim(self, k):
@@ -249,34 +267,41 @@ class PairGenerator:
                     yield interior(sim.flow.sigma).clone(), sim.flow.mu0[1:-1, 1:-1, 1:-1, :].clone()
             k += 1
 
+    def _pair(self, t, e):
+        P = self.P
+        s, em = float(t.abs().max()), float(e.abs().max())
+        if not (s > 0 and em > 0):
+            return None
+        self.gains.append(em / s)
+        tg = torch.zeros((P + 2,) * 3, dtype=torch.float64, device=t.device)
+        tg[1:-1, 1:-1, 1:-1] = t
+        x0 = net_input(tg, self.solver.L, self.lrho)
+        tgt = torch.zeros(x0.shape[:-1], dtype=torch.float32, device=t.device)
+        tgt[0, 1:-1, 1:-1, 1:-1] = _cl(e / em).float()
+        return x0, tgt
+
     def pairs(self):
         """Yields (x0 [1,P+2,P+2,P+2,4], target [1,P+2,P+2,P+2]) FP32 device tensors."""
-        P, n = self.P, self.N // self.P
+        P, n, sv = self.P, self.N // self.P, self.solver
         for z, L in self.snapshots():
             for ox in range(n):
                 for oy in range(n):
                     for oz in range(n):
                         sl = (slice(ox * P, ox * P + P), slice(oy * P, oy * P + P), slice(oz * P, oz * P + P))
-                        r, Lp = z[sl], L[sl]
-                        e, it = self.solver.solve(r, Lp)
-                        self.iters.append(it)
-                        rm = r - r.mean()
-                        s = float(rm.abs().max())
-                        if not (s > 0):
+                        if not (sv.set_system(z[sl], L[sl]) > 0):
                             continue
-                        if self.scale is None:
-                            self.scale = float(e.abs().max()) / s
-                        xg = torch.zeros((P + 2,) * 3, dtype=torch.float64, device=z.device)
-                        xg[1:-1, 1:-1, 1:-1] = rm
-                        Lg = torch.zeros((P + 2,) * 3 + (3,), dtype=torch.float64, device=z.device)
-                        Lg[1:-1, 1:-1, 1:-1, :] = Lp
-                        Lg[1, :, :, 0] = 0.0
-                        Lg[:, 1, :, 1] = 0.0
-                        Lg[:, :, 1, 2] = 0.0
-                        x0 = net_input(xg, Lg, self.lrho)
-                        tgt = torch.zeros(x0.shape[:-1], dtype=torch.float32, device=z.device)
-                        tgt[0, 1:-1, 1:-1, 1:-1] = _cl(e / (s * self.scale)).float()
-                        yield x0, tgt
+                        self.iters.append(sv.run())
+                        e_star = interior(sv.x).clone()
+                        for k in self.ks:
+                            if k == 0:
+                                t, e = interior(sv.z).clone(), e_star
+                            else:
+                                sv.run(k)
+                                t = sv.residual()
+                                e = e_star - interior(sv.x)
+                            pr = self._pair(t, e - e.mean())
+                            if pr is not None:
+                                yield pr
 
 
 def batches(pairs, B):
@@ -304,6 +329,55 @@ def train(net: Net, pairs, n_pairs: int, batch=4, lr=1e-3, lr_final=1e-4, log_ev
     return losses
 
 
+def eval_system(N=64, seed=999, steps=2, device="cuda"):
+    """A held-out pressure system: μ₀ and σ after ``steps`` steps of a bubbly N³ run."""
+    from .simulation import TwoPhaseSimulation, sim_step
+    G, D = 1e-3, 0.25 * N
+    sigma = G * D * D / 10.0
+    mu = (1e-3 * sigma ** 3 / G) ** 0.25
+    sim = TwoPhaseSimulation((N, N, N), (0.0, 0.0, 0.0), float(N), perdir=(0, 2), λρ=1e-3, λμ=1e-2, ν=mu, η=sigma,
+                             g=(0.0, -G, 0.0), InterfaceSDF=bubbles_sdf(bubble_layout(seed, N)), poisson="mixed",
+                             poisson_tol=1e-9, poisson_itmx=400, device=device)
+    for _ in range(steps):
+        sim_step(sim)
+    return sim.flow.mu0.clone(), sim.flow.sigma.clone()
+
+
+def evaluate(weights, L, z, tol=1e-8, preconds=("none", "net", "vcycle", "hybrid"), inner_max=30, reps=3):
+    """FCG iterations, solve time (median of ``reps``) and FP64 residual of the learned mode per
+    inner preconditioner, against the plain FP64 multigrid, on the system (L, z)."""
+    from .simulation import poisson_stats, set_learned
+    N = tuple(n - 2 for n in z.shape)
+    out = {}
+
+    def run(mode, precond=None):
+        h = Handle(make_config(N, perdir=(0, 2), poisson=mode, lrho=1e-3))
+        if mode == "learned":
+            set_learned(h, precond=precond, weights=weights,
+                        inner_max=(2000 if precond in ("none", "net") else inner_max))
+        times, it, res = [], C.c_int32(), C.c_double()
+        for _ in range(reps):
+            x = fzeros(z.shape)
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            rc = h.call("ia_poisson_solve", ptr(x), ptr(z), ptr(L), tol, 4000, C.byref(it), C.byref(res))
+            torch.cuda.synchronize()
+            times.append(time.perf_counter() - t0)
+            _lib.check(rc, "ia_poisson_solve", allow=(_lib.IA_OK, _lib.IA_WARN_NOT_CONVERGED))
+        r = dict(iters=it.value, resid=res.value, ms=1e3 * float(np.median(times)))
+        if mode == "learned":
+            st = poisson_stats(h)
+            r.update(fallbacks=st["fallbacks"] // reps, net_per_solve=st["net"] // reps,
+                     vcycles_per_solve=st["vcycles"] // reps)
+        return r
+
+    out["fp64_mg"] = run("fp64")
+    out["mixed_mg"] = run("mixed")
+    for p in preconds:
+        out[p] = run("learned", p)
+    return out
+
+
 def main(argv=None):
     ap = argparse.ArgumentParser(description="train the learned Poisson preconditioner")
     ap.add_argument("--pairs", type=int, default=20000)
@@ -314,6 +388,7 @@ def main(argv=None):
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--steps-per-run", type=int, default=6)
     ap.add_argument("--out", default=WEIGHTS)
+    ap.add_argument("--eval-N", type=int, default=64, help="held-out system size for the ablation (0 = skip)")
     a = ap.parse_args(argv)
     torch.cuda.set_device(0)
     net = Net()
@@ -322,11 +397,14 @@ def main(argv=None):
     t0 = time.time()
     losses = train(net, gen.pairs(), a.pairs, batch=a.batch, lr=a.lr)
     meta = dict(pairs=a.pairs, N=a.N, P=a.P, batch=a.batch, lr=a.lr, seed=a.seed, seed_base=gen.seed_base,
-                steps_per_run=gen.steps_per_run, target_scale=gen.scale, first_loss=losses[0],
+                steps_per_run=gen.steps_per_run, gain_median=float(np.median(gen.gains)), first_loss=losses[0],
                 final_loss=float(np.mean(losses[-20:])), seconds=time.time() - t0,
                 patch_mg_iters_mean=float(np.mean(gen.iters)) if gen.iters else None)
     save_params(a.out, net.get_params(), **meta)
     print(json.dumps(meta))
+    if a.eval_N:
+        L, z = eval_system(a.eval_N)
+        print(json.dumps({"eval_N": a.eval_N, **evaluate(a.out, L, z)}))
 
 
 if __name__ == "__main__":
