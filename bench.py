@@ -37,10 +37,10 @@ for _p in (ROOT, PKG):
 
 METRIC = "Mcell-steps/s"
 PTOL = 1e-8
-B_RBGS_PER_CELL_F32 = 20   # one FP32 red-black half-sweep: L (12) + x read/write (4) + b (2) + iD (2) per cell
+B_RBGS_PER_CELL_F32 = 18   # one FP32 red-black half-sweep: L (12) + x read/write (4) + b (2) per cell
 B_BULK_PER_CELL = 33       # vof_bulk: read f, u_d, u0_d (24) + c̄ (1); write ρuf_d (8)
 TK = {"vof_bulk": 0, "vof_cells": 1, "ustar": 2, "forcing": 3, "mg_vcycle": 4, "mg_transfer": 6, "krylov": 7,
-      "vof_faces": 9, "momflux": 10, "momupdate": 11, "update_project": 12, "mg_fine_rbgs": 13}
+      "vof_faces": 9, "momflux": 10, "momupdate": 11, "update_project": 12, "mg_fine_rbgs": 13, "nn_precond": 14}
 
 
 def parse():
@@ -265,7 +265,7 @@ def run_bubble(args, world, local_rank):
         b = B_RBGS_PER_CELL_F32 * cells
         ach = b / (fine["avg_launch_ms"] / 1e3) / 1e9
         roof = {"bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s", "frac": ach / peak, "traffic": None,
-                "kernel": "rbgs_k<float> (finest-level red-black Gauss-Seidel half-sweep, mixed V-cycle)",
+                "kernel": "rbgs_pair_k<float> (finest-level red-black Gauss-Seidel half-sweep, mixed V-cycle)",
                 "peak_kind": peak_kind, "bytes_per_launch": b, "avg_launch_ms": fine["avg_launch_ms"]}
     e2e = None
     if not args.no_e2e:
@@ -310,6 +310,26 @@ def run_bubble(args, world, local_rank):
         out["speedup_vs_fp64_mg"] = value / out["fp64_mg"]["value"]
         del ref
         torch.cuda.empty_cache()
+        from intfadv import learned
+        if os.path.exists(learned.WEIGHTS):
+            # learned preconditioner: the same step with the inner FCG preconditioned by V-cycle + net
+            lrn = make_bubble(N, "learned", dev)
+            for _ in range(max(1, args.warmup - 1)):
+                ia.sim_step(lrn)
+            k = max(2, min(args.steps, 5))
+            st0 = ia.poisson_stats(lrn.handle)
+            ms3, its3, res3, _ = timed_steps(lrn, k, barrier, False, local_rank)
+            st1 = ia.poisson_stats(lrn.handle)
+            kt3 = kernel_times(lrn, 2)
+            out["learned_hybrid"] = {
+                "value": world * cells * k / (ms3 / 1e3) / 1e6, "ms_per_step": ms3 / k,
+                "poisson_iters_per_step": statistics.mean(its3), "max_resid": max(res3),
+                "fallbacks": st1["fallbacks"] - st0["fallbacks"],
+                "net_ms_per_step": kt3["nn_precond"]["ms_per_step"],
+                "mg_vcycle_ms_per_step": kt3["mg_vcycle"]["ms_per_step"],
+                "weights": learned.load_params()[1]}
+            del lrn
+            torch.cuda.empty_cache()
     return out
 
 
@@ -414,6 +434,7 @@ def main():
                 "clocks": res["clocks"], "e2e": res["e2e"], "gpu_launches": res["launches"],
                 "roofline": res["roofline"], "cpu_baseline": cpu,
                 "fp64_mg": res.get("fp64_mg"), "speedup_vs_fp64_mg": res.get("speedup_vs_fp64_mg"),
+                "learned_hybrid": res.get("learned_hybrid"),
                 "poisson_iters_per_step": res["poisson_iters_per_step"], "max_poisson_resid": res["max_resid"],
                 "kernels_ms_per_step": {k: v["ms_per_step"] for k, v in res["kernels"].items()},
                 "vof_only": vof}

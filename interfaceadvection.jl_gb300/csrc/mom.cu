@@ -113,7 +113,7 @@ __device__ double limiter(int which, double u, double c, double d) {
             return c + s * dmin(s * (c - u), s * (d - c));
         }
         default:   // Koren
-            return median3((7.0 * c + d - 2.0 * u) * (1.0 / 6.0), c, median3(2.0 * c - u, c, d));
+            return median3(fma(-2.0, u, fma(7.0, c, d)) * (1.0 / 6.0), c, median3(fma(2.0, c, -u), c, d));
     }
 }
 
@@ -124,46 +124,65 @@ struct FluxCtx {
     const double* us;
     const double* rj;     // ρuf[:, j] before the 1/δt scaling
     const double* fold;
-    double dt, inv_dt;
+    double dt, inv_dt, half_inv_dt;
+    // pure-phase faces: m_old < m_out  <=>  |Ψ| > thr (thr = m_old/δt), l₂ = |Ψ|·kl (kl = δt/m_old)
+    double thr_l, thr_1, kl_l, kl_1;
 };
 
-// BC!'d ρuf[X, j] / δt (the reference scales by inv(δt) then applies BC!)
-__device__ __forceinline__ double rflux(const FluxCtx& F, int c[3]) {
+// ρuf[X, j] (raw, before 1/δt) or, on a BC! face, the boundary velocity (returns true)
+__device__ __forceinline__ bool rraw(const FluxCtx& F, int c[3], double& v) {
     const Grid& g = F.k.g;
-    if (vel_bc(g, F.j, c)) return F.k.uBC[F.j];
-    return F.rj[lin3(g, c)] * F.inv_dt;
+    if (vel_bc(g, F.j, c)) {
+        v = F.k.uBC[F.j];
+        return true;
+    }
+    v = F.rj[lin3(g, c)];
+    return false;
+}
+// Ψ = ϕ(i, CI(I,j), ρuf/δt) = (ρuf[a]/δt + ρuf[b]/δt)/2, one product when neither is a BC face
+__device__ __forceinline__ double face_psi(const FluxCtx& F, int ca[3], int cb[3]) {
+    double va, vb;
+    const bool ba = rraw(F, ca, va), bb = rraw(F, cb, vb);
+    if (!ba && !bb) return (va + vb) * F.half_inv_dt;
+    return ((ba ? va : va * F.inv_dt) + (bb ? vb : vb * F.inv_dt)) / 2.0;
 }
 
-// 1 + (λρ - 1)... : λρ + (1-λρ) dρ[X, i], dρ = BCv!(f2face!(f_old)); the upper normal
-// face of a zero-gradient dimension is never written by the reference and keeps
-// the 1 it is initialised with (src/cVOF.jl:74).
-__device__ __forceinline__ double m_old(const FluxCtx& F, int i, int c[3], bool& is_lrho, bool& is_rho1) {
+// m_old = λρ + (1-λρ) dρ[X, i] with dρ = BCv!(f2face!(f_old)): kind 1 light, 2 dark (constants),
+// 0 mixed (value in m).  The upper normal face of a zero-gradient dimension is never written by
+// the reference and keeps the 1 it is initialised with (src/cVOF.jl:74).
+__device__ __forceinline__ int m_old_kind(const FluxCtx& F, int i, int c[3], double& m) {
     const Grid& g = F.k.g;
-    is_lrho = is_rho1 = false;
-    if (face_bc(g, i, c)) { is_rho1 = true; return F.k.rho1; }
+    if (face_bc(g, i, c)) return 2;
     const long long P = lin3(g, c);
     const double fa = F.fold[P], fb = F.fold[P - g.s[i]];
     const unsigned long long a = dbits(fa), b = dbits(fb);
-    if (a == b && a == 0ull) { is_lrho = true; return F.k.lrho; }
-    if (a == b && a == kOneBits) { is_rho1 = true; return F.k.rho1; }
-    return F.k.lrho + F.k.one_m * ((fa + fb) / 2.0);
+    if (a == b && a == 0ull) return 1;
+    if (a == b && a == kOneBits) return 2;
+    m = F.k.lrho + F.k.one_m * ((fa + fb) / 2.0);
+    return 0;
 }
 
-// ϕq (src/flow.jl:37-57) on the upwind triple (uu, cc, dd); cic = coords of the face
+// ϕq (src/flow.jl:37-57) on the upwind triple (uu, cc, dd); cic = coords of the face.
+// With v_a = 2v_I - v_d and l₁ = 1 - l₂ the reference's Ψ (v_b + v_d)/2 is Ψ (v_d + l₂ (v_I - v_d)).
 __device__ double phiq(const FluxCtx& F, int i, const int cic[3], double Psi, double uu, double cc, double dd) {
     int c[3] = {cic[0], cic[1], cic[2]};
     if (okey(Psi) > 0) c[F.j] -= 1;                       // IiCell = Ψ>0 ? Ii-δj : Ii
-    const double vI = cc;
     const double vd = limiter(F.lim, uu, cc, dd);
-    const double va = 2.0 * vI - vd;
-    const double mOut = dabs(Psi) * F.dt;
-    bool isl, isr;
-    const double mOld = m_old(F, i, c, isl, isr);
-    if (dlt(mOld, mOut)) return Psi * vI;
-    const double l2 = isl ? mOut * F.k.inv_lrho : (isr ? mOut * F.k.inv_rho1 : mOut / mOld);
-    const double l1 = 1.0 - l2;
-    const double vb = l2 * va + l1 * vd;
-    return Psi * (vb + vd) / 2.0;
+    const double aP = dabs(Psi);
+    double mOld = 0.0, l2;
+    const int kind = m_old_kind(F, i, c, mOld);
+    if (kind == 1) {
+        if (dlt(F.thr_l, aP)) return Psi * cc;
+        l2 = aP * F.kl_l;
+    } else if (kind == 2) {
+        if (dlt(F.thr_1, aP)) return Psi * cc;
+        l2 = aP * F.kl_1;
+    } else {
+        const double mOut = aP * F.dt;
+        if (dlt(mOld, mOut)) return Psi * cc;
+        l2 = mOut / mOld;
+    }
+    return Psi * fma(l2, cc - vd, vd);
 }
 
 __global__ void momflux_kern(FluxCtx F, double* __restrict__ Phi) {
@@ -185,7 +204,7 @@ __global__ void momflux_kern(FluxCtx F, double* __restrict__ Phi) {
     for (int i = 0; i < g.D; ++i) {
         int ca[3] = {c[0], c[1], c[2]}, cb[3] = {c[0], c[1], c[2]};
         cb[i] -= 1;
-        const double Psi = (rflux(F, ca) + rflux(F, cb)) / 2.0;      // ϕ(i, CI(I,j), ρuf)
+        const double Psi = face_psi(F, ca, cb);                         // ϕ(i, CI(I,j), ρuf)
         const double* u = F.us + i * g.N;
         const bool pos = okey(Psi) > 0;
         double uu, cc, dd;
@@ -206,15 +225,15 @@ __global__ void momflux_kern(FluxCtx F, double* __restrict__ Phi) {
     }
 }
 
-// ρ̄∂ⱼuⱼ at a (ghost-mapped) cell: getρ(I,c̄,λρ)(∂(d,I,u)+∂(d,I,u⁰))/2, BCf! ghosts
-__device__ __forceinline__ double dila(const MomConsts& k, int d, int c[3], const double* u1, const double* u2,
-                                       const int8_t* cbar) {
+// ρ̄∂ⱼuⱼ/2 at a (ghost-mapped) cell: getρ(I,c̄,λρ)(∂(d,I,u)+∂(d,I,u⁰))/4, BCf! ghosts; the
+// reference's ϕ(i, I, ρ̄∂ⱼuⱼ) = (d(I) + d(I-δi))/2 is then the plain sum of two of these.
+__device__ __forceinline__ double dila_q(const MomConsts& k, double rq_l, double rq_1, int d, int c[3],
+                                         const double* u1, const double* u2, const int8_t* cbar) {
     const Grid& g = k.g;
     for (int e = 0; e < g.D; ++e) c[e] = bc_src(g, e, c[e]);
     const long long P = lin3(g, c);
     const long long sd = g.s[d];
-    const double rho = cbar[P] ? k.rho1 : k.lrho;
-    return rho * ((u1[P + sd] - u1[P]) + (u2[P + sd] - u2[P])) / 2.0;
+    return (cbar[P] ? rq_1 : rq_l) * ((u1[P + sd] - u1[P]) + (u2[P + sd] - u2[P]));
 }
 
 __global__ void momupdate_kern(MomConsts k, int j, const double* __restrict__ Phi, const double* __restrict__ uOld,
@@ -225,14 +244,15 @@ __global__ void momupdate_kern(MomConsts k, int j, const double* __restrict__ Ph
     const int c0[3] = {x, y, z};
     if (!is_interior(g, c0)) return;
     const long long I = lin(g, x, y, z);
+    const double rq_l = 0.25 * k.lrho, rq_1 = 0.25 * k.rho1;
     int cc[3] = {x, y, z};
-    const double dI = dila(k, j, cc, u1d, u2d, cbar);
+    const double dI = dila_q(k, rq_l, rq_1, j, cc, u1d, u2d, cbar);
     for (int i = 0; i < g.D; ++i) {
         int cm[3] = {x, y, z};
         cm[i] -= 1;
-        const double dm = dila(k, j, cm, u1d, u2d, cbar);
-        const double r = (Phi[I + i * g.N] - Phi[I + g.s[j] + i * g.N]) + uOld[I + i * g.N] * ((dI + dm) / 2.0);
-        rhou[I + i * g.N] = rhou[I + i * g.N] + dt * r;
+        const double dm = dila_q(k, rq_l, rq_1, j, cm, u1d, u2d, cbar);
+        const double r = fma(uOld[I + i * g.N], dI + dm, Phi[I + i * g.N] - Phi[I + g.s[j] + i * g.N]);
+        rhou[I + i * g.N] = fma(dt, r, rhou[I + i * g.N]);
     }
 }
 
@@ -559,6 +579,11 @@ cudaError_t k_momflux(const MomConsts& k, int j, int limiter, const double* usta
     F.fold = fold;
     F.dt = dt;
     F.inv_dt = 1.0 / dt;
+    F.half_inv_dt = 0.5 / dt;
+    F.thr_l = k.lrho / dt;
+    F.thr_1 = k.rho1 / dt;
+    F.kl_l = dt * k.inv_lrho;
+    F.kl_1 = dt * k.inv_rho1;
     { momflux_kern<<<grd(k.g), blk(), 0, s>>>(F, Phi); ia::note_launch(); }
     return cudaGetLastError();
 }

@@ -106,12 +106,34 @@ __global__ void restrict_L_k(Grid gc, Grid gf, const T* __restrict__ Lf, T* __re
     }
 }
 
+// Red-black Gauss-Seidel half-sweep, one thread per cell of the colour: thread tx takes the pair of
+// interior cells (1 + 2tx, 2 + 2tx) of its row and updates the one of this colour, so no
+// lane idles; the diagonal comes from the face coefficients the update reads anyway
+// (same value and zero-diagonal rule as set_diag_k).
 template <class T>
-__global__ void rbgs_k(Grid g, const T* __restrict__ L, const T* __restrict__ iD, const T* __restrict__ b,
-                       T* __restrict__ xv, int color) {
-    INTERIOR_XYZ
-    if (((x + y + z) & 1) != color) return;
-    xv[I] = (b[I] - offdiag(g, L, xv, I, c)) * iD[I];
+__global__ void rbgs_pair_k(Grid g, const T* __restrict__ L, const T* __restrict__ b, T* __restrict__ xv,
+                            int color) {
+    const int y = 1 + blockIdx.y * blockDim.y + threadIdx.y;
+    const int z = g.D == 3 ? 1 + blockIdx.z : 0;
+    if (y > g.n[1] - 2) return;
+    int x = 1 + 2 * (blockIdx.x * blockDim.x + threadIdx.x);
+    if (((x + y + z) & 1) != color) ++x;
+    if (x > g.n[0] - 2) return;
+    const int c[3] = {x, y, z};
+    const long long I = lin(g, x, y, z);
+    T off = T(0), dd = T(0);
+    for (int i = 0; i < g.D; ++i) {
+        const T lo = L[I + i * g.N], hi = L[I + g.s[i] + i * g.N];
+        off += lo * xv[I + lo_off(g, i, c[i])] + hi * xv[I + hi_off(g, i, c[i])];
+        dd -= lo + hi;
+    }
+    const T eps = sizeof(T) == 8 ? T(2.220446049250313e-16) : T(1.1920929e-7);
+    const T iD = (dd * dd < T(2) * eps) ? T(0) : T(1) / dd;
+    xv[I] = (b[I] - off) * iD;
+}
+inline dim3 pair_grid(const Grid& g) {
+    const int pairs = (g.n[0] - 2 + 1) / 2;
+    return dim3((pairs + 31) / 32, (g.n[1] - 2 + 7) / 8, g.D == 3 ? g.n[2] - 2 : 1);
 }
 
 // first red sweep from x = 0: neighbours are zero
@@ -201,97 +223,127 @@ __global__ void to_f64_k(long long n, const float* __restrict__ a, double* __res
         b[q] = double(a[q]);
 }
 
-// ------------------------------------------------------------------ FP64 Krylov kernels
+// ------------------------------------------------------------------ Krylov kernels
+// Row loops: a block takes whole x-rows of interior cells (rows dealt round-robin over a
+// grid of at most KBLOCKS blocks), so the reductions end in one warp-shuffle block sum per
+// block and the cross-block sums read only gridDim.x partials.
+constexpr int KTHREADS = 256;
+constexpr int KBLOCKS = 1216;   // 8 blocks on each of 152 SMs
+
+#define ROWS_BEGIN(g)                                                                      \
+    {                                                                                      \
+        const int nxi_ = (g).n[0] - 2, nyi_ = (g).n[1] - 2;                                \
+        const long long nrows_ = (long long)nyi_ * ((g).D == 3 ? (g).n[2] - 2 : 1);        \
+        for (long long rw_ = blockIdx.x; rw_ < nrows_; rw_ += gridDim.x) {                 \
+            const int y = 1 + int(rw_ % nyi_), z = (g).D == 3 ? 1 + int(rw_ / nyi_) : 0;   \
+            for (int x = 1 + threadIdx.x; x <= nxi_; x += blockDim.x) {                    \
+                const int c[3] = {x, y, z};                                                \
+                const long long I = lin(g, x, y, z);
+#define ROWS_END \
+    }            \
+    }            \
+    }
+
+inline int kblocks(const Grid& g) {
+    const long long rows = (long long)(g.n[1] - 2) * (g.D == 3 ? g.n[2] - 2 : 1);
+    return int(rows < KBLOCKS ? rows : KBLOCKS);
+}
+
+__device__ __forceinline__ double warp_sum(double v) {
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    return v;
+}
+__device__ __forceinline__ unsigned long long warp_max(unsigned long long v) {
+    for (int o = 16; o > 0; o >>= 1) {
+        const unsigned long long w = __shfl_down_sync(0xffffffffu, v, o);
+        v = w > v ? w : v;
+    }
+    return v;
+}
+// block sums of a and b, valid in thread 0 (fixed order: deterministic)
+__device__ __forceinline__ void block_sum2(double& a, double& b) {
+    __shared__ double sa[32], sb[32];
+    a = warp_sum(a);
+    b = warp_sum(b);
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    if (lane == 0) {
+        sa[w] = a;
+        sb[w] = b;
+    }
+    __syncthreads();
+    if (w == 0) {
+        const int nw = blockDim.x >> 5;
+        a = warp_sum(lane < nw ? sa[lane] : 0.0);
+        b = warp_sum(lane < nw ? sb[lane] : 0.0);
+    }
+}
+__device__ __forceinline__ unsigned long long block_max(unsigned long long m) {
+    __shared__ unsigned long long sm[32];
+    m = warp_max(m);
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    if (lane == 0) sm[w] = m;
+    __syncthreads();
+    if (w == 0) m = warp_max(lane < (int)(blockDim.x >> 5) ? sm[lane] : 0ull);
+    return m;
+}
+
 __device__ __forceinline__ unsigned long long abs_bits(double v) {
     return (unsigned long long)__double_as_longlong(v) & 0x7FFFFFFFFFFFFFFFull;
 }
 
-// r = z - A x over interior cells, L∞(r) into *linf
-__global__ void true_resid_k(Grid g, const double* __restrict__ L, const double* __restrict__ zz,
-                             const double* __restrict__ xv, double* __restrict__ r, unsigned long long* linf) {
-    __shared__ unsigned long long sm[256];
-    const int t = threadIdx.y * blockDim.x + threadIdx.x;
+// diagonal D_I = -Σ_i (L[I,i] + L[I+δi,i]) of the FP64 operator
+__device__ __forceinline__ double diag_of(const Grid& g, const double* L, long long I) {
+    double dd = 0.0;
+    for (int i = 0; i < g.D; ++i) dd -= L[I + i * g.N] + L[I + g.s[i] + i * g.N];
+    return dd;
+}
+__global__ void set_diag64_k(Grid g, const double* __restrict__ L, double* __restrict__ diag) {
+    ROWS_BEGIN(g)
+    diag[I] = diag_of(g, L, I);
+    ROWS_END
+}
+
+// r = z - A x over interior cells, L∞(r) into *linf; diag precomputed (or NULL: from L)
+__global__ void true_resid_k(Grid g, const double* __restrict__ L, const double* __restrict__ diag,
+                             const double* __restrict__ zz, const double* __restrict__ xv, double* __restrict__ r,
+                             unsigned long long* linf) {
     unsigned long long m = 0ull;
-    {
-        const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y;
-        const int z = blockIdx.z;
-        const int c[3] = {x, y, z};
-        if (x < g.n[0] && y < g.n[1] && is_interior(g, c)) {
-            const long long I = lin(g, x, y, z);
-            double dd = 0.0;
-            for (int i = 0; i < g.D; ++i) dd -= L[I + i * g.N] + L[I + g.s[i] + i * g.N];
-            const double v = zz[I] - (offdiag(g, L, xv, I, c) + dd * xv[I]);
-            r[I] = v;
-            m = abs_bits(v);
-        }
-    }
-    sm[t] = m;
-    __syncthreads();
-    for (int w = 128; w > 0; w >>= 1) {
-        if (t < w) sm[t] = sm[t] > sm[t + w] ? sm[t] : sm[t + w];
-        __syncthreads();
-    }
-    if (t == 0) atomicMax(linf, sm[0]);
+    ROWS_BEGIN(g)
+    const double dd = diag ? diag[I] : diag_of(g, L, I);
+    const double v = zz[I] - (offdiag(g, L, xv, I, c) + dd * xv[I]);
+    r[I] = v;
+    const unsigned long long b = abs_bits(v);
+    m = b > m ? b : m;
+    ROWS_END
+    m = block_max(m);
+    if (threadIdx.x == 0) atomicMax(linf, m);
 }
 
 // q = A p and partial dot p·q
-__global__ void matvec_dot_k(Grid g, const double* __restrict__ L, const double* __restrict__ pv,
-                             double* __restrict__ q, double* __restrict__ partial) {
-    __shared__ double sm[256];
-    const int t = threadIdx.y * blockDim.x + threadIdx.x;
-    double acc = 0.0;
-    {
-        const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y;
-        const int z = blockIdx.z;
-        const int c[3] = {x, y, z};
-        if (x < g.n[0] && y < g.n[1] && is_interior(g, c)) {
-            const long long I = lin(g, x, y, z);
-            double dd = 0.0;
-            for (int i = 0; i < g.D; ++i) dd -= L[I + i * g.N] + L[I + g.s[i] + i * g.N];
-            const double v = offdiag(g, L, pv, I, c) + dd * pv[I];
-            q[I] = v;
-            acc = pv[I] * v;
-        }
-    }
-    sm[t] = acc;
-    __syncthreads();
-    for (int w = 128; w > 0; w >>= 1) {
-        if (t < w) sm[t] += sm[t + w];
-        __syncthreads();
-    }
-    if (t == 0) partial[(blockIdx.z * gridDim.y + blockIdx.y) * gridDim.x + blockIdx.x] = sm[0];
+__global__ void matvec_dot_k(Grid g, const double* __restrict__ L, const double* __restrict__ diag,
+                             const double* __restrict__ pv, double* __restrict__ q, double* __restrict__ partial) {
+    double acc = 0.0, unused = 0.0;
+    ROWS_BEGIN(g)
+    const double v = offdiag(g, L, pv, I, c) + diag[I] * pv[I];
+    q[I] = v;
+    acc += pv[I] * v;
+    ROWS_END
+    block_sum2(acc, unused);
+    if (threadIdx.x == 0) partial[blockIdx.x] = acc;
 }
 
 // partial dots s·q and s·r
 __global__ void dot2_k(Grid g, const double* __restrict__ sv, const double* __restrict__ q,
-                       const double* __restrict__ r, double* __restrict__ partial, long long nblocks) {
-    __shared__ double s1[256], s2[256];
-    const int t = threadIdx.y * blockDim.x + threadIdx.x;
+                       const double* __restrict__ r, double* __restrict__ partial) {
     double a1 = 0.0, a2 = 0.0;
-    {
-        const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y;
-        const int z = blockIdx.z;
-        const int c[3] = {x, y, z};
-        if (x < g.n[0] && y < g.n[1] && is_interior(g, c)) {
-            const long long I = lin(g, x, y, z);
-            a1 = sv[I] * q[I];
-            a2 = sv[I] * r[I];
-        }
-    }
-    s1[t] = a1;
-    s2[t] = a2;
-    __syncthreads();
-    for (int w = 128; w > 0; w >>= 1) {
-        if (t < w) {
-            s1[t] += s1[t + w];
-            s2[t] += s2[t + w];
-        }
-        __syncthreads();
-    }
-    if (t == 0) {
-        const long long b = (blockIdx.z * gridDim.y + blockIdx.y) * gridDim.x + blockIdx.x;
-        partial[b] = s1[0];
-        partial[nblocks + b] = s2[0];
+    ROWS_BEGIN(g)
+    a1 += sv[I] * q[I];
+    a2 += sv[I] * r[I];
+    ROWS_END
+    block_sum2(a1, a2);
+    if (threadIdx.x == 0) {
+        partial[blockIdx.x] = a1;
+        partial[gridDim.x + blockIdx.x] = a2;
     }
 }
 
@@ -313,188 +365,116 @@ __global__ void finalize_k(const double* __restrict__ partial, long long n, int 
 }
 
 __global__ void xpby_k(Grid g, const double* __restrict__ sv, double beta, double* __restrict__ pv) {
-    INTERIOR_XYZ
-    pv[I] = sv[I] + beta * pv[I];
+    ROWS_BEGIN(g)
+    pv[I] = (beta == 0.0) ? sv[I] : sv[I] + beta * pv[I];
+    ROWS_END
 }
 
 // x += α p ; r -= α q ; L∞(r)
 __global__ void update_k(Grid g, double alpha, const double* __restrict__ pv, const double* __restrict__ q,
                          double* __restrict__ xv, double* __restrict__ r, unsigned long long* linf) {
-    __shared__ unsigned long long sm[256];
-    const int t = threadIdx.y * blockDim.x + threadIdx.x;
     unsigned long long m = 0ull;
-    {
-        const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y;
-        const int z = blockIdx.z;
-        const int c[3] = {x, y, z};
-        if (x < g.n[0] && y < g.n[1] && is_interior(g, c)) {
-            const long long I = lin(g, x, y, z);
-            xv[I] += alpha * pv[I];
-            const double v = r[I] - alpha * q[I];
-            r[I] = v;
-            m = abs_bits(v);
-        }
-    }
-    sm[t] = m;
-    __syncthreads();
-    for (int w = 128; w > 0; w >>= 1) {
-        if (t < w) sm[t] = sm[t] > sm[t + w] ? sm[t] : sm[t + w];
-        __syncthreads();
-    }
-    if (t == 0) atomicMax(linf, sm[0]);
+    ROWS_BEGIN(g)
+    xv[I] += alpha * pv[I];
+    const double v = r[I] - alpha * q[I];
+    r[I] = v;
+    const unsigned long long b = abs_bits(v);
+    m = b > m ? b : m;
+    ROWS_END
+    m = block_max(m);
+    if (threadIdx.x == 0) atomicMax(linf, m);
 }
 
-// ---- FP32 inner Krylov kernels (mixed mode): products and block sums in FP32,
-// one FP64 partial per block, reduced across blocks in FP64.
-__device__ __forceinline__ float block_sum_f(float v, float* sm, int t) {
-    sm[t] = v;
-    __syncthreads();
-    for (int w = 128; w > 0; w >>= 1) {
-        if (t < w) sm[t] += sm[t + w];
-        __syncthreads();
-    }
-    return sm[0];
-}
-
+// ---- FP32 inner Krylov kernels (mixed / learned): FP32 products, per-thread sums in FP32
+// over its cells, FP64 block and cross-block sums.
 __global__ void matvec32_dot_k(Grid g, const float* __restrict__ L, const float* __restrict__ pv,
                                float* __restrict__ q, double* __restrict__ partial) {
-    __shared__ float sm[256];
-    const int t = threadIdx.y * blockDim.x + threadIdx.x;
     float acc = 0.f;
-    {
-        const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y;
-        const int z = blockIdx.z;
-        const int c[3] = {x, y, z};
-        if (x < g.n[0] && y < g.n[1] && is_interior(g, c)) {
-            const long long I = lin(g, x, y, z);
-            float dd = 0.f;
-            for (int i = 0; i < g.D; ++i) dd -= L[I + i * g.N] + L[I + g.s[i] + i * g.N];
-            const float v = offdiag(g, L, pv, I, c) + dd * pv[I];
-            q[I] = v;
-            acc = pv[I] * v;
-        }
-    }
-    const float b = block_sum_f(acc, sm, t);
-    if (t == 0) partial[(blockIdx.z * gridDim.y + blockIdx.y) * gridDim.x + blockIdx.x] = double(b);
+    ROWS_BEGIN(g)
+    float dd = 0.f;
+    for (int i = 0; i < g.D; ++i) dd -= L[I + i * g.N] + L[I + g.s[i] + i * g.N];
+    const float v = offdiag(g, L, pv, I, c) + dd * pv[I];
+    q[I] = v;
+    acc += pv[I] * v;
+    ROWS_END
+    double a = acc, unused = 0.0;
+    block_sum2(a, unused);
+    if (threadIdx.x == 0) partial[blockIdx.x] = a;
 }
 
 __global__ void dot2_32_k(Grid g, const float* __restrict__ sv, const float* __restrict__ q,
-                          const float* __restrict__ r, double* __restrict__ partial, long long nblocks) {
-    __shared__ float s1[256], s2[256];
-    const int t = threadIdx.y * blockDim.x + threadIdx.x;
+                          const float* __restrict__ r, double* __restrict__ partial) {
     float a1 = 0.f, a2 = 0.f;
-    {
-        const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y;
-        const int z = blockIdx.z;
-        const int c[3] = {x, y, z};
-        if (x < g.n[0] && y < g.n[1] && is_interior(g, c)) {
-            const long long I = lin(g, x, y, z);
-            a1 = sv[I] * q[I];
-            a2 = sv[I] * r[I];
-        }
-    }
-    s1[t] = a1;
-    s2[t] = a2;
-    __syncthreads();
-    for (int w = 128; w > 0; w >>= 1) {
-        if (t < w) {
-            s1[t] += s1[t + w];
-            s2[t] += s2[t + w];
-        }
-        __syncthreads();
-    }
-    if (t == 0) {
-        const long long b = (blockIdx.z * gridDim.y + blockIdx.y) * gridDim.x + blockIdx.x;
-        partial[b] = double(s1[0]);
-        partial[nblocks + b] = double(s2[0]);
+    ROWS_BEGIN(g)
+    a1 += sv[I] * q[I];
+    a2 += sv[I] * r[I];
+    ROWS_END
+    double b1 = a1, b2 = a2;
+    block_sum2(b1, b2);
+    if (threadIdx.x == 0) {
+        partial[blockIdx.x] = b1;
+        partial[gridDim.x + blockIdx.x] = b2;
     }
 }
 
 // p = s + β p; β = 0 restarts from s without reading the old direction (which a rejected
 // preconditioner output may have left non-finite)
 __global__ void xpby32_k(Grid g, const float* __restrict__ sv, float beta, float* __restrict__ pv) {
-    INTERIOR_XYZ
+    ROWS_BEGIN(g)
     pv[I] = (beta == 0.f) ? sv[I] : sv[I] + beta * pv[I];
+    ROWS_END
 }
 
 // e += α p ; r -= α q ; L∞(r) as float bits
 __global__ void update32_k(Grid g, float alpha, const float* __restrict__ pv, const float* __restrict__ q,
                            float* __restrict__ e, float* __restrict__ r, unsigned int* linf) {
-    __shared__ unsigned int sm[256];
-    const int t = threadIdx.y * blockDim.x + threadIdx.x;
-    unsigned int m = 0u;
-    {
-        const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y;
-        const int z = blockIdx.z;
-        const int c[3] = {x, y, z};
-        if (x < g.n[0] && y < g.n[1] && is_interior(g, c)) {
-            const long long I = lin(g, x, y, z);
-            e[I] += alpha * pv[I];
-            const float v = r[I] - alpha * q[I];
-            r[I] = v;
-            m = __float_as_uint(v) & 0x7FFFFFFFu;
-        }
-    }
-    sm[t] = m;
-    __syncthreads();
-    for (int w = 128; w > 0; w >>= 1) {
-        if (t < w) sm[t] = sm[t] > sm[t + w] ? sm[t] : sm[t + w];
-        __syncthreads();
-    }
-    if (t == 0) atomicMax(linf, sm[0]);
+    unsigned long long m = 0ull;
+    ROWS_BEGIN(g)
+    e[I] += alpha * pv[I];
+    const float v = r[I] - alpha * q[I];
+    r[I] = v;
+    const unsigned long long b = __float_as_uint(v) & 0x7FFFFFFFu;
+    m = b > m ? b : m;
+    ROWS_END
+    m = block_max(m);
+    if (threadIdx.x == 0) atomicMax(linf, (unsigned int)m);
 }
 
 // ---- learned hybrid preconditioner: t = A v with partial dots r·t and t·t
 __global__ void matvec32_dot2_k(Grid g, const float* __restrict__ L, const float* __restrict__ v,
-                                float* __restrict__ t, const float* __restrict__ r, double* __restrict__ partial,
-                                long long nblocks) {
-    __shared__ float s1[256], s2[256];
-    const int tt = threadIdx.y * blockDim.x + threadIdx.x;
+                                float* __restrict__ t, const float* __restrict__ r, double* __restrict__ partial) {
     float a1 = 0.f, a2 = 0.f;
-    {
-        const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y;
-        const int z = blockIdx.z;
-        const int c[3] = {x, y, z};
-        if (x < g.n[0] && y < g.n[1] && is_interior(g, c)) {
-            const long long I = lin(g, x, y, z);
-            float dd = 0.f;
-            for (int i = 0; i < g.D; ++i) dd -= L[I + i * g.N] + L[I + g.s[i] + i * g.N];
-            const float w = offdiag(g, L, v, I, c) + dd * v[I];
-            t[I] = w;
-            a1 = r[I] * w;
-            a2 = w * w;
-        }
-    }
-    s1[tt] = a1;
-    s2[tt] = a2;
-    __syncthreads();
-    for (int w = 128; w > 0; w >>= 1) {
-        if (tt < w) {
-            s1[tt] += s1[tt + w];
-            s2[tt] += s2[tt + w];
-        }
-        __syncthreads();
-    }
-    if (tt == 0) {
-        const long long b = (blockIdx.z * gridDim.y + blockIdx.y) * gridDim.x + blockIdx.x;
-        partial[b] = double(s1[0]);
-        partial[nblocks + b] = double(s2[0]);
+    ROWS_BEGIN(g)
+    float dd = 0.f;
+    for (int i = 0; i < g.D; ++i) dd -= L[I + i * g.N] + L[I + g.s[i] + i * g.N];
+    const float w = offdiag(g, L, v, I, c) + dd * v[I];
+    t[I] = w;
+    a1 += r[I] * w;
+    a2 += w * w;
+    ROWS_END
+    double b1 = a1, b2 = a2;
+    block_sum2(b1, b2);
+    if (threadIdx.x == 0) {
+        partial[blockIdx.x] = b1;
+        partial[gridDim.x + blockIdx.x] = b2;
     }
 }
 
 // s += ω n with ω = (t·An)/(An·An) from the device dots (0 unless An·An is positive and finite)
 __global__ void add_scaled_k(Grid g, const double* __restrict__ dots, const float* __restrict__ nv,
                              float* __restrict__ sv) {
-    INTERIOR_XYZ
     const double tn = dots[0], n2 = dots[1];
     const float w = float((n2 > 0.0 && n2 < 1e300 && tn == tn) ? tn / n2 : 0.0);
+    ROWS_BEGIN(g)
     sv[I] += w * nv[I];
+    ROWS_END
 }
 
 // x += e (FP64 += FP32), interior cells
 __global__ void add_correction_k(Grid g, const float* __restrict__ e, double* __restrict__ xv) {
-    INTERIOR_XYZ
+    ROWS_BEGIN(g)
     xv[I] += double(e[I]);
+    ROWS_END
 }
 
 // periodic ghosts of a scalar (WaterLily perBC!)
@@ -539,7 +519,7 @@ static cudaError_t vcycle(ia_handle* h, PoissonMG* mg, int l, cudaStream_t st, i
     }
     auto half = [&](int color) {
         const int tk = (l == 0) ? timing_begin(h, TK_MG_FINE) : -1;
-        { rbgs_k<T><<<grd(L.g), blk(), 0, st>>>(L.g, Lc, iD, b, x, color); ia::note_launch(); }
+        { rbgs_pair_k<T><<<pair_grid(L.g), blk(), 0, st>>>(L.g, Lc, b, x, color); ia::note_launch(); }
         timing_end(h, tk);
     };
     { rb_first_k<T><<<grd(L.g), blk(), 0, st>>>(L.g, iD, b, x); ia::note_launch(); }
@@ -619,9 +599,10 @@ int mg_create(ia_handle* h) {
     e = e ? e : cudaMalloc(&mg->s, 8 * N);
     e = e ? e : cudaMalloc(&mg->p, 8 * N);
     e = e ? e : cudaMalloc(&mg->q, 8 * N);
-    const dim3 gb = grd(g0);
-    mg->nblocks = (long long)gb.x * gb.y * gb.z;
-    e = e ? e : cudaMalloc(&mg->partial, 8 * 2 * (size_t)mg->nblocks);
+    mg->kb = kblocks(g0);
+    e = e ? e : cudaMalloc(&mg->partial, 8 * 2 * (size_t)KBLOCKS);
+    e = e ? e : cudaMalloc(&mg->diag64, 8 * N);
+    if (!e) cudaMemset(mg->diag64, 0, 8 * N);
     if (mixed) {
         e = e ? e : cudaMalloc(&mg->p32, 4 * N);
         e = e ? e : cudaMalloc(&mg->q32, 4 * N);
@@ -666,7 +647,7 @@ void mg_destroy(ia_handle* h) {
     cudaFree(mg->r); cudaFree(mg->s); cudaFree(mg->p); cudaFree(mg->q);
     cudaFree(mg->p32); cudaFree(mg->q32); cudaFree(mg->e32);
     cudaFree(mg->rl32); cudaFree(mg->nl32); cudaFree(mg->t32);
-    cudaFree(mg->partial); cudaFree(mg->dsc);
+    cudaFree(mg->partial); cudaFree(mg->dsc); cudaFree(mg->diag64);
     if (mg->hsc) cudaFreeHost(mg->hsc);
     delete mg;
     h->mg = nullptr;
@@ -679,6 +660,7 @@ static cudaError_t mg_setup(ia_handle* h, const double* L0) {
     const bool mixed = h->cfg.poisson_mode != IA_POISSON_FP64;
     MGLevel& F = mg->lev[0];
     const long long nv = F.g.N * F.g.D;
+    { set_diag64_k<<<mg->kb, KTHREADS, 0, st>>>(F.g, L0, mg->diag64); ia::note_launch(); }
     if (!mixed) {
         cudaMemcpyAsync(F.L, L0, 8 * nv, cudaMemcpyDeviceToDevice, st);
         { set_diag_k<double><<<grd(F.g), blk(), 0, st>>>(F.g, F.L, F.iD); ia::note_launch(); }
@@ -803,16 +785,16 @@ static int poisson_solve_mixed(ia_handle* h, double* xv, const double* zz, const
         timing_end(h, tk);
         if (!net(mg->t32)) return false;
         tk = timing_begin(h, TK_KRYLOV);
-        { matvec32_dot2_k<<<gb, blk(), 0, st>>>(g, F.L32, mg->nl32, F.r32, mg->t32, mg->partial, mg->nblocks); ia::note_launch(); }
-        { finalize_k<<<1, 1024, 0, st>>>(mg->partial, mg->nblocks, 2, hdots); ia::note_launch(); }
-        { add_scaled_k<<<gb, blk(), 0, st>>>(g, hdots, mg->nl32, F.x32); ia::note_launch(); }
+        { matvec32_dot2_k<<<mg->kb, KTHREADS, 0, st>>>(g, F.L32, mg->nl32, F.r32, mg->t32, mg->partial); ia::note_launch(); }
+        { finalize_k<<<1, 1024, 0, st>>>(mg->partial, mg->kb, 2, hdots); ia::note_launch(); }
+        { add_scaled_k<<<mg->kb, KTHREADS, 0, st>>>(g, hdots, mg->nl32, F.x32); ia::note_launch(); }
         timing_end(h, tk);
         return cudaGetLastError() == cudaSuccess;
     };
     int total = 0;
     cudaMemsetAsync(dlinf, 0, 8, st);
     int tk = timing_begin(h, TK_KRYLOV);
-    { true_resid_k<<<gb, blk(), 0, st>>>(g, L, zz, xv, mg->r, dlinf); ia::note_launch(); }
+    { true_resid_k<<<mg->kb, KTHREADS, 0, st>>>(g, L, mg->diag64, zz, xv, mg->r, dlinf); ia::note_launch(); }
     timing_end(h, tk);
     double res = read_linf(h, dlinf);
     while (!(res <= tol) && total < itmx) {
@@ -826,17 +808,17 @@ static int poisson_solve_mixed(ia_handle* h, double* xv, const double* zz, const
             float* sv = nullptr;
             if (!precond(sv)) return IA_ERR_CUDA;
             tk = timing_begin(h, TK_KRYLOV);
-            { dot2_32_k<<<gb, blk(), 0, st>>>(g, sv, mg->q32, rr, mg->partial, mg->nblocks); ia::note_launch(); }
-            { finalize_k<<<1, 1024, 0, st>>>(mg->partial, mg->nblocks, 2, dots); ia::note_launch(); }
+            { dot2_32_k<<<mg->kb, KTHREADS, 0, st>>>(g, sv, mg->q32, rr, mg->partial); ia::note_launch(); }
+            { finalize_k<<<1, 1024, 0, st>>>(mg->partial, mg->kb, 2, dots); ia::note_launch(); }
             timing_end(h, tk);
             cudaMemcpyAsync(mg->hsc + 2, dots, 16, cudaMemcpyDeviceToHost, st);
             if (cudaStreamSynchronize(st) != cudaSuccess) return IA_ERR_CUDA;
             const double sq = mg->hsc[2], sr = mg->hsc[3];
             const double beta = (it == 0) ? 0.0 : (-alpha_prev * sq) / rho_prev;
             tk = timing_begin(h, TK_KRYLOV);
-            { xpby32_k<<<gb, blk(), 0, st>>>(g, sv, float(beta), mg->p32); ia::note_launch(); }
-            { matvec32_dot_k<<<gb, blk(), 0, st>>>(g, F.L32, mg->p32, mg->q32, mg->partial); ia::note_launch(); }
-            { finalize_k<<<1, 1024, 0, st>>>(mg->partial, mg->nblocks, 1, dots); ia::note_launch(); }
+            { xpby32_k<<<mg->kb, KTHREADS, 0, st>>>(g, sv, float(beta), mg->p32); ia::note_launch(); }
+            { matvec32_dot_k<<<mg->kb, KTHREADS, 0, st>>>(g, F.L32, mg->p32, mg->q32, mg->partial); ia::note_launch(); }
+            { finalize_k<<<1, 1024, 0, st>>>(mg->partial, mg->kb, 1, dots); ia::note_launch(); }
             timing_end(h, tk);
             cudaMemcpyAsync(mg->hsc + 2, dots, 8, cudaMemcpyDeviceToHost, st);
             if (cudaStreamSynchronize(st) != cudaSuccess) return IA_ERR_CUDA;
@@ -847,7 +829,7 @@ static int poisson_solve_mixed(ia_handle* h, double* xv, const double* zz, const
             const double alpha = sr / pq;
             cudaMemsetAsync(dlinf32, 0, 4, st);
             tk = timing_begin(h, TK_KRYLOV);
-            { update32_k<<<gb, blk(), 0, st>>>(g, float(alpha), mg->p32, mg->q32, mg->e32, rr, dlinf32); ia::note_launch(); }
+            { update32_k<<<mg->kb, KTHREADS, 0, st>>>(g, float(alpha), mg->p32, mg->q32, mg->e32, rr, dlinf32); ia::note_launch(); }
             timing_end(h, tk);
             const double rin = read_linf32(h, dlinf32);
             rho_prev = sr;
@@ -855,9 +837,9 @@ static int poisson_solve_mixed(ia_handle* h, double* xv, const double* zz, const
             if (rin <= target) break;
         }
         tk = timing_begin(h, TK_KRYLOV);
-        { add_correction_k<<<gb, blk(), 0, st>>>(g, mg->e32, xv); ia::note_launch(); }
+        { add_correction_k<<<mg->kb, KTHREADS, 0, st>>>(g, mg->e32, xv); ia::note_launch(); }
         cudaMemsetAsync(dlinf, 0, 8, st);
-        { true_resid_k<<<gb, blk(), 0, st>>>(g, L, zz, xv, mg->r, dlinf); ia::note_launch(); }
+        { true_resid_k<<<mg->kb, KTHREADS, 0, st>>>(g, L, mg->diag64, zz, xv, mg->r, dlinf); ia::note_launch(); }
         timing_end(h, tk);
         const double res_old = res;
         res = read_linf(h, dlinf);
@@ -881,7 +863,7 @@ int poisson_residual(ia_handle* h, double* r, const double* x, const double* z, 
     cudaStream_t st = h->stream;
     unsigned long long* d = reinterpret_cast<unsigned long long*>(h->dscalar + 60);
     cudaMemsetAsync(d, 0, 8, st);
-    { true_resid_k<<<grd(h->g), blk(), 0, st>>>(h->g, L, z, x, r, d); ia::note_launch(); }
+    { true_resid_k<<<kblocks(h->g), KTHREADS, 0, st>>>(h->g, L, nullptr, z, x, r, d); ia::note_launch(); }
     unsigned long long v = 0;
     cudaMemcpyAsync(&v, d, 8, cudaMemcpyDeviceToHost, st);
     if (cudaStreamSynchronize(st) != cudaSuccess) return IA_ERR_CUDA;
@@ -906,7 +888,7 @@ int poisson_solve(ia_handle* h, double* xv, const double* zz, const double* L, d
     double* dots = mg->dsc;
     cudaMemsetAsync(dlinf, 0, 8, st);
     int tk = timing_begin(h, TK_KRYLOV);
-    { true_resid_k<<<gb, blk(), 0, st>>>(g, L, zz, xv, mg->r, dlinf); ia::note_launch(); }
+    { true_resid_k<<<mg->kb, KTHREADS, 0, st>>>(g, L, mg->diag64, zz, xv, mg->r, dlinf); ia::note_launch(); }
     timing_end(h, tk);
     double res = read_linf(h, dlinf);
     int it = 0;
@@ -914,8 +896,8 @@ int poisson_solve(ia_handle* h, double* xv, const double* zz, const double* L, d
     while (!(res <= tol) && it < itmx) {
         if (mg_precondition(h) != cudaSuccess) return IA_ERR_CUDA;
         tk = timing_begin(h, TK_KRYLOV);
-        { dot2_k<<<gb, blk(), 0, st>>>(g, mg->s, mg->q, mg->r, mg->partial, mg->nblocks); ia::note_launch(); }
-        { finalize_k<<<1, 1024, 0, st>>>(mg->partial, mg->nblocks, 2, dots); ia::note_launch(); }
+        { dot2_k<<<mg->kb, KTHREADS, 0, st>>>(g, mg->s, mg->q, mg->r, mg->partial); ia::note_launch(); }
+        { finalize_k<<<1, 1024, 0, st>>>(mg->partial, mg->kb, 2, dots); ia::note_launch(); }
         timing_end(h, tk);
         cudaMemcpyAsync(mg->hsc + 2, dots, 16, cudaMemcpyDeviceToHost, st);
         if (cudaStreamSynchronize(st) != cudaSuccess) return IA_ERR_CUDA;
@@ -924,9 +906,9 @@ int poisson_solve(ia_handle* h, double* xv, const double* zz, const double* L, d
         const double beta = (it == 0) ? 0.0 : (-alpha_prev * sq) / rho_prev;
         const double rho = sr;
         tk = timing_begin(h, TK_KRYLOV);
-        { xpby_k<<<gb, blk(), 0, st>>>(g, mg->s, beta, mg->p); ia::note_launch(); }
-        { matvec_dot_k<<<gb, blk(), 0, st>>>(g, L, mg->p, mg->q, mg->partial); ia::note_launch(); }
-        { finalize_k<<<1, 1024, 0, st>>>(mg->partial, mg->nblocks, 1, dots); ia::note_launch(); }
+        { xpby_k<<<mg->kb, KTHREADS, 0, st>>>(g, mg->s, beta, mg->p); ia::note_launch(); }
+        { matvec_dot_k<<<mg->kb, KTHREADS, 0, st>>>(g, L, mg->diag64, mg->p, mg->q, mg->partial); ia::note_launch(); }
+        { finalize_k<<<1, 1024, 0, st>>>(mg->partial, mg->kb, 1, dots); ia::note_launch(); }
         timing_end(h, tk);
         cudaMemcpyAsync(mg->hsc + 2, dots, 8, cudaMemcpyDeviceToHost, st);
         if (cudaStreamSynchronize(st) != cudaSuccess) return IA_ERR_CUDA;
@@ -935,7 +917,7 @@ int poisson_solve(ia_handle* h, double* xv, const double* zz, const double* L, d
         const double alpha = rho / pq;
         cudaMemsetAsync(dlinf, 0, 8, st);
         tk = timing_begin(h, TK_KRYLOV);
-        { update_k<<<gb, blk(), 0, st>>>(g, alpha, mg->p, mg->q, xv, mg->r, dlinf); ia::note_launch(); }
+        { update_k<<<mg->kb, KTHREADS, 0, st>>>(g, alpha, mg->p, mg->q, xv, mg->r, dlinf); ia::note_launch(); }
         timing_end(h, tk);
         res = read_linf(h, dlinf);
         rho_prev = rho;

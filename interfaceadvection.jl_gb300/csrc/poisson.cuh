@@ -46,7 +46,8 @@ struct PoissonMG {
     int inner_max = 30;                                               // inner FCG iterations per correction
     double inner_rtol = 1e-4;                                         // inner relative residual target
     double* partial = nullptr;                                        // per-block dot partials
-    long long nblocks = 0;
+    int kb = 0;                                                       // blocks of the Krylov row loops
+    double* diag64 = nullptr;                                         // FP64 operator diagonal
     double* dsc = nullptr;                                            // device scalars
     double* hsc = nullptr;                                            // pinned host scalars
     int nu1 = 2, nu2 = 2, nuc = 16;
