@@ -33,7 +33,7 @@ extern "C" {
 #define IA_ERR_INVALID            4   /* bad argument / unbound field                  */
 #define IA_ERR_CUDA               5   /* CUDA runtime error                            */
 #define IA_ERR_NO_DEVICE          6
-#define IA_ERR_TOO_LARGE          7
+#define IA_ERR_TOO_LARGE          7   /* grid of 2^31 cells or more (ghosts included)  */
 #define IA_WARN_FILL            100   /* over/under-fill past tol (printed, not fatal)  */
 #define IA_WARN_NOT_CONVERGED   101   /* Poisson stopped at itmx                        */
 

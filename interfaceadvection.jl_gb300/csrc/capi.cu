@@ -245,7 +245,8 @@ int ia_create(const ia_config* cfg, ia_handle** out) {
     if (!h) return IA_ERR_INVALID;
     h->cfg = *cfg;
     h->g = make_grid(cfg->D, cfg->perdir, cfg->N);
-    if (h->g.N >= (1ll << 32)) { delete h; return IA_ERR_TOO_LARGE; }
+    // cell offsets within a field are 32-bit signed in the stencil kernels
+    if (h->g.N >= (1ll << 31)) { delete h; return IA_ERR_TOO_LARGE; }
     cudaGetDevice(&h->device);
     int sms = 0;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, h->device);

@@ -86,7 +86,7 @@ __global__ void bcvel_kern(MomConsts k, double* a, double A0, double A1, double 
 __device__ __forceinline__ double median3(double a, double b, double c) { return dmax(dmin(a, b), dmin(dmax(a, b), c)); }
 __device__ __forceinline__ double sgn(double v) { return okey(v) > 0 ? 1.0 : (okey(v) < 0 ? -1.0 : 0.0); }
 
-__device__ double limiter(int which, double u, double c, double d) {
+__device__ __forceinline__ double limiter(int which, double u, double c, double d) {
     switch (which) {
         case IA_LIMITER_UPWIND: return c;
         case IA_LIMITER_MINMOD: return median3((3.0 * c - u) * 0.5, c, (c + d) * 0.5);
@@ -162,12 +162,22 @@ __device__ __forceinline__ int m_old_kind(const FluxCtx& F, int i, int c[3], dou
     return 0;
 }
 
+// l₂ = m_out / m_old on a face whose old fractions fa, fb are not both 0 or both 1, or -1 when
+// m_old < m_out (the flux is then Ψ v_I).  Out of line so that bulk faces do not issue it.
+__device__ __noinline__ double l2_mixed(const FluxCtx& F, double fa, double fb, double aP) {
+    const double mOld = F.k.lrho + F.k.one_m * ((fa + fb) / 2.0);
+    const double mOut = aP * F.dt;
+    if (dlt(mOld, mOut)) return -1.0;
+    return mOut / mOld;
+}
+
 // ϕq (src/flow.jl:37-57) on the upwind triple (uu, cc, dd); cic = coords of the face.
 // With v_a = 2v_I - v_d and l₁ = 1 - l₂ the reference's Ψ (v_b + v_d)/2 is Ψ (v_d + l₂ (v_I - v_d)).
+template <int LIM>
 __device__ double phiq(const FluxCtx& F, int i, const int cic[3], double Psi, double uu, double cc, double dd) {
     int c[3] = {cic[0], cic[1], cic[2]};
     if (okey(Psi) > 0) c[F.j] -= 1;                       // IiCell = Ψ>0 ? Ii-δj : Ii
-    const double vd = limiter(F.lim, uu, cc, dd);
+    const double vd = limiter(LIM, uu, cc, dd);
     const double aP = dabs(Psi);
     double mOld = 0.0, l2;
     const int kind = m_old_kind(F, i, c, mOld);
@@ -185,16 +195,54 @@ __device__ double phiq(const FluxCtx& F, int i, const int cic[3], double Psi, do
     return Psi * fma(l2, cc - vd, vd);
 }
 
+// ϕq for a face far from every boundary: donor old fractions at P and P - δi
+template <int LIM>
+__device__ __forceinline__ double phiq_inner(const FluxCtx& F, double Psi, double uu, double cc, double dd,
+                                             double fa, double fb) {
+    const double vd = limiter(LIM, uu, cc, dd);
+    const double aP = dabs(Psi);
+    const unsigned long long a = dbits(fa), b = dbits(fb);
+    double l2;
+    if (a == b && (a == 0ull || a == kOneBits)) {
+        const bool light = a == 0ull;
+        if (dlt(light ? F.thr_l : F.thr_1, aP)) return Psi * cc;
+        l2 = aP * (light ? F.kl_l : F.kl_1);
+    } else {
+        l2 = l2_mixed(F, fa, fb, aP);
+        if (l2 < 0.0) return Psi * cc;
+    }
+    return Psi * fma(l2, cc - vd, vd);
+}
+
+template <int LIM>
 __global__ void momflux_kern(FluxCtx F, double* __restrict__ Phi) {
     const Grid& g = F.k.g;
     CELL_XYZ
     const int j = F.j;
     int c[3] = {x, y, z};
+    bool inner = true;
     for (int e = 0; e < g.D; ++e) {
         const int hi = (e == j) ? g.n[e] - 1 : g.n[e] - 2;
         if (c[e] < 1 || c[e] > hi) return;
+        if (c[e] < 3 || c[e] > g.n[e] - 3) inner = false;
     }
     const long long K = lin(g, x, y, z);
+    if (inner) {
+        // no ghost, wall, periodic-image or boundary-face rule reaches this face's stencil
+        const long long sj = g.s[j];
+        for (int i = 0; i < g.D; ++i) {
+            const long long si = g.s[i];
+            const double Psi = (F.rj[K] + F.rj[K - si]) * F.half_inv_dt;
+            const double* u = F.us + i * g.N;
+            const bool pos = okey(Psi) > 0;
+            const double uu = pos ? u[K - 2 * sj] : u[K + sj];
+            const double cc = pos ? u[K - sj] : u[K];
+            const double dd = pos ? u[K] : u[K - sj];
+            const long long P = pos ? K - sj : K;
+            Phi[K + i * g.N] = phiq_inner<LIM>(F, Psi, uu, cc, dd, F.fold[P], F.fold[P - si]);
+        }
+        return;
+    }
     const bool per = g.isper(j);
     if (per && c[j] == g.n[j] - 1) c[j] = 1;              // periodic upper face = lower face
     const long long Kk = lin3(g, c);
@@ -221,7 +269,7 @@ __global__ void momflux_kern(FluxCtx F, double* __restrict__ Phi) {
             if (pos) { uu = u[Kk - 2 * sj]; cc = u[Kk - sj]; dd = u[Kk]; }
             else { uu = u[Kk + sj]; cc = u[Kk]; dd = u[Kk - sj]; }
         }
-        Phi[K + i * g.N] = phiq(F, i, c, Psi, uu, cc, dd);
+        Phi[K + i * g.N] = phiq<LIM>(F, i, c, Psi, uu, cc, dd);
     }
 }
 
@@ -276,8 +324,10 @@ __device__ __forceinline__ double fface(const ViscCtx& V, int d, int c[3]) {
     return (fa + fb) / 2.0;
 }
 
-// getμ(i,j,I,fFace,λμ,μ,λρ) (src/VOFutil.jl:186-191)
-__device__ double get_mu(const ViscCtx& V, int i, int j, const int cI[3]) {
+// getμ(i,j,I,fFace,λμ,μ,λρ) (src/VOFutil.jl:186-191).  Kept out of line: inlined, its
+// mixed-face arithmetic is if-converted and the predicated-off FP64 instructions still take
+// FP64 issue slots in every bulk cell.
+__device__ __noinline__ double get_mu(const ViscCtx& V, int i, int j, const int cI[3]) {
     int a[3] = {cI[0], cI[1], cI[2]}, b[3] = {cI[0], cI[1], cI[2]}, c[3] = {cI[0], cI[1], cI[2]},
         d[3] = {cI[0], cI[1], cI[2]};
     a[j] -= 1;
@@ -294,6 +344,22 @@ __device__ double get_mu(const ViscCtx& V, int i, int j, const int cI[3]) {
     return V.mu * dmin(V.lmu + (1.0 - V.lmu) * s, fac * (V.k.lrho + V.k.one_m * fr));
 }
 
+// getμ for an edge/face whose cells all lie at least two cells inside the grid (no ghost or
+// boundary-face rule applies): the fractions of the 3 (i == j) or 4 cells decide a pure phase
+// with integer compares; anything else goes to the general helper.
+__device__ __forceinline__ double get_mu_inner(const ViscCtx& V, int i, int j, const int c[3], long long K) {
+    const Grid& g = V.k.g;
+    const double* f = V.f;
+    const unsigned long long a = dbits(f[K]), b = dbits(f[K - g.s[i]]);
+    const unsigned long long e = dbits(i == j ? f[K - 2 * g.s[i]] : f[K - g.s[j]]);
+    const unsigned long long d = i == j ? a : dbits(f[K - g.s[i] - g.s[j]]);
+    if (a == b && a == e && a == d) {
+        if (a == 0ull) return V.mu_face0;
+        if (a == kOneBits) return V.mu_face1;
+    }
+    return get_mu(V, i, j, c);
+}
+
 __device__ __forceinline__ int pair_index(int D, int i, int j) {
     if (i == j) return i;
     const int a = i < j ? i : j, b = i < j ? j : i;
@@ -305,6 +371,9 @@ __global__ void viscflux_kern(ViscCtx V, double* __restrict__ Phi6) {
     CELL_XYZ
     const int c[3] = {x, y, z};
     const long long K = lin(g, x, y, z);
+    bool inner = true;
+    for (int e = 0; e < g.D; ++e)
+        if (c[e] < 3 || c[e] > g.n[e] - 3) inner = false;
     for (int i = 0; i < g.D; ++i)
         for (int j = i; j < g.D; ++j) {
             bool ok = true;
@@ -313,7 +382,7 @@ __global__ void viscflux_kern(ViscCtx V, double* __restrict__ Phi6) {
                 if (c[e] < 1 || c[e] > hi) ok = false;
             }
             if (!ok) continue;
-            const double mu = get_mu(V, i, j, c);
+            const double mu = inner ? get_mu_inner(V, i, j, c, K) : get_mu(V, i, j, c);
             const double sji = V.u[K + i * g.N] - V.u[K - g.s[j] + i * g.N];
             const double sij = V.u[K + j * g.N] - V.u[K - g.s[i] + j * g.N];
             Phi6[pair_index(g.D, i, j) * g.N + K] = -(mu * (sji + sij));
@@ -584,7 +653,16 @@ cudaError_t k_momflux(const MomConsts& k, int j, int limiter, const double* usta
     F.thr_1 = k.rho1 / dt;
     F.kl_l = dt * k.inv_lrho;
     F.kl_1 = dt * k.inv_rho1;
-    { momflux_kern<<<grd(k.g), blk(), 0, s>>>(F, Phi); ia::note_launch(); }
+    switch (limiter) {
+        case IA_LIMITER_UPWIND: { momflux_kern<IA_LIMITER_UPWIND><<<grd(k.g), blk(), 0, s>>>(F, Phi); ia::note_launch(); } break;
+        case IA_LIMITER_MINMOD: { momflux_kern<IA_LIMITER_MINMOD><<<grd(k.g), blk(), 0, s>>>(F, Phi); ia::note_launch(); } break;
+        case IA_LIMITER_VANALBADA1: { momflux_kern<IA_LIMITER_VANALBADA1><<<grd(k.g), blk(), 0, s>>>(F, Phi); ia::note_launch(); } break;
+        case IA_LIMITER_SWEBY: { momflux_kern<IA_LIMITER_SWEBY><<<grd(k.g), blk(), 0, s>>>(F, Phi); ia::note_launch(); } break;
+        case IA_LIMITER_SUPERBEE: { momflux_kern<IA_LIMITER_SUPERBEE><<<grd(k.g), blk(), 0, s>>>(F, Phi); ia::note_launch(); } break;
+        case IA_LIMITER_TVDCEN: { momflux_kern<IA_LIMITER_TVDCEN><<<grd(k.g), blk(), 0, s>>>(F, Phi); ia::note_launch(); } break;
+        case IA_LIMITER_TVDDOWN: { momflux_kern<IA_LIMITER_TVDDOWN><<<grd(k.g), blk(), 0, s>>>(F, Phi); ia::note_launch(); } break;
+        default: { momflux_kern<IA_LIMITER_KOREN><<<grd(k.g), blk(), 0, s>>>(F, Phi); ia::note_launch(); } break;
+    }
     return cudaGetLastError();
 }
 cudaError_t k_momupdate(const MomConsts& k, int j, const double* Phi, const double* uOld, const double* u1,

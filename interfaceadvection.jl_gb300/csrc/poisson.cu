@@ -57,6 +57,69 @@ __device__ __forceinline__ T offdiag(const Grid& g, const T* L, const T* x, long
     return a;
 }
 
+// ---- dimension-specialised stencil with 32-bit cell offsets (a grid holds < 2^31 cells)
+struct Nb {
+    int xl, xh, yl, yh, zl, zh;   // offsets of the six neighbours; periodic ends wrap
+};
+template <int D>
+__device__ __forceinline__ Nb nb_of(const Grid& g, int x, int y, int z) {
+    Nb o;
+    const int s1 = int(g.s[1]), s2 = int(g.s[2]);
+    o.xl = (g.isper(0) && x == 1) ? g.n[0] - 3 : -1;
+    o.xh = (g.isper(0) && x == g.n[0] - 2) ? 3 - g.n[0] : 1;
+    o.yl = (g.isper(1) && y == 1) ? (g.n[1] - 3) * s1 : -s1;
+    o.yh = (g.isper(1) && y == g.n[1] - 2) ? (3 - g.n[1]) * s1 : s1;
+    o.zl = o.zh = 0;
+    if (D == 3) {
+        o.zl = (g.isper(2) && z == 1) ? (g.n[2] - 3) * s2 : -s2;
+        o.zh = (g.isper(2) && z == g.n[2] - 2) ? (3 - g.n[2]) * s2 : s2;
+    }
+    return o;
+}
+// Σ_i L[I,i] v[I-δi] + L[I+δi,i] v[I+δi]  (same order as offdiag)
+template <int D, class T>
+__device__ __forceinline__ T off7(const Grid& g, const T* __restrict__ L, const T* v, int I, const Nb& o) {
+    const int s1 = int(g.s[1]), s2 = int(g.s[2]);
+    const T* L1 = L + g.N;
+    T a = L[I] * v[I + o.xl] + L[I + 1] * v[I + o.xh];
+    a += L1[I] * v[I + o.yl] + L1[I + s1] * v[I + o.yh];
+    if (D == 3) {
+        const T* L2 = L1 + g.N;
+        a += L2[I] * v[I + o.zl] + L2[I + s2] * v[I + o.zh];
+    }
+    return a;
+}
+// D_I = -Σ_i (L[I,i] + L[I+δi,i])
+template <int D, class T>
+__device__ __forceinline__ T diag7(const Grid& g, const T* __restrict__ L, int I) {
+    const int s1 = int(g.s[1]), s2 = int(g.s[2]);
+    const T* L1 = L + g.N;
+    T dd = T(0);
+    dd -= L[I] + L[I + 1];
+    dd -= L1[I] + L1[I + s1];
+    if (D == 3) {
+        const T* L2 = L1 + g.N;
+        dd -= L2[I] + L2[I + s2];
+    }
+    return dd;
+}
+// interior-cell launch: x, y from the 2D block, z from blockIdx.z (3D) or 0 (2D)
+#define CELL_INTERIOR(g)                                                  \
+    const int x = 1 + blockIdx.x * blockDim.x + threadIdx.x;              \
+    const int y = 1 + blockIdx.y * blockDim.y + threadIdx.y;              \
+    const int z = D == 3 ? 1 + int(blockIdx.z) : 0;                       \
+    if (x > (g).n[0] - 2 || y > (g).n[1] - 2) return;                     \
+    const int I = x + y * int((g).s[1]) + z * int((g).s[2]);
+inline dim3 cell_grid(const Grid& g) {
+    return dim3((g.n[0] - 2 + 31) / 32, (g.n[1] - 2 + 7) / 8, g.D == 3 ? g.n[2] - 2 : 1);
+}
+// launch K<D> for the grid's dimension
+#define LAUNCH_D(gg, K, grid, block, ...)                                             \
+    do {                                                                              \
+        if ((gg).D == 3) { K<3><<<grid, block, 0, st>>>(__VA_ARGS__); ia::note_launch(); } \
+        else { K<2><<<grid, block, 0, st>>>(__VA_ARGS__); ia::note_launch(); }             \
+    } while (0)
+
 #define INTERIOR_XYZ                                                                                     \
     const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y;     \
     const int z = blockIdx.z;                                                                            \
@@ -110,23 +173,19 @@ __global__ void restrict_L_k(Grid gc, Grid gf, const T* __restrict__ Lf, T* __re
 // interior cells (1 + 2tx, 2 + 2tx) of its row and updates the one of this colour, so no
 // lane idles; the diagonal comes from the face coefficients the update reads anyway
 // (same value and zero-diagonal rule as set_diag_k).
-template <class T>
+template <class T, int D>
 __global__ void rbgs_pair_k(Grid g, const T* __restrict__ L, const T* __restrict__ b, T* __restrict__ xv,
                             int color) {
     const int y = 1 + blockIdx.y * blockDim.y + threadIdx.y;
-    const int z = g.D == 3 ? 1 + blockIdx.z : 0;
+    const int z = D == 3 ? 1 + int(blockIdx.z) : 0;
     if (y > g.n[1] - 2) return;
     int x = 1 + 2 * (blockIdx.x * blockDim.x + threadIdx.x);
     if (((x + y + z) & 1) != color) ++x;
     if (x > g.n[0] - 2) return;
-    const int c[3] = {x, y, z};
-    const long long I = lin(g, x, y, z);
-    T off = T(0), dd = T(0);
-    for (int i = 0; i < g.D; ++i) {
-        const T lo = L[I + i * g.N], hi = L[I + g.s[i] + i * g.N];
-        off += lo * xv[I + lo_off(g, i, c[i])] + hi * xv[I + hi_off(g, i, c[i])];
-        dd -= lo + hi;
-    }
+    const int I = x + y * int(g.s[1]) + z * int(g.s[2]);
+    const Nb o = nb_of<D>(g, x, y, z);
+    const T off = off7<D>(g, L, xv, I, o);
+    const T dd = diag7<D>(g, L, I);
     const T eps = sizeof(T) == 8 ? T(2.220446049250313e-16) : T(1.1920929e-7);
     const T iD = (dd * dd < T(2) * eps) ? T(0) : T(1) / dd;
     xv[I] = (b[I] - off) * iD;
@@ -143,13 +202,12 @@ __global__ void rb_first_k(Grid g, const T* __restrict__ iD, const T* __restrict
     xv[I] = (((x + y + z) & 1) == 0) ? b[I] * iD[I] : T(0);
 }
 
-template <class T>
+template <class T, int D>
 __global__ void residual_k(Grid g, const T* __restrict__ L, const T* __restrict__ b, const T* __restrict__ xv,
                            T* __restrict__ r) {
-    INTERIOR_XYZ
-    T dd = T(0);
-    for (int i = 0; i < g.D; ++i) dd -= L[I + i * g.N] + L[I + g.s[i] + i * g.N];
-    r[I] = b[I] - (offdiag(g, L, xv, I, c) + dd * xv[I]);
+    CELL_INTERIOR(g)
+    const Nb o = nb_of<D>(g, x, y, z);
+    r[I] = b[I] - (off7<D>(g, L, xv, I, o) + diag7<D>(g, L, I) * xv[I]);
 }
 
 template <class T>
@@ -244,6 +302,18 @@ constexpr int KBLOCKS = 1216;   // 8 blocks on each of 152 SMs
     }            \
     }
 
+// the same with a 32-bit cell index and the dimension fixed at compile time
+#define ROWS_BEGIN_D(g)                                                                    \
+    {                                                                                      \
+        const int nxi_ = (g).n[0] - 2, nyi_ = (g).n[1] - 2;                                \
+        const int s1_ = int((g).s[1]), s2_ = int((g).s[2]);                                \
+        const long long nrows_ = (long long)nyi_ * (D == 3 ? (g).n[2] - 2 : 1);            \
+        for (long long rw_ = blockIdx.x; rw_ < nrows_; rw_ += gridDim.x) {                 \
+            const int y = 1 + int(rw_ % nyi_), z = D == 3 ? 1 + int(rw_ / nyi_) : 0;       \
+            const int row_ = y * s1_ + z * s2_;                                            \
+            for (int x = 1 + threadIdx.x; x <= nxi_; x += blockDim.x) {                    \
+                const int I = row_ + x;
+
 inline int kblocks(const Grid& g) {
     const long long rows = (long long)(g.n[1] - 2) * (g.D == 3 ? g.n[2] - 2 : 1);
     return int(rows < KBLOCKS ? rows : KBLOCKS);
@@ -304,13 +374,15 @@ __global__ void set_diag64_k(Grid g, const double* __restrict__ L, double* __res
 }
 
 // r = z - A x over interior cells, L∞(r) into *linf; diag precomputed (or NULL: from L)
+template <int D>
 __global__ void true_resid_k(Grid g, const double* __restrict__ L, const double* __restrict__ diag,
                              const double* __restrict__ zz, const double* __restrict__ xv, double* __restrict__ r,
                              unsigned long long* linf) {
     unsigned long long m = 0ull;
-    ROWS_BEGIN(g)
-    const double dd = diag ? diag[I] : diag_of(g, L, I);
-    const double v = zz[I] - (offdiag(g, L, xv, I, c) + dd * xv[I]);
+    ROWS_BEGIN_D(g)
+    const Nb o = nb_of<D>(g, x, y, z);
+    const double dd = diag ? diag[I] : diag7<D>(g, L, I);
+    const double v = zz[I] - (off7<D>(g, L, xv, I, o) + dd * xv[I]);
     r[I] = v;
     const unsigned long long b = abs_bits(v);
     m = b > m ? b : m;
@@ -320,11 +392,13 @@ __global__ void true_resid_k(Grid g, const double* __restrict__ L, const double*
 }
 
 // q = A p and partial dot p·q
+template <int D>
 __global__ void matvec_dot_k(Grid g, const double* __restrict__ L, const double* __restrict__ diag,
                              const double* __restrict__ pv, double* __restrict__ q, double* __restrict__ partial) {
     double acc = 0.0, unused = 0.0;
-    ROWS_BEGIN(g)
-    const double v = offdiag(g, L, pv, I, c) + diag[I] * pv[I];
+    ROWS_BEGIN_D(g)
+    const Nb o = nb_of<D>(g, x, y, z);
+    const double v = off7<D>(g, L, pv, I, o) + diag[I] * pv[I];
     q[I] = v;
     acc += pv[I] * v;
     ROWS_END
@@ -387,13 +461,13 @@ __global__ void update_k(Grid g, double alpha, const double* __restrict__ pv, co
 
 // ---- FP32 inner Krylov kernels (mixed / learned): FP32 products, per-thread sums in FP32
 // over its cells, FP64 block and cross-block sums.
+template <int D>
 __global__ void matvec32_dot_k(Grid g, const float* __restrict__ L, const float* __restrict__ pv,
                                float* __restrict__ q, double* __restrict__ partial) {
     float acc = 0.f;
-    ROWS_BEGIN(g)
-    float dd = 0.f;
-    for (int i = 0; i < g.D; ++i) dd -= L[I + i * g.N] + L[I + g.s[i] + i * g.N];
-    const float v = offdiag(g, L, pv, I, c) + dd * pv[I];
+    ROWS_BEGIN_D(g)
+    const Nb o = nb_of<D>(g, x, y, z);
+    const float v = off7<D>(g, L, pv, I, o) + diag7<D>(g, L, I) * pv[I];
     q[I] = v;
     acc += pv[I] * v;
     ROWS_END
@@ -441,13 +515,13 @@ __global__ void update32_k(Grid g, float alpha, const float* __restrict__ pv, co
 }
 
 // ---- learned hybrid preconditioner: t = A v with partial dots r·t and t·t
+template <int D>
 __global__ void matvec32_dot2_k(Grid g, const float* __restrict__ L, const float* __restrict__ v,
                                 float* __restrict__ t, const float* __restrict__ r, double* __restrict__ partial) {
     float a1 = 0.f, a2 = 0.f;
-    ROWS_BEGIN(g)
-    float dd = 0.f;
-    for (int i = 0; i < g.D; ++i) dd -= L[I + i * g.N] + L[I + g.s[i] + i * g.N];
-    const float w = offdiag(g, L, v, I, c) + dd * v[I];
+    ROWS_BEGIN_D(g)
+    const Nb o = nb_of<D>(g, x, y, z);
+    const float w = off7<D>(g, L, v, I, o) + diag7<D>(g, L, I) * v[I];
     t[I] = w;
     a1 += r[I] * w;
     a2 += w * w;
@@ -519,7 +593,8 @@ static cudaError_t vcycle(ia_handle* h, PoissonMG* mg, int l, cudaStream_t st, i
     }
     auto half = [&](int color) {
         const int tk = (l == 0) ? timing_begin(h, TK_MG_FINE) : -1;
-        { rbgs_pair_k<T><<<pair_grid(L.g), blk(), 0, st>>>(L.g, Lc, b, x, color); ia::note_launch(); }
+        if (L.g.D == 3) { rbgs_pair_k<T, 3><<<pair_grid(L.g), blk(), 0, st>>>(L.g, Lc, b, x, color); ia::note_launch(); }
+        else { rbgs_pair_k<T, 2><<<pair_grid(L.g), blk(), 0, st>>>(L.g, Lc, b, x, color); ia::note_launch(); }
         timing_end(h, tk);
     };
     { rb_first_k<T><<<grd(L.g), blk(), 0, st>>>(L.g, iD, b, x); ia::note_launch(); }
@@ -528,7 +603,8 @@ static cudaError_t vcycle(ia_handle* h, PoissonMG* mg, int l, cudaStream_t st, i
         half(0);
         half(1);
     }
-    { residual_k<T><<<grd(L.g), blk(), 0, st>>>(L.g, Lc, b, x, r); ia::note_launch(); }
+    if (L.g.D == 3) { residual_k<T, 3><<<cell_grid(L.g), blk(), 0, st>>>(L.g, Lc, b, x, r); ia::note_launch(); }
+    else { residual_k<T, 2><<<cell_grid(L.g), blk(), 0, st>>>(L.g, Lc, b, x, r); ia::note_launch(); }
     auto& C = mg->lev[l + 1];
     { restrict_k<T><<<grd(C.g), blk(), 0, st>>>(C.g, L.g, r, C.template b_<T>()); ia::note_launch(); }
     cudaError_t e = vcycle<T>(h, mg, l + 1, st, nu1, nu2, nuc);
@@ -781,11 +857,12 @@ static int poisson_solve_mixed(ia_handle* h, double* xv, const double* zz, const
         // hybrid: the net corrects what the V-cycle left, s += ω net(t) with t = r - A s and
         // ω minimising |t - ω A net(t)|
         int tk = timing_begin(h, TK_KRYLOV);
-        { residual_k<float><<<gb, blk(), 0, st>>>(g, F.L32, rr, F.x32, mg->t32); ia::note_launch(); }
+        if (g.D == 3) { residual_k<float, 3><<<cell_grid(g), blk(), 0, st>>>(g, F.L32, rr, F.x32, mg->t32); ia::note_launch(); }
+        else { residual_k<float, 2><<<cell_grid(g), blk(), 0, st>>>(g, F.L32, rr, F.x32, mg->t32); ia::note_launch(); }
         timing_end(h, tk);
         if (!net(mg->t32)) return false;
         tk = timing_begin(h, TK_KRYLOV);
-        { matvec32_dot2_k<<<mg->kb, KTHREADS, 0, st>>>(g, F.L32, mg->nl32, F.r32, mg->t32, mg->partial); ia::note_launch(); }
+        LAUNCH_D(g, matvec32_dot2_k, mg->kb, KTHREADS, g, F.L32, mg->nl32, F.r32, mg->t32, mg->partial);
         { finalize_k<<<1, 1024, 0, st>>>(mg->partial, mg->kb, 2, hdots); ia::note_launch(); }
         { add_scaled_k<<<mg->kb, KTHREADS, 0, st>>>(g, hdots, mg->nl32, F.x32); ia::note_launch(); }
         timing_end(h, tk);
@@ -794,7 +871,7 @@ static int poisson_solve_mixed(ia_handle* h, double* xv, const double* zz, const
     int total = 0;
     cudaMemsetAsync(dlinf, 0, 8, st);
     int tk = timing_begin(h, TK_KRYLOV);
-    { true_resid_k<<<mg->kb, KTHREADS, 0, st>>>(g, L, mg->diag64, zz, xv, mg->r, dlinf); ia::note_launch(); }
+    LAUNCH_D(g, true_resid_k, mg->kb, KTHREADS, g, L, mg->diag64, zz, xv, mg->r, dlinf);
     timing_end(h, tk);
     double res = read_linf(h, dlinf);
     while (!(res <= tol) && total < itmx) {
@@ -817,7 +894,7 @@ static int poisson_solve_mixed(ia_handle* h, double* xv, const double* zz, const
             const double beta = (it == 0) ? 0.0 : (-alpha_prev * sq) / rho_prev;
             tk = timing_begin(h, TK_KRYLOV);
             { xpby32_k<<<mg->kb, KTHREADS, 0, st>>>(g, sv, float(beta), mg->p32); ia::note_launch(); }
-            { matvec32_dot_k<<<mg->kb, KTHREADS, 0, st>>>(g, F.L32, mg->p32, mg->q32, mg->partial); ia::note_launch(); }
+            LAUNCH_D(g, matvec32_dot_k, mg->kb, KTHREADS, g, F.L32, mg->p32, mg->q32, mg->partial);
             { finalize_k<<<1, 1024, 0, st>>>(mg->partial, mg->kb, 1, dots); ia::note_launch(); }
             timing_end(h, tk);
             cudaMemcpyAsync(mg->hsc + 2, dots, 8, cudaMemcpyDeviceToHost, st);
@@ -839,7 +916,7 @@ static int poisson_solve_mixed(ia_handle* h, double* xv, const double* zz, const
         tk = timing_begin(h, TK_KRYLOV);
         { add_correction_k<<<mg->kb, KTHREADS, 0, st>>>(g, mg->e32, xv); ia::note_launch(); }
         cudaMemsetAsync(dlinf, 0, 8, st);
-        { true_resid_k<<<mg->kb, KTHREADS, 0, st>>>(g, L, mg->diag64, zz, xv, mg->r, dlinf); ia::note_launch(); }
+        LAUNCH_D(g, true_resid_k, mg->kb, KTHREADS, g, L, mg->diag64, zz, xv, mg->r, dlinf);
         timing_end(h, tk);
         const double res_old = res;
         res = read_linf(h, dlinf);
@@ -863,7 +940,7 @@ int poisson_residual(ia_handle* h, double* r, const double* x, const double* z, 
     cudaStream_t st = h->stream;
     unsigned long long* d = reinterpret_cast<unsigned long long*>(h->dscalar + 60);
     cudaMemsetAsync(d, 0, 8, st);
-    { true_resid_k<<<kblocks(h->g), KTHREADS, 0, st>>>(h->g, L, nullptr, z, x, r, d); ia::note_launch(); }
+    LAUNCH_D(h->g, true_resid_k, kblocks(h->g), KTHREADS, h->g, L, nullptr, z, x, r, d);
     unsigned long long v = 0;
     cudaMemcpyAsync(&v, d, 8, cudaMemcpyDeviceToHost, st);
     if (cudaStreamSynchronize(st) != cudaSuccess) return IA_ERR_CUDA;
@@ -888,7 +965,7 @@ int poisson_solve(ia_handle* h, double* xv, const double* zz, const double* L, d
     double* dots = mg->dsc;
     cudaMemsetAsync(dlinf, 0, 8, st);
     int tk = timing_begin(h, TK_KRYLOV);
-    { true_resid_k<<<mg->kb, KTHREADS, 0, st>>>(g, L, mg->diag64, zz, xv, mg->r, dlinf); ia::note_launch(); }
+    LAUNCH_D(g, true_resid_k, mg->kb, KTHREADS, g, L, mg->diag64, zz, xv, mg->r, dlinf);
     timing_end(h, tk);
     double res = read_linf(h, dlinf);
     int it = 0;
@@ -907,7 +984,7 @@ int poisson_solve(ia_handle* h, double* xv, const double* zz, const double* L, d
         const double rho = sr;
         tk = timing_begin(h, TK_KRYLOV);
         { xpby_k<<<mg->kb, KTHREADS, 0, st>>>(g, mg->s, beta, mg->p); ia::note_launch(); }
-        { matvec_dot_k<<<mg->kb, KTHREADS, 0, st>>>(g, L, mg->diag64, mg->p, mg->q, mg->partial); ia::note_launch(); }
+        LAUNCH_D(g, matvec_dot_k, mg->kb, KTHREADS, g, L, mg->diag64, mg->p, mg->q, mg->partial);
         { finalize_k<<<1, 1024, 0, st>>>(mg->partial, mg->kb, 1, dots); ia::note_launch(); }
         timing_end(h, tk);
         cudaMemcpyAsync(mg->hsc + 2, dots, 8, cudaMemcpyDeviceToHost, st);
