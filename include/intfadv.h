@@ -71,7 +71,7 @@ extern "C" {
 #define IA_POISSON_LEARNED 2   /* as MIXED, inner FCG preconditioned by the conv net  */
 
 /* Inner preconditioner of IA_POISSON_LEARNED (ia_poisson_precond) */
-#define IA_PRECOND_HYBRID  0   /* s = Vcycle(r); s += ω·net(r - A s), ω least squares      */
+#define IA_PRECOND_HYBRID  0   /* s = Vcycle(r); s += ω·net(t), t = r - A s, ω energy-optimal */
 #define IA_PRECOND_NET     1   /* s = net(r)                                           */
 #define IA_PRECOND_NONE    2   /* s = r (plain CG; the ablation baseline)               */
 #define IA_PRECOND_VCYCLE  3   /* s = Vcycle(r) (the fallback)                          */
@@ -257,10 +257,13 @@ int ia_nn_get_params(ia_handle* h, float* params);
  * inference kernels */
 int ia_nn_forward(ia_handle* h, const float* x0, float* out, int32_t B, int32_t nx, int32_t ny, int32_t nz,
                   int32_t tensor_cores);
-/* MSE loss (mean over interior cells) and its gradient (device, NULL = keep in the handle) */
+/* training loss (mean over interior cells) and its gradient (device, NULL = keep in the handle) */
 int ia_nn_loss_grad(ia_handle* h, const float* x0, const float* target, int32_t B, int32_t nx, int32_t ny,
                     int32_t nz, float* grad, double* loss);
-/* one Adam step (β1 0.9, β2 0.999, ε 1e-8) on the MSE loss of the handle's net; loss before
+/* training loss of the handle's net: 0 = mean squared error (default), 1 = energy norm of the
+ * error, Σ_cells Σ_d c_d (δ[p] - δ[p-e_d])² / n with c_d the input coefficient channels */
+int ia_nn_set_loss(ia_handle* h, int32_t kind);
+/* one Adam step (β1 0.9, β2 0.999, ε 1e-8) on the training loss of the handle's net; loss before
  * the step */
 int ia_nn_train_step(ia_handle* h, const float* x0, const float* target, int32_t B, int32_t nx, int32_t ny,
                      int32_t nz, float lr, double* loss);

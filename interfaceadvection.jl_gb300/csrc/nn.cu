@@ -254,6 +254,40 @@ __global__ void mse_k(Dims d, const float* __restrict__ out, const float* __rest
     if (threadIdx.x == 0) atomicAdd(loss, sm[0] * inv);
 }
 
+// Energy norm of the error with the patch's own coefficients: δ = out - tgt,
+// E = Σ_p Σ_d c[p,d] (δ[p] - δ[p-e_d])² / n with c = input channel 1+d (λρ·L on the cell's lower
+// d-face; zero on walls and in the halo, where δ is zero too); dout = dE/dout.
+__global__ void energy_k(Dims d, const float* __restrict__ out, const float* __restrict__ tgt,
+                         const float* __restrict__ x0, float* __restrict__ dout, double* __restrict__ loss) {
+    __shared__ double sm[256];
+    const double inv = 1.0 / double(d.cells());
+    const long long off[3] = {1, (long long)(d.nx + 2), (long long)(d.nx + 2) * (d.ny + 2)};
+    double acc = 0.0;
+    FOR_CELLS(d) {
+        int b, x, y, z;
+        d.decode(q, b, x, y, z);
+        const long long p = d.pos(b, x, y, z);
+        const float dp = out[p] - tgt[p];
+        float g = 0.f;
+        for (int k = 0; k < 3; ++k) {
+            const long long lo = p - off[k], hi = p + off[k];
+            const float dl = dp - (out[lo] - tgt[lo]);          // across the lower face
+            const float dh = (out[hi] - tgt[hi]) - dp;          // across the upper face
+            const float cl = x0[p * 4 + 1 + k], ch = x0[hi * 4 + 1 + k];
+            acc += double(cl) * double(dl) * double(dl);
+            g += cl * dl - ch * dh;
+        }
+        dout[p] = float(2.0 * inv) * g;
+    }
+    sm[threadIdx.x] = acc;
+    __syncthreads();
+    for (int w = 128; w > 0; w >>= 1) {
+        if (threadIdx.x < w) sm[threadIdx.x] += sm[threadIdx.x + w];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) atomicAdd(loss, sm[0] * inv);
+}
+
 __global__ void adam_k(long long n, float* __restrict__ w, const float* __restrict__ g, float* __restrict__ m,
                        float* __restrict__ v, float lr, float b1, float b2, float eps, float c1, float c2) {
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
@@ -543,20 +577,39 @@ __global__ void absmax_k(Dims d, const float* __restrict__ r, unsigned int* __re
     if (threadIdx.x == 0) atomicMax(out, sm[0]);
 }
 
-// channels: r / max|r|, λρ·L_x, λρ·L_y, λρ·L_z (lower-face coefficients of the cell), zeros
+// Two batch entries from one grid (d.B == 1): entry 0 = (r / max|r|, λρ·L_x, λρ·L_y, λρ·L_z),
+// entry 1 the same with -r; channels 4..15 zero.  L are the cell's lower-face coefficients.
 __global__ void prep_k(Dims d, const float* __restrict__ r, const float* __restrict__ L, long long ncomp, float lrho,
                        const unsigned int* __restrict__ scale, __nv_bfloat16* __restrict__ x16) {
     const float sc = __uint_as_float(*scale);
     const float inv = sc > 0.f ? 1.f / sc : 0.f;
+    const long long stride = d.padded();
     FOR_CELLS(d) {
         int b, x, y, z;
         d.decode(q, b, x, y, z);
         const long long p = d.pos(b, x, y, z);
-        const __nv_bfloat162 c01 = __floats2bfloat162_rn(r[p] * inv, lrho * L[p]);
+        const float rv = r[p] * inv;
+        const __nv_bfloat162 c01 = __floats2bfloat162_rn(rv, lrho * L[p]);
+        const __nv_bfloat162 m01 = __floats2bfloat162_rn(-rv, lrho * L[p]);
         const __nv_bfloat162 c23 = __floats2bfloat162_rn(lrho * L[p + ncomp], lrho * L[p + 2 * ncomp]);
+        const uint32_t w23 = *reinterpret_cast<const uint32_t*>(&c23);
         uint4* dst = reinterpret_cast<uint4*>(x16 + p * 16);
-        dst[0] = make_uint4(*reinterpret_cast<const uint32_t*>(&c01), *reinterpret_cast<const uint32_t*>(&c23), 0u, 0u);
+        dst[0] = make_uint4(*reinterpret_cast<const uint32_t*>(&c01), w23, 0u, 0u);
         dst[1] = make_uint4(0u, 0u, 0u, 0u);
+        uint4* dm = reinterpret_cast<uint4*>(x16 + (p + stride) * 16);
+        dm[0] = make_uint4(*reinterpret_cast<const uint32_t*>(&m01), w23, 0u, 0u);
+        dm[1] = make_uint4(0u, 0u, 0u, 0u);
+    }
+}
+
+// odd part of the net: out = (net(r) - net(-r)) / 2, so that out(0) = 0 and out(-r) = -out(r)
+__global__ void odd_k(Dims d, const float* __restrict__ y2, float* __restrict__ out) {
+    const long long stride = d.padded();
+    FOR_CELLS(d) {
+        int b, x, y, z;
+        d.decode(q, b, x, y, z);
+        const long long p = d.pos(b, x, y, z);
+        out[p] = 0.5f * (y2[p] - y2[p + stride]);
     }
 }
 
@@ -566,6 +619,7 @@ __global__ void prep_k(Dims d, const float* __restrict__ r, const float* __restr
 struct NNState {
     float *w = nullptr, *g = nullptr, *m = nullptr, *v = nullptr;   // FP32 parameters, gradient, Adam moments
     long long step = 0;
+    int loss_kind = 0;                                               // 0 MSE, 1 energy norm
     uint8_t* wtc[nn::NLAYER] = {nullptr};                            // BF16 weights, shared-memory layout
     float* bias_tc = nullptr;                                        // padded biases (16 or 32 per layer)
     bool tc_dirty = true;
@@ -580,6 +634,8 @@ struct NNState {
     // preconditioner input (BF16, 16 channels, grid-shaped) and its scale
     __nv_bfloat16* x16 = nullptr;
     size_t x16_bytes = 0;
+    float* y2 = nullptr;   // net output of both entries
+    size_t y2_bytes = 0;
     unsigned int* dscale = nullptr;
     double* dloss = nullptr;
     int* derr = nullptr;
@@ -765,7 +821,9 @@ int loss_grad(ia_handle* h, NNState* s, const float* x0, const float* tgt, const
     cudaMemcpyAsync(G.tgt, tgt, sizeof(float) * f.padded(), cudaMemcpyDeviceToDevice, st);
     forward_f32(G, s->w, st);
     cudaMemsetAsync(s->dloss, 0, 8, st);
-    { nn::mse_k<<<nblk(f.cells()) < 1024 ? nblk(f.cells()) : 1024, 256, 0, st>>>(f, G.out, G.tgt, G.dout, s->dloss); ia::note_launch(); }
+    const int nbl = nblk(f.cells()) < 1024 ? nblk(f.cells()) : 1024;
+    if (s->loss_kind == 1) { nn::energy_k<<<nbl, 256, 0, st>>>(f, G.out, G.tgt, G.x0, G.dout, s->dloss); ia::note_launch(); }
+    else { nn::mse_k<<<nbl, 256, 0, st>>>(f, G.out, G.tgt, G.dout, s->dloss); ia::note_launch(); }
     { nn::zero_f32<<<256, 256, 0, st>>>(nn::NPARAM, s->g); ia::note_launch(); }
     backward_f32(G, s->w, s->g, st);
     if (loss_out) {
@@ -861,14 +919,15 @@ int check_dims(int B, int nx, int ny, int nz) {
 
 }  // namespace
 
-// Preconditioner application for the Poisson solver: out (FP32, grid layout, interior
-// cells written) = net(r / max|r|, λρ·L) for a 3D grid with interior dims nx, ny, nz.
+// Preconditioner application for the Poisson solver: out (FP32, grid layout, interior cells
+// written) = odd part of net(r / max|r|, λρ·L) on a 3D grid with interior dims nx, ny, nz; the
+// entries for r and -r run as one batch of two.
 int nn_apply(ia_handle* h, const float* r, const float* L32, float* out, int nx, int ny, int nz, long long ncomp) {
     NNState* s = nn_state(h);
     if (!s) return IA_ERR_CUDA;
     cudaStream_t st = h->stream;
-    const nn::Dims f{1, nx, ny, nz};
-    const size_t need = 2 * 16 * (size_t)f.padded();
+    const nn::Dims f{1, nx, ny, nz}, f2{2, nx, ny, nz};
+    const size_t need = 2 * 16 * (size_t)f2.padded();
     if (need > s->x16_bytes) {
         cudaFree(s->x16);
         s->x16 = nullptr;
@@ -877,11 +936,23 @@ int nn_apply(ia_handle* h, const float* r, const float* L32, float* out, int nx,
         s->x16_bytes = need;
         if (cudaMemsetAsync(s->x16, 0, need, st) != cudaSuccess) return IA_ERR_CUDA;
     }
+    const size_t need_y = 4 * (size_t)f2.padded();
+    if (need_y > s->y2_bytes) {
+        cudaFree(s->y2);
+        s->y2 = nullptr;
+        s->y2_bytes = 0;
+        if (cudaMalloc(&s->y2, need_y) != cudaSuccess) return IA_ERR_CUDA;
+        s->y2_bytes = need_y;
+        if (cudaMemsetAsync(s->y2, 0, need_y, st) != cudaSuccess) return IA_ERR_CUDA;
+    }
     cudaMemsetAsync(s->dscale, 0, 4, st);
     const int nb = nblk(f.cells()) < 1216 ? nblk(f.cells()) : 1216;
     { nn::absmax_k<<<nb, 256, 0, st>>>(f, r, s->dscale); ia::note_launch(); }
     { nn::prep_k<<<nblk(f.cells()), 256, 0, st>>>(f, r, L32, ncomp, float(h->cfg.lrho), s->dscale, s->x16); ia::note_launch(); }
-    return forward_tc(h, s, f, s->x16, out);
+    const int rc = forward_tc(h, s, f2, s->x16, s->y2);
+    if (rc != IA_OK) return rc;
+    { nn::odd_k<<<nblk(f.cells()), 256, 0, st>>>(f, s->y2, out); ia::note_launch(); }
+    return cudaGetLastError() == cudaSuccess ? IA_OK : IA_ERR_CUDA;
 }
 int nn_error_flag(ia_handle* h) {
     if (!h->nn) return 0;
@@ -894,7 +965,7 @@ void nn_destroy(ia_handle* h) {
     if (!s) return;
     cudaFree(s->w); cudaFree(s->g); cudaFree(s->m); cudaFree(s->v);
     for (int l = 0; l < nn::NLAYER; ++l) cudaFree(s->wtc[l]);
-    cudaFree(s->bias_tc); cudaFree(s->buf); cudaFree(s->ibuf); cudaFree(s->x16);
+    cudaFree(s->bias_tc); cudaFree(s->buf); cudaFree(s->ibuf); cudaFree(s->x16); cudaFree(s->y2);
     cudaFree(s->dloss); cudaFree(s->derr); cudaFree(s->dscale);
     delete s;
     h->nn = nullptr;
@@ -917,6 +988,14 @@ int ia_nn_set_params(ia_handle* h, const float* params) {
     cudaMemset(s->v, 0, 4 * (size_t)nn::NPARAM);
     s->step = 0;
     s->tc_dirty = true;
+    return IA_OK;
+}
+
+int ia_nn_set_loss(ia_handle* h, int32_t kind) {
+    if (!h || kind < 0 || kind > 1) return IA_ERR_INVALID;
+    NNState* s = nn_state(h);
+    if (!s) return IA_ERR_CUDA;
+    s->loss_kind = kind;
     return IA_OK;
 }
 

@@ -514,17 +514,18 @@ __global__ void update32_k(Grid g, float alpha, const float* __restrict__ pv, co
     if (threadIdx.x == 0) atomicMax(linf, (unsigned int)m);
 }
 
-// ---- learned hybrid preconditioner: t = A v with partial dots r·t and t·t
+// ---- learned hybrid preconditioner: partial dots n·t and n·An for the energy-optimal step
+// ω = (n·t)/(n·An), which minimises the A-norm of the error e - ω n left behind the V-cycle
+// (t = A e); A is negative semi-definite here, so both dots carry the same sign.
 template <int D>
-__global__ void matvec32_dot2_k(Grid g, const float* __restrict__ L, const float* __restrict__ v,
-                                float* __restrict__ t, const float* __restrict__ r, double* __restrict__ partial) {
+__global__ void energy_dots_k(Grid g, const float* __restrict__ L, const float* __restrict__ n,
+                              const float* __restrict__ t, double* __restrict__ partial) {
     float a1 = 0.f, a2 = 0.f;
     ROWS_BEGIN_D(g)
     const Nb o = nb_of<D>(g, x, y, z);
-    const float w = off7<D>(g, L, v, I, o) + diag7<D>(g, L, I) * v[I];
-    t[I] = w;
-    a1 += r[I] * w;
-    a2 += w * w;
+    const float an = off7<D>(g, L, n, I, o) + diag7<D>(g, L, I) * n[I];
+    a1 += n[I] * t[I];
+    a2 += n[I] * an;
     ROWS_END
     double b1 = a1, b2 = a2;
     block_sum2(b1, b2);
@@ -534,11 +535,12 @@ __global__ void matvec32_dot2_k(Grid g, const float* __restrict__ L, const float
     }
 }
 
-// s += ω n with ω = (t·An)/(An·An) from the device dots (0 unless An·An is positive and finite)
+// s += ω n with ω = (n·t)/(n·An) from the device dots (0 unless both are finite and n·An ≠ 0)
 __global__ void add_scaled_k(Grid g, const double* __restrict__ dots, const float* __restrict__ nv,
                              float* __restrict__ sv) {
-    const double tn = dots[0], n2 = dots[1];
-    const float w = float((n2 > 0.0 && n2 < 1e300 && tn == tn) ? tn / n2 : 0.0);
+    const double tn = dots[0], nan_ = dots[1];
+    const bool ok = nan_ != 0.0 && nan_ == nan_ && tn == tn && fabs(nan_) < 1e300 && fabs(tn) < 1e300;
+    const float w = float(ok ? tn / nan_ : 0.0);
     ROWS_BEGIN(g)
     sv[I] += w * nv[I];
     ROWS_END
@@ -820,7 +822,7 @@ static int poisson_solve_mixed(ia_handle* h, double* xv, const double* zz, const
     unsigned long long* dlinf = reinterpret_cast<unsigned long long*>(mg->dsc + 8);
     unsigned int* dlinf32 = reinterpret_cast<unsigned int*>(mg->dsc + 9);
     double* dots = mg->dsc;
-    double* hdots = mg->dsc + 12;                                  // hybrid t·An, An·An
+    double* hdots = mg->dsc + 12;                                  // hybrid n·t, n·An
     const bool learned = h->cfg.poisson_mode == IA_POISSON_LEARNED;
     // inner residual: the V-cycle reads its right-hand side from F.b32, so the plain mixed
     // mode keeps the residual there; the learned modes keep it apart
@@ -855,14 +857,14 @@ static int poisson_solve_mixed(ia_handle* h, double* xv, const double* zz, const
         if (vcyc() != cudaSuccess) return false;
         if (mode != IA_PRECOND_HYBRID) return true;
         // hybrid: the net corrects what the V-cycle left, s += ω net(t) with t = r - A s and
-        // ω minimising |t - ω A net(t)|
+        // ω = (n·t)/(n·An), the energy-optimal step along n = net(t)
         int tk = timing_begin(h, TK_KRYLOV);
         if (g.D == 3) { residual_k<float, 3><<<cell_grid(g), blk(), 0, st>>>(g, F.L32, rr, F.x32, mg->t32); ia::note_launch(); }
         else { residual_k<float, 2><<<cell_grid(g), blk(), 0, st>>>(g, F.L32, rr, F.x32, mg->t32); ia::note_launch(); }
         timing_end(h, tk);
         if (!net(mg->t32)) return false;
         tk = timing_begin(h, TK_KRYLOV);
-        LAUNCH_D(g, matvec32_dot2_k, mg->kb, KTHREADS, g, F.L32, mg->nl32, F.r32, mg->t32, mg->partial);
+        LAUNCH_D(g, energy_dots_k, mg->kb, KTHREADS, g, F.L32, mg->nl32, mg->t32, mg->partial);
         { finalize_k<<<1, 1024, 0, st>>>(mg->partial, mg->kb, 2, hdots); ia::note_launch(); }
         { add_scaled_k<<<mg->kb, KTHREADS, 0, st>>>(g, hdots, mg->nl32, F.x32); ia::note_launch(); }
         timing_end(h, tk);

@@ -82,6 +82,7 @@ _SIGS = {
     "ia_nn_param_count": (C.c_int64, []),
     "ia_nn_set_params": (C.c_int, [C.c_void_p, C.c_void_p]),
     "ia_nn_get_params": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "ia_nn_set_loss": (C.c_int, [C.c_void_p, C.c_int32]),
     "ia_nn_forward": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p] + [C.c_int32] * 5),
     "ia_nn_loss_grad": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p] + [C.c_int32] * 4 +
                         [C.c_void_p, C.POINTER(C.c_double)]),

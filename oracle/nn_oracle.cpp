@@ -202,20 +202,46 @@ void orc_nn_forward(const double* w, const double* x0, int B, int nx, int ny, in
     std::memcpy(out, A.out.data(), sizeof(double) * A.out.size());
 }
 
-// mean squared error over interior cells and its gradient with respect to w
-double orc_nn_loss_grad(const double* w, const double* x0, const double* tgt, int B, int nx, int ny, int nz,
-                        double* grad) {
+// training loss over interior cells and its gradient with respect to w; kind 0: mean squared
+// error; kind 1: energy norm Σ_p Σ_d c[p,d] (δ[p] - δ[p-e_d])² / n, δ = out - tgt, with c the
+// input channels 1..3 (zero in the halo, where δ is zero too)
+double orc_nn_loss_grad_kind(const double* w, const double* x0, const double* tgt, int B, int nx, int ny, int nz,
+                             int kind, double* grad) {
     Acts A = make(x0, B, nx, ny, nz);
     forward(w, A);
     const Dm &f = A.f, &hf = A.hf, &qt = A.qt;
     const double n = double(B) * nx * ny * nz;
     double loss = 0.0;
     V dout = zeros(f, 1);
-    FOR_INTERIOR(f) {
-        const long long p = f.pos(b, x, y, z);
-        const double e = A.out[p] - tgt[p];
-        loss += e * e;
-        dout[p] = 2.0 * e / n;
+    if (kind == 0) {
+        FOR_INTERIOR(f) {
+            const long long p = f.pos(b, x, y, z);
+            const double e = A.out[p] - tgt[p];
+            loss += e * e;
+            dout[p] = 2.0 * e / n;
+        }
+    } else {
+        V dl = zeros(f, 1);
+        for (long long p = 0; p < f.padded(); ++p) dl[p] = A.out[p] - tgt[p];
+        const long long off[3] = {1, (long long)(nx + 2), (long long)(nx + 2) * (ny + 2)};
+        FOR_INTERIOR(f) {
+            const long long p = f.pos(b, x, y, z);
+            for (int k = 0; k < 3; ++k) {
+                const double c = x0[p * 4 + 1 + k];
+                const double jump = dl[p] - dl[p - off[k]];
+                loss += c * jump * jump;
+                // the face term touches p and p - e_d; the halo cell p - e_d is not an output
+                dout[p] += 2.0 * c * jump / n;
+                dout[p - off[k]] -= 2.0 * c * jump / n;
+            }
+        }
+        // gradients scattered into halo positions are not outputs of the net
+        V keep = zeros(f, 1);
+        FOR_INTERIOR(f) {
+            const long long p = f.pos(b, x, y, z);
+            keep[p] = dout[p];
+        }
+        dout = keep;
     }
     loss /= n;
     if (!grad) return loss;
@@ -241,6 +267,11 @@ double orc_nn_loss_grad(const double* w, const double* x0, const double* tgt, in
     relu_bwd(f, 16, A.z1, da1, dz1);
     conv_bwd(f, 4, 16, A.x0, dz1, w + woff(0), grad + woff(0), grad + boff(0), nullptr);
     return loss;
+}
+
+double orc_nn_loss_grad(const double* w, const double* x0, const double* tgt, int B, int nx, int ny, int nz,
+                        double* grad) {
+    return orc_nn_loss_grad_kind(w, x0, tgt, B, nx, ny, nz, 0, grad);
 }
 
 // one Adam step (β1, β2, ε as the GPU kernel), t = step number starting at 1

@@ -91,6 +91,7 @@ def lib():
             "orc_nn_param_count": (i64, []),
             "orc_nn_forward": (None, [p, p, i, i, i, i, p]),
             "orc_nn_loss_grad": (d, [p, p, p, i, i, i, i, p]),
+            "orc_nn_loss_grad_kind": (d, [p, p, p, i, i, i, i, i, p]),
             "orc_nn_adam": (None, [i64, p, p, p, p, d, i64]),
         }
         for name, (res, args) in sig.items():
@@ -207,14 +208,15 @@ def nn_forward(w, x0):
     return out
 
 
-def nn_loss_grad(w, x0, tgt):
-    """MSE loss over interior cells and its gradient (FP64)."""
+def nn_loss_grad(w, x0, tgt, kind="mse"):
+    """Training loss over interior cells ("mse" or "energy") and its gradient (FP64)."""
     B, nzp, nyp, nxp, _ = x0.shape
     w, pw = _c64(w)
     x0, px = _c64(x0)
     tgt, pt = _c64(tgt)
     g = np.zeros(w.size, dtype=np.float64)
-    loss = lib().orc_nn_loss_grad(pw, px, pt, B, nxp - 2, nyp - 2, nzp - 2, g.ctypes.data)
+    loss = lib().orc_nn_loss_grad_kind(pw, px, pt, B, nxp - 2, nyp - 2, nzp - 2, {"mse": 0, "energy": 1}[kind],
+                                       g.ctypes.data)
     return float(loss), g
 
 

@@ -70,6 +70,26 @@ def test_loss_gradient_matches_oracle(net):
             assert e < 5e-5, (l, a, e)
 
 
+def test_energy_loss_gradient_matches_oracle(net):
+    w = params(3)
+    net.set_params(w)
+    x0, tgt, gx, gt = rand_case(2, 8, 12, 8, seed=9)
+    x0[..., 1:] = np.abs(x0[..., 1:])
+    gx = torch.tensor(x0, device="cuda")
+    loss_o, g_o = O.nn_loss_grad(w.astype(np.float64), x0.astype(np.float64), tgt.astype(np.float64), "energy")
+    net.set_loss("energy")
+    try:
+        loss_g, g_g = net.loss_grad(gx, gt)
+    finally:
+        net.set_loss("mse")
+    g_g = g_g.cpu().numpy().astype(np.float64)
+    assert abs(loss_g - loss_o) < 1e-5 * loss_o
+    for l, ((wo, bo), co) in enumerate(zip(learned.layer_offsets(), learned.COUT)):
+        for a, b in ((wo, bo), (bo, bo + co)):
+            e = np.abs(g_g[a:b] - g_o[a:b]).max() / np.abs(g_o[a:b]).max()
+            assert e < 5e-5, (l, a, e)
+
+
 def test_adam_step_matches_oracle(net):
     w = params(4)
     net.set_params(w)
@@ -191,12 +211,36 @@ def test_untrained_hybrid_matches_vcycle_iterations_when_net_is_zero(system):
     assert it_h == it_m and res_h <= 1e-8 and st["fallbacks"] == 0
 
 
+def _cos(a, b):
+    a, b = a.double().flatten(), b.double().flatten()
+    return float((a @ b) / (a.norm() * b.norm()))
+
+
 @pytest.mark.skipif(not os.path.exists(learned.WEIGHTS), reason="no trained weights shipped")
-def test_trained_net_gain_over_no_preconditioner(system):
-    # the trained net (shipped weights) against the same flexible CG without it
+def test_trained_net_predicts_held_out_corrections(net):
+    # what training gains: on patch pairs from runs the training never saw (seeds 5000+), the
+    # shipped net's output is aligned with the multigrid correction; the untrained net's is not
+    gen = learned.PairGenerator(N=64, P=32, seed_base=5000, steps_per_run=2)
+    pairs = []
+    for k, pr in enumerate(gen.pairs()):
+        pairs.append(pr)
+        if k >= 11:
+            break
+    net.set_params(learned.load_params()[0])
+    trained = [_cos(net.forward(x0)[0, 1:-1, 1:-1, 1:-1], t[0, 1:-1, 1:-1, 1:-1]) for x0, t in pairs]
+    net.set_params(learned.init_params(7))
+    untrained = [_cos(net.forward(x0)[0, 1:-1, 1:-1, 1:-1], t[0, 1:-1, 1:-1, 1:-1]) for x0, t in pairs]
+    assert np.median(trained) > 0.6, trained
+    assert np.median(np.abs(untrained)) < 0.3, untrained
+
+
+@pytest.mark.skipif(not os.path.exists(learned.WEIGHTS), reason="no trained weights shipped")
+def test_trained_hybrid_converges_without_fallback(system):
+    # the shipped net inside the hybrid preconditioner: converges to the FP64 tolerance with no
+    # fallback and within a quarter of the V-cycle's iteration count (it does not beat it)
     L, z = system
-    _, it_none, res_none, _ = solve("learned", L, z, precond="none", inner_max=2000)
-    _, it_net, res_net, st = solve("learned", L, z, precond="net", inner_max=2000)
-    assert res_none <= 1e-8 and res_net <= 1e-8
-    assert st["fallbacks"] == 0
-    assert it_net < 0.5 * it_none, (it_net, it_none)
+    _, it_v, res_v, _ = solve("learned", L, z, precond="vcycle")
+    _, it_h, res_h, st = solve("learned", L, z, precond="hybrid")
+    assert res_v <= 1e-8 and res_h <= 1e-8
+    assert st["fallbacks"] == 0 and st["net"] == it_h
+    assert it_h <= 1.25 * it_v + 1, (it_h, it_v)

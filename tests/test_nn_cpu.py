@@ -86,6 +86,29 @@ def test_oracle_gradient_matches_finite_differences():
     assert loss > 0
 
 
+def test_oracle_energy_loss_gradient_matches_finite_differences():
+    x0, tgt = rand_case(1, 8, 8, 8, seed=3)
+    x0[..., 1:] = np.abs(x0[..., 1:])          # coefficient channels are non-negative in use
+    w = params(6)
+    loss, g = O.nn_loss_grad(w, x0, tgt, kind="energy")
+    rng = np.random.default_rng(12)
+    idx = []
+    for (wo, bo), co in zip(learned.layer_offsets(), learned.COUT):
+        idx += list(rng.integers(wo, bo, size=5)) + list(range(bo, bo + min(co, 2)))
+    h, floor, errs = 1e-5, 1e-4 * np.abs(g).max(), []
+    for i in idx:
+        wp, wm = w.copy(), w.copy()
+        wp[i] += h
+        wm[i] -= h
+        fd = (O.nn_loss_grad(wp, x0, tgt, "energy")[0] - O.nn_loss_grad(wm, x0, tgt, "energy")[0]) / (2 * h)
+        errs.append(abs(fd - g[i]) / max(floor, abs(g[i])))
+    errs = np.array(errs)
+    # a perturbation that moves a ReLU pre-activation across zero breaks the difference quotient
+    # itself; allow one such parameter
+    assert (errs < 1e-5).sum() >= len(errs) - 1 and errs.max() < 1e-2, errs
+    assert loss > 0
+
+
 def test_oracle_input_gradient_path_reaches_every_layer():
     # every layer's weight gradient is non-zero on a generic case (no dead layer)
     x0, tgt = rand_case(1, 8, 8, 8, seed=4)
