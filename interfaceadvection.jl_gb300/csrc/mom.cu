@@ -26,18 +26,26 @@ inline dim3 grd(const Grid& g) { return dim3((g.n[0] + 31) / 32, (g.n[1] + 7) / 
     const int z = blockIdx.z;                                                                      \
     if (x >= g.n[0] || y >= g.n[1]) return;
 
-// x / getρ for a face between cells with fractions fa, fb (src/VOFutil.jl:176, 198-201)
+// x / getρ and x · getρ for a face between cells with fractions fa, fb (src/VOFutil.jl:176,
+// 198-201).  The mixed-face forms stay out of line: inlined, they are if-converted and their
+// predicated-off FP64 instructions would take FP64 issue slots on every bulk face.
+__device__ __noinline__ double div_rho_mixed(double lrho, double one_m, double v, double fa, double fb) {
+    return v / (lrho + one_m * ((fa + fb) / 2.0));
+}
+__device__ __noinline__ double mul_rho_mixed(double lrho, double one_m, double v, double fa, double fb) {
+    return v * (lrho + one_m * ((fa + fb) / 2.0));
+}
 __device__ __forceinline__ double div_rho(const MomConsts& k, double v, double fa, double fb) {
     const unsigned long long a = dbits(fa), b = dbits(fb);
     if (a == b && a == 0ull) return v * k.inv_lrho;
     if (a == b && a == kOneBits) return v * k.inv_rho1;
-    return v / (k.lrho + k.one_m * ((fa + fb) / 2.0));
+    return div_rho_mixed(k.lrho, k.one_m, v, fa, fb);
 }
 __device__ __forceinline__ double mul_rho(const MomConsts& k, double v, double fa, double fb) {
     const unsigned long long a = dbits(fa), b = dbits(fb);
     if (a == b && a == 0ull) return v * k.lrho;
     if (a == b && a == kOneBits) return v * k.rho1;
-    return v * (k.lrho + k.one_m * ((fa + fb) / 2.0));
+    return mul_rho_mixed(k.lrho, k.one_m, v, fa, fb);
 }
 
 // ------------------------------------------------------------------ velocity from momentum
@@ -284,23 +292,56 @@ __device__ __forceinline__ double dila_q(const MomConsts& k, double rq_l, double
     return (cbar[P] ? rq_1 : rq_l) * ((u1[P + sd] - u1[P]) + (u2[P + sd] - u2[P]));
 }
 
-__global__ void momupdate_kern(MomConsts k, int j, const double* __restrict__ Phi, const double* __restrict__ uOld,
-                               const double* __restrict__ u1d, const double* __restrict__ u2d,
-                               const int8_t* __restrict__ cbar, double dt, double* __restrict__ rhou) {
+// ρu += δt (Φ(I) - Φ(I+δj) + uOld ϕ(i, I, ρ̄∂ⱼuⱼ)).  A block owns a 32 x 8 column of cells
+// and marches MU_ZC planes up z; each plane's ρ̄∂ⱼuⱼ/2 values (plus the x-1 / y-1 halo) go to
+// shared memory and the previous plane's stay in a register, so every value is computed once
+// (4 FP64 ops) instead of once per use (4 uses per cell).
+constexpr int MU_ZC = 16;
+
+template <int D>
+__global__ void __launch_bounds__(256) momupdate_kern(MomConsts k, int j, const double* __restrict__ Phi,
+                                                      const double* __restrict__ uOld,
+                                                      const double* __restrict__ u1d, const double* __restrict__ u2d,
+                                                      const int8_t* __restrict__ cbar, double dt,
+                                                      double* __restrict__ rhou) {
     const Grid& g = k.g;
-    CELL_XYZ
-    const int c0[3] = {x, y, z};
-    if (!is_interior(g, c0)) return;
-    const long long I = lin(g, x, y, z);
+    __shared__ double tile[9][33];
+    const int tx = threadIdx.x, ty = threadIdx.y;
+    const int x0 = 1 + blockIdx.x * 32, y0 = 1 + blockIdx.y * 8;
+    const int x = x0 + tx, y = y0 + ty;
+    const bool active = x <= g.n[0] - 2 && y <= g.n[1] - 2;
     const double rq_l = 0.25 * k.lrho, rq_1 = 0.25 * k.rho1;
-    int cc[3] = {x, y, z};
-    const double dI = dila_q(k, rq_l, rq_1, j, cc, u1d, u2d, cbar);
-    for (int i = 0; i < g.D; ++i) {
-        int cm[3] = {x, y, z};
-        cm[i] -= 1;
-        const double dm = dila_q(k, rq_l, rq_1, j, cm, u1d, u2d, cbar);
-        const double r = fma(uOld[I + i * g.N], dI + dm, Phi[I + i * g.N] - Phi[I + g.s[j] + i * g.N]);
-        rhou[I + i * g.N] = fma(dt, r, rhou[I + i * g.N]);
+    const int zs = D == 3 ? 1 + int(blockIdx.z) * MU_ZC : 0;
+    const int ze = D == 3 ? min(zs + MU_ZC, g.n[2] - 1) : 1;
+    double dprev = 0.0;
+    if (D == 3 && active) {
+        int cm[3] = {x, y, zs - 1};
+        dprev = dila_q(k, rq_l, rq_1, j, cm, u1d, u2d, cbar);
+    }
+    for (int z = zs; z < ze; ++z) {
+        for (int l = ty * 32 + tx; l < 9 * 33; l += 256) {
+            const int xx = x0 - 1 + l % 33, yy = y0 - 1 + l / 33;
+            double v = 0.0;
+            if (xx <= g.n[0] - 2 && yy <= g.n[1] - 2) {
+                int cc[3] = {xx, yy, z};
+                v = dila_q(k, rq_l, rq_1, j, cc, u1d, u2d, cbar);
+            }
+            tile[l / 33][l % 33] = v;
+        }
+        __syncthreads();
+        if (active) {
+            const long long I = lin(g, x, y, z);
+            const double dI = tile[ty + 1][tx + 1];
+            const double dm[3] = {tile[ty + 1][tx], tile[ty][tx + 1], dprev};
+            const long long sj = g.s[j];
+#pragma unroll
+            for (int i = 0; i < D; ++i) {
+                const double r = fma(uOld[I + i * g.N], dI + dm[i], Phi[I + i * g.N] - Phi[I + sj + i * g.N]);
+                rhou[I + i * g.N] = fma(dt, r, rhou[I + i * g.N]);
+            }
+            dprev = dI;
+        }
+        __syncthreads();
     }
 }
 
@@ -667,7 +708,10 @@ cudaError_t k_momflux(const MomConsts& k, int j, int limiter, const double* usta
 }
 cudaError_t k_momupdate(const MomConsts& k, int j, const double* Phi, const double* uOld, const double* u1,
                         const double* u2, const int8_t* cbar, double dt, double* rhou, cudaStream_t s) {
-    { momupdate_kern<<<grd(k.g), blk(), 0, s>>>(k, j, Phi, uOld, u1 + j * k.g.N, u2 + j * k.g.N, cbar, dt, rhou); ia::note_launch(); }
+    const Grid& g = k.g;
+    const dim3 tg((g.n[0] - 2 + 31) / 32, (g.n[1] - 2 + 7) / 8, g.D == 3 ? (g.n[2] - 2 + MU_ZC - 1) / MU_ZC : 1);
+    if (g.D == 3) { momupdate_kern<3><<<tg, blk(), 0, s>>>(k, j, Phi, uOld, u1 + j * g.N, u2 + j * g.N, cbar, dt, rhou); ia::note_launch(); }
+    else { momupdate_kern<2><<<tg, blk(), 0, s>>>(k, j, Phi, uOld, u1 + j * g.N, u2 + j * g.N, cbar, dt, rhou); ia::note_launch(); }
     return cudaGetLastError();
 }
 cudaError_t k_visc(const MomConsts& k, const double* u, const double* f, double lmu, double mu, double* Phi6,

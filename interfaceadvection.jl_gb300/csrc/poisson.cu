@@ -210,17 +210,26 @@ __global__ void residual_k(Grid g, const T* __restrict__ L, const T* __restrict_
     r[I] = b[I] - (off7<D>(g, L, xv, I, o) + diag7<D>(g, L, I) * xv[I]);
 }
 
-template <class T>
-__global__ void restrict_k(Grid gc, Grid gf, const T* __restrict__ rf, T* __restrict__ bc) {
-    const Grid& g = gc;
-    INTERIOR_XYZ
-    const int nz = g.D == 3 ? 2 : 1;
-    T s = T(0);
-    for (int k = 0; k < nz; ++k)
+// residual of the 2^D fine children of each coarse cell, summed straight into the coarse
+// right-hand side (residual_k + restrict_k without the fine residual array; same sums, same order)
+template <class T, int D>
+__global__ void resid_restrict_k(Grid gc, Grid gf, const T* __restrict__ L, const T* __restrict__ b,
+                                 const T* __restrict__ xv, T* __restrict__ bc) {
+    const int xc = 1 + blockIdx.x * blockDim.x + threadIdx.x;
+    const int yc = 1 + blockIdx.y * blockDim.y + threadIdx.y;
+    const int zc = D == 3 ? 1 + int(blockIdx.z) : 0;
+    if (xc > gc.n[0] - 2 || yc > gc.n[1] - 2) return;
+    const int s1 = int(gf.s[1]), s2 = int(gf.s[2]);
+    T sum = T(0);
+    for (int k = 0; k < (D == 3 ? 2 : 1); ++k)
         for (int j = 0; j < 2; ++j)
-            for (int i = 0; i < 2; ++i)
-                s += rf[lin(gf, 2 * c[0] - 1 + i, 2 * c[1] - 1 + j, g.D == 3 ? 2 * c[2] - 1 + k : 0)];
-    bc[I] = s;
+            for (int i = 0; i < 2; ++i) {
+                const int x = 2 * xc - 1 + i, y = 2 * yc - 1 + j, z = D == 3 ? 2 * zc - 1 + k : 0;
+                const int I = x + y * s1 + z * s2;
+                const Nb o = nb_of<D>(gf, x, y, z);
+                sum += b[I] - (off7<D>(gf, L, xv, I, o) + diag7<D>(gf, L, I) * xv[I]);
+            }
+    bc[xc + yc * int(gc.s[1]) + zc * int(gc.s[2])] = sum;
 }
 
 template <class T>
@@ -605,10 +614,9 @@ static cudaError_t vcycle(ia_handle* h, PoissonMG* mg, int l, cudaStream_t st, i
         half(0);
         half(1);
     }
-    if (L.g.D == 3) { residual_k<T, 3><<<cell_grid(L.g), blk(), 0, st>>>(L.g, Lc, b, x, r); ia::note_launch(); }
-    else { residual_k<T, 2><<<cell_grid(L.g), blk(), 0, st>>>(L.g, Lc, b, x, r); ia::note_launch(); }
     auto& C = mg->lev[l + 1];
-    { restrict_k<T><<<grd(C.g), blk(), 0, st>>>(C.g, L.g, r, C.template b_<T>()); ia::note_launch(); }
+    if (L.g.D == 3) { resid_restrict_k<T, 3><<<cell_grid(C.g), blk(), 0, st>>>(C.g, L.g, Lc, b, x, C.template b_<T>()); ia::note_launch(); }
+    else { resid_restrict_k<T, 2><<<cell_grid(C.g), blk(), 0, st>>>(C.g, L.g, Lc, b, x, C.template b_<T>()); ia::note_launch(); }
     cudaError_t e = vcycle<T>(h, mg, l + 1, st, nu1, nu2, nuc);
     if (e != cudaSuccess) return e;
     { prolong_k<T><<<grd(L.g), blk(), 0, st>>>(L.g, C.g, C.template x_<T>(), x); ia::note_launch(); }

@@ -220,11 +220,11 @@ def _cos(a, b):
 def test_trained_net_predicts_held_out_corrections(net):
     # what training gains: on patch pairs from runs the training never saw (seeds 5000+), the
     # shipped net's output is aligned with the multigrid correction; the untrained net's is not
-    gen = learned.PairGenerator(N=64, P=32, seed_base=5000, steps_per_run=2)
+    gen = learned.PairGenerator(N=128, P=64, seed_base=5000, steps_per_run=1)
     pairs = []
     for k, pr in enumerate(gen.pairs()):
         pairs.append(pr)
-        if k >= 11:
+        if k >= 9:
             break
     net.set_params(learned.load_params()[0])
     trained = [_cos(net.forward(x0)[0, 1:-1, 1:-1, 1:-1], t[0, 1:-1, 1:-1, 1:-1]) for x0, t in pairs]
