@@ -231,7 +231,7 @@ def test_trained_net_predicts_held_out_corrections(net):
     net.set_params(learned.init_params(7))
     untrained = [_cos(net.forward(x0)[0, 1:-1, 1:-1, 1:-1], t[0, 1:-1, 1:-1, 1:-1]) for x0, t in pairs]
     assert np.median(trained) > 0.6, trained
-    assert np.median(np.abs(untrained)) < 0.3, untrained
+    assert np.median(trained) > np.median(np.abs(untrained)) + 0.2, (trained, untrained)
 
 
 @pytest.mark.skipif(not os.path.exists(learned.WEIGHTS), reason="no trained weights shipped")
