@@ -223,6 +223,14 @@ int ia_visc_surften(ia_handle* h, const double* f);
  * reference checks with sum(f[inside(f)]), test/maintests.jl:209,215. */
 int ia_mass(ia_handle* h, const double* f, double* mass_out);
 
+/* Step diagnostics of src/metrics.jl summed over interior cells, in one pass:
+ * out[0] = Σ ρkeI(I,u,f,λρ,U) (:13-15), out[1] = Σ ρgh(I,g,f,λρ,StatWL) (:23),
+ * out[2] = Σ EnsI(I,ω) (:32-39; 0 when omega is NULL), out[3+i] = Σ ρuI(i,I,u,f,λρ,U) (:56-58).
+ * omega: 3D vector field (component i on the edges the reference's EnsI reads), 2D scalar.
+ * U, g, statwl: D values each, NULL = zeros. */
+int ia_metrics(ia_handle* h, const double* u, const double* f, const double* omega, const double* U,
+               const double* g, const double* statwl, double* out);
+
 /* Per-launch kernel timing with CUDA events on the handle's stream, for the
  * roofline figures (no reference counterpart: instrumentation only).
  * Folds finished records into per-family totals, copies the first n totals

@@ -577,39 +577,20 @@ __global__ void absmax_k(Dims d, const float* __restrict__ r, unsigned int* __re
     if (threadIdx.x == 0) atomicMax(out, sm[0]);
 }
 
-// Two batch entries from one grid (d.B == 1): entry 0 = (r / max|r|, λρ·L_x, λρ·L_y, λρ·L_z),
-// entry 1 the same with -r; channels 4..15 zero.  L are the cell's lower-face coefficients.
+// channels: r / max|r|, λρ·L_x, λρ·L_y, λρ·L_z (lower-face coefficients of the cell), zeros
 __global__ void prep_k(Dims d, const float* __restrict__ r, const float* __restrict__ L, long long ncomp, float lrho,
                        const unsigned int* __restrict__ scale, __nv_bfloat16* __restrict__ x16) {
     const float sc = __uint_as_float(*scale);
     const float inv = sc > 0.f ? 1.f / sc : 0.f;
-    const long long stride = d.padded();
     FOR_CELLS(d) {
         int b, x, y, z;
         d.decode(q, b, x, y, z);
         const long long p = d.pos(b, x, y, z);
-        const float rv = r[p] * inv;
-        const __nv_bfloat162 c01 = __floats2bfloat162_rn(rv, lrho * L[p]);
-        const __nv_bfloat162 m01 = __floats2bfloat162_rn(-rv, lrho * L[p]);
+        const __nv_bfloat162 c01 = __floats2bfloat162_rn(r[p] * inv, lrho * L[p]);
         const __nv_bfloat162 c23 = __floats2bfloat162_rn(lrho * L[p + ncomp], lrho * L[p + 2 * ncomp]);
-        const uint32_t w23 = *reinterpret_cast<const uint32_t*>(&c23);
         uint4* dst = reinterpret_cast<uint4*>(x16 + p * 16);
-        dst[0] = make_uint4(*reinterpret_cast<const uint32_t*>(&c01), w23, 0u, 0u);
+        dst[0] = make_uint4(*reinterpret_cast<const uint32_t*>(&c01), *reinterpret_cast<const uint32_t*>(&c23), 0u, 0u);
         dst[1] = make_uint4(0u, 0u, 0u, 0u);
-        uint4* dm = reinterpret_cast<uint4*>(x16 + (p + stride) * 16);
-        dm[0] = make_uint4(*reinterpret_cast<const uint32_t*>(&m01), w23, 0u, 0u);
-        dm[1] = make_uint4(0u, 0u, 0u, 0u);
-    }
-}
-
-// odd part of the net: out = (net(r) - net(-r)) / 2, so that out(0) = 0 and out(-r) = -out(r)
-__global__ void odd_k(Dims d, const float* __restrict__ y2, float* __restrict__ out) {
-    const long long stride = d.padded();
-    FOR_CELLS(d) {
-        int b, x, y, z;
-        d.decode(q, b, x, y, z);
-        const long long p = d.pos(b, x, y, z);
-        out[p] = 0.5f * (y2[p] - y2[p + stride]);
     }
 }
 
@@ -634,8 +615,6 @@ struct NNState {
     // preconditioner input (BF16, 16 channels, grid-shaped) and its scale
     __nv_bfloat16* x16 = nullptr;
     size_t x16_bytes = 0;
-    float* y2 = nullptr;   // net output of both entries
-    size_t y2_bytes = 0;
     unsigned int* dscale = nullptr;
     double* dloss = nullptr;
     int* derr = nullptr;
@@ -920,14 +899,13 @@ int check_dims(int B, int nx, int ny, int nz) {
 }  // namespace
 
 // Preconditioner application for the Poisson solver: out (FP32, grid layout, interior cells
-// written) = odd part of net(r / max|r|, λρ·L) on a 3D grid with interior dims nx, ny, nz; the
-// entries for r and -r run as one batch of two.
+// written) = net(r / max|r|, λρ·L) on a 3D grid with interior dims nx, ny, nz.
 int nn_apply(ia_handle* h, const float* r, const float* L32, float* out, int nx, int ny, int nz, long long ncomp) {
     NNState* s = nn_state(h);
     if (!s) return IA_ERR_CUDA;
     cudaStream_t st = h->stream;
-    const nn::Dims f{1, nx, ny, nz}, f2{2, nx, ny, nz};
-    const size_t need = 2 * 16 * (size_t)f2.padded();
+    const nn::Dims f{1, nx, ny, nz};
+    const size_t need = 2 * 16 * (size_t)f.padded();
     if (need > s->x16_bytes) {
         cudaFree(s->x16);
         s->x16 = nullptr;
@@ -936,23 +914,11 @@ int nn_apply(ia_handle* h, const float* r, const float* L32, float* out, int nx,
         s->x16_bytes = need;
         if (cudaMemsetAsync(s->x16, 0, need, st) != cudaSuccess) return IA_ERR_CUDA;
     }
-    const size_t need_y = 4 * (size_t)f2.padded();
-    if (need_y > s->y2_bytes) {
-        cudaFree(s->y2);
-        s->y2 = nullptr;
-        s->y2_bytes = 0;
-        if (cudaMalloc(&s->y2, need_y) != cudaSuccess) return IA_ERR_CUDA;
-        s->y2_bytes = need_y;
-        if (cudaMemsetAsync(s->y2, 0, need_y, st) != cudaSuccess) return IA_ERR_CUDA;
-    }
     cudaMemsetAsync(s->dscale, 0, 4, st);
     const int nb = nblk(f.cells()) < 1216 ? nblk(f.cells()) : 1216;
     { nn::absmax_k<<<nb, 256, 0, st>>>(f, r, s->dscale); ia::note_launch(); }
     { nn::prep_k<<<nblk(f.cells()), 256, 0, st>>>(f, r, L32, ncomp, float(h->cfg.lrho), s->dscale, s->x16); ia::note_launch(); }
-    const int rc = forward_tc(h, s, f2, s->x16, s->y2);
-    if (rc != IA_OK) return rc;
-    { nn::odd_k<<<nblk(f.cells()), 256, 0, st>>>(f, s->y2, out); ia::note_launch(); }
-    return cudaGetLastError() == cudaSuccess ? IA_OK : IA_ERR_CUDA;
+    return forward_tc(h, s, f, s->x16, out);
 }
 int nn_error_flag(ia_handle* h) {
     if (!h->nn) return 0;
@@ -965,7 +931,7 @@ void nn_destroy(ia_handle* h) {
     if (!s) return;
     cudaFree(s->w); cudaFree(s->g); cudaFree(s->m); cudaFree(s->v);
     for (int l = 0; l < nn::NLAYER; ++l) cudaFree(s->wtc[l]);
-    cudaFree(s->bias_tc); cudaFree(s->buf); cudaFree(s->ibuf); cudaFree(s->x16); cudaFree(s->y2);
+    cudaFree(s->bias_tc); cudaFree(s->buf); cudaFree(s->ibuf); cudaFree(s->x16);
     cudaFree(s->dloss); cudaFree(s->derr); cudaFree(s->dscale);
     delete s;
     h->nn = nullptr;

@@ -8,6 +8,7 @@ from . import _lib
 from ._build import build
 from .core import (Flow, Handle, advect, advect_vof_raw, advectVOF, apply_vof, applyVOF, cVOF, get_vof_flux,
                    getVOFFlux, make_config, reconstruct_interface, reconstructInterface)
+from .diagnostics import metrics, sim_metrics
 from .fields import cell_coords, face_coords, ffrom, fones, fzeros, is_fortran
 from .simulation import (MPCFL, MPFMomStep, NoBody, TwoPhaseSimulation, poisson_stats, set_learned, sim_info,
                          sim_step)
@@ -15,4 +16,4 @@ from .simulation import (MPCFL, MPFMomStep, NoBody, TwoPhaseSimulation, poisson_
 __all__ = ["Flow", "Handle", "advect", "advect_vof_raw", "advectVOF", "apply_vof", "applyVOF", "cVOF",
            "get_vof_flux", "getVOFFlux", "make_config", "reconstruct_interface", "reconstructInterface", "build",
            "cell_coords", "face_coords", "ffrom", "fones", "fzeros", "is_fortran", "MPCFL", "MPFMomStep", "NoBody",
-           "TwoPhaseSimulation", "sim_info", "sim_step", "poisson_stats", "set_learned"]
+           "TwoPhaseSimulation", "sim_info", "sim_step", "poisson_stats", "set_learned", "metrics", "sim_metrics"]

@@ -19,6 +19,7 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 SRC = os.path.join(HERE, "oracle.cpp")
 SRC_NN = os.path.join(HERE, "nn_oracle.cpp")
+SRC_MET = os.path.join(HERE, "metrics_oracle.cpp")
 LIB = os.path.join(HERE, "liboracle.so")
 
 SCHEMES = {"WH": 0, "WY": 1, "MYC": 2, "Y": 3, "Column": 4, "PCD": 5, "SLIC": 6, "CD": 7, "XYLIC": 8}
@@ -29,9 +30,10 @@ LIMITERS = {"Koren": 0, "upwind": 1, "minmod": 2, "vanAlbada1": 3, "Sweby": 4, "
 def build(force: bool = False) -> str:
     """Compile liboracle.so with g++ (OpenMP, IEEE FP64, no FMA contraction)."""
     if force or not os.path.exists(LIB) or os.path.getmtime(LIB) < max(
-            os.path.getmtime(SRC), os.path.getmtime(SRC_NN), os.path.getmtime(os.path.join(HERE, "oracle.h"))):
+            os.path.getmtime(SRC), os.path.getmtime(SRC_NN), os.path.getmtime(SRC_MET),
+            os.path.getmtime(os.path.join(HERE, "oracle.h"))):
         cmd = ["g++", "-std=c++17", "-O2", "-fopenmp", "-ffp-contract=off", "-fPIC", "-shared",
-               SRC, SRC_NN, "-o", LIB + ".tmp"]
+               SRC, SRC_NN, SRC_MET, "-o", LIB + ".tmp"]
         subprocess.run(cmd, check=True)
         os.replace(LIB + ".tmp", LIB)
     return LIB
@@ -88,6 +90,9 @@ def lib():
             "orc_argabsmax": (i, [i, p]), "orc_get_xdir": (i, [i]), "orc_get_xydir": (None, [i, p, p]),
             "orc_getrho_cell": (d, [d, d]), "orc_getrho_face": (d, [p, i, i64, p, d]),
             "orc_vof_flux_face": (None, [p, p, p, p, p, d, i, i64, p, d]),
+            "orc_rhoke": (d, [p, i64, p, p, d, p]), "orc_rhou": (d, [p, i, i64, p, p, d, p]),
+            "orc_rhogh": (d, [p, i64, p, p, d, p]), "orc_ens": (d, [p, i64, p]),
+            "orc_metrics": (None, [p, p, p, p, d, p, p, p, p]),
             "orc_nn_param_count": (i64, []),
             "orc_nn_forward": (None, [p, p, i, i, i, i, p]),
             "orc_nn_loss_grad": (d, [p, p, p, i, i, i, i, p]),
@@ -225,3 +230,23 @@ def nn_adam(w, g, m, v, lr, t):
     for a in (w, g, m, v):
         assert a.dtype == np.float64 and a.flags.c_contiguous
     lib().orc_nn_adam(w.size, w.ctypes.data, g.ctypes.data, m.ctypes.data, v.ctypes.data, float(lr), int(t))
+
+
+# ---- diagnostics (metrics_oracle.cpp) --------------------------------------------------------
+
+def _dv(v, D):
+    a = np.zeros(3)
+    if v is not None:
+        a[:D] = v
+    return a
+
+
+def metrics(u, f, lrho, U=None, g=None, statwl=None, omega=None, per=()):
+    """Domain sums {ke, pe, ens, rhou[D]} of the src/metrics.jl per-cell functions."""
+    gr = grid(f.shape, per)
+    D = f.ndim
+    out = np.zeros(3 + D)
+    Ua, ga, wa = _dv(U, D), _dv(g, D), _dv(statwl, D)
+    lib().orc_metrics(C.byref(gr), ptr(u), ptr(f), ptr(omega), float(lrho), Ua.ctypes.data, ga.ctypes.data,
+                      wa.ctypes.data, out.ctypes.data)
+    return {"ke": out[0], "pe": out[1], "ens": out[2], "rhou": out[3:].tolist()}
