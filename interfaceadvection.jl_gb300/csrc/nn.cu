@@ -12,6 +12,7 @@
 //    accumulator back with tcgen05.ld for the bias / ReLU / skip epilogue.
 //    Every mbarrier wait is bounded; on timeout the kernel raises an error flag,
 //    releases its TMEM and returns.
+#include <cuda.h>
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
@@ -518,6 +519,197 @@ __global__ void __launch_bounds__(128) conv_tc_kernel(Dims d, const __nv_bfloat1
     if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(32));
 }
 
+// ------------------------------------------------------------------ TMA-fed tensor-core convolution
+// A tile is M = 128 consecutive cells of one x-row (rows shorter than 128 leave the tail masked).
+// For each of the 9 (dy, dz) neighbour rows, one TMA box of WR = 136 consecutive cells x 8
+// channels per 8-channel chunk lands in shared memory as 136 rows of 16 B: the chunk column of a
+// K-major no-swizzle operand whose 8-row core matrices are contiguous (SBO 128 B) and whose
+// K-neighbour chunks are one box apart (LBO = 2176 B).  The A operand of tap (dx, dy, dz) is the
+// (dy, dz) window started dx + 1 rows in, so all 27 taps are read from one set of 9·Cin/8 boxes.
+// Two stages: thread 0 issues the next tile's boxes before the MMAs of this one; one commit per
+// tile releases the epilogue (all four warps, tcgen05.ld) and the stage.
+constexpr int WR = 136;
+constexpr int BOX_BYTES = WR * 16;
+
+template <int CI, int COP>
+struct TmaSmem {
+    static constexpr int W_BYTES = 27 * COP * CI * 2;
+    static constexpr int NBOX = 9 * (CI / 8);
+    static constexpr int STAGE_BYTES = NBOX * BOX_BYTES;
+    static constexpr int A_OFF = (W_BYTES + 1023) / 1024 * 1024;
+    static constexpr int BAR_OFF = A_OFF + 2 * STAGE_BYTES;
+    static constexpr int TOTAL = BAR_OFF + 64;
+};
+
+__device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap* map, int c0, int c1, uint32_t bar) {
+    asm volatile(
+        "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];"
+        ::"r"(dst), "l"(reinterpret_cast<uint64_t>(map)), "r"(c0), "r"(c1), "r"(bar)
+        : "memory");
+}
+
+template <int CI, int CO, bool RELU, bool OUTF32>
+__global__ void __launch_bounds__(128) conv_tma_kernel(const __grid_constant__ CUtensorMap tmap, Dims d,
+                                                       const uint8_t* __restrict__ Wg, const float* __restrict__ bias,
+                                                       const __nv_bfloat16* __restrict__ skip,
+                                                       __nv_bfloat16* __restrict__ Y, float* __restrict__ Yf,
+                                                       int* __restrict__ err) {
+    constexpr int COP = CO < 16 ? 16 : CO;
+    using S = TmaSmem<CI, COP>;
+    static_assert(CI % 16 == 0 && COP % 16 == 0 && COP <= 32, "tile shape");
+    extern __shared__ __align__(1024) uint8_t smem[];
+    __shared__ uint32_t tmem_holder;
+    const int tid = threadIdx.x, warp = tid >> 5;
+    for (int i = tid; i < S::W_BYTES / 16; i += blockDim.x)
+        reinterpret_cast<uint4*>(smem)[i] = __ldg(reinterpret_cast<const uint4*>(Wg) + i);
+    const uint32_t full0 = smem_u32(smem + S::BAR_OFF), mdone = full0 + 16;
+    if (tid == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(full0));
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(full0 + 8));
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(mdone));
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmem_holder)),
+                     "r"(32));
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+    }
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");   // weights: generic writes, async reads
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    const uint32_t tmem = tmem_holder;
+    const uint32_t wbase = smem_u32(smem), abase = smem_u32(smem + S::A_OFF);
+    constexpr uint32_t idesc = idesc_bf16(kM, COP);
+    const int xtiles = (d.nx + kM - 1) / kM;
+    const long long ntiles = (long long)xtiles * d.ny * d.nz * d.B;
+    const int rowp = d.nx + 2;
+    const long long planep = (long long)(d.nx + 2) * (d.ny + 2);
+    float bias_r[CO];
+#pragma unroll
+    for (int o = 0; o < CO; ++o) bias_r[o] = __ldg(bias + o);
+
+    auto tile_origin = [&](long long t, int& x0) -> long long {
+        x0 = int(t % xtiles) * kM;
+        long long r = t / xtiles;
+        const int y = int(r % d.ny);
+        r /= d.ny;
+        const int z = int(r % d.nz);
+        const int b = int(r / d.nz);
+        return d.pos(b, x0, y, z);
+    };
+    auto issue = [&](long long t, int s) {   // thread 0
+        int x0;
+        const long long p0 = tile_origin(t, x0);
+        const uint32_t bar = full0 + 8 * s;
+        asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(S::STAGE_BYTES)
+                     : "memory");
+        for (int w = 0; w < 9; ++w) {
+            const long long row = p0 - 1 + (long long)(w % 3 - 1) * rowp + (long long)(w / 3 - 1) * planep;
+#pragma unroll
+            for (int j = 0; j < CI / 8; ++j)
+                tma_load_2d(abase + s * S::STAGE_BYTES + (w * (CI / 8) + j) * BOX_BYTES, &tmap, 8 * j, int(row), bar);
+        }
+    };
+    int issued[2] = {0, 0}, waited[2] = {0, 0}, commits = 0, commits_waited = 0;
+    if (tid == 0 && (long long)blockIdx.x < ntiles) issue(blockIdx.x, 0);
+    if ((long long)blockIdx.x < ntiles) issued[0] = 1;
+    bool failed = false;
+    int i = 0;
+    for (long long tile = blockIdx.x; tile < ntiles; tile += gridDim.x, ++i) {
+        const int s = i & 1;
+        const long long next = tile + gridDim.x;
+        if (next < ntiles) {
+            if (tid == 0) issue(next, s ^ 1);
+            issued[s ^ 1] += 1;
+        }
+        bool ok = mbar_wait(full0 + 8 * s, uint32_t((i >> 1) & 1));
+        if (__syncthreads_or(!ok)) {
+            failed = true;
+            break;
+        }
+        waited[s] += 1;
+        if (tid == 0) {
+            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+            const uint32_t st = abase + s * S::STAGE_BYTES;
+#pragma unroll 1
+            for (int t = 0; t < 27; ++t) {
+                const int w = t / 3, dx1 = t % 3;   // window (dy, dz) and dx + 1
+#pragma unroll
+                for (int ks = 0; ks < CI / 16; ++ks) {
+                    const uint64_t ad =
+                        smem_desc(st + (w * (CI / 8) + 2 * ks) * BOX_BYTES + dx1 * 16, BOX_BYTES, 128);
+                    const uint64_t bd = smem_desc(wbase + t * COP * CI * 2 + ks * 256, 128, CI * 16);
+                    const uint32_t acc = (t > 0 || ks > 0) ? 1u : 0u;
+                    asm volatile(
+                        "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+                        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(tmem),
+                        "l"(ad), "l"(bd), "r"(idesc), "r"(acc));
+                }
+            }
+            asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(mdone)
+                         : "memory");
+        }
+        ++commits;
+        ok = mbar_wait(mdone, uint32_t(i & 1));
+        if (__syncthreads_or(!ok)) {
+            failed = true;
+            break;
+        }
+        ++commits_waited;
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        int x0;
+        const long long p0 = tile_origin(tile, x0);
+        const bool valid = x0 + tid < d.nx;
+        const long long p = p0 + tid;
+        const uint32_t trow = tmem + ((uint32_t)(warp * 32) << 16);
+        if (OUTF32) {
+            float v[16];
+            tmem_ld16(trow, v);
+            if (valid) Yf[p] = v[0] + bias_r[0];
+        } else {
+#pragma unroll
+            for (int c0 = 0; c0 < CO; c0 += 16) {
+                float v[16];
+                tmem_ld16(trow + c0, v);
+                if (valid) {
+                    uint32_t packed[8];
+#pragma unroll
+                    for (int k = 0; k < 16; k += 2) {
+                        float a = v[k] + bias_r[c0 + k], b2 = v[k + 1] + bias_r[c0 + k + 1];
+                        if (RELU) {
+                            a = fmaxf(a, 0.f);
+                            b2 = fmaxf(b2, 0.f);
+                        }
+                        if (skip) {
+                            const __nv_bfloat162 sk = reinterpret_cast<const __nv_bfloat162*>(skip + p * CO + c0)[k / 2];
+                            a += __low2float(sk);
+                            b2 += __high2float(sk);
+                        }
+                        const __nv_bfloat162 o2 = __floats2bfloat162_rn(a, b2);
+                        packed[k / 2] = *reinterpret_cast<const uint32_t*>(&o2);
+                    }
+                    uint4* dst = reinterpret_cast<uint4*>(Y + p * CO + c0);
+                    dst[0] = make_uint4(packed[0], packed[1], packed[2], packed[3]);
+                    dst[1] = make_uint4(packed[4], packed[5], packed[6], packed[7]);
+                }
+            }
+        }
+        asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+        __syncthreads();
+    }
+    if (failed) {
+        if (tid == 0) atomicExch(err, 1);
+        // bounded drain: the last commit and every box load still in flight
+        if (commits > commits_waited) mbar_wait(mdone, uint32_t((commits - 1) & 1));
+        for (int s = 0; s < 2; ++s)
+            if (issued[s] > waited[s]) mbar_wait(full0 + 8 * s, uint32_t((issued[s] - 1) & 1));
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(32));
+}
+
 // ------------------------------------------------------------------ BF16 glue kernels (inference)
 __global__ void pool_bf16(Dims dc, int C, const __nv_bfloat16* __restrict__ in, __nv_bfloat16* __restrict__ out) {
     const Dims df{dc.B, 2 * dc.nx, 2 * dc.ny, 2 * dc.nz};
@@ -604,6 +796,7 @@ struct NNState {
     uint8_t* wtc[nn::NLAYER] = {nullptr};                            // BF16 weights, shared-memory layout
     float* bias_tc = nullptr;                                        // padded biases (16 or 32 per layer)
     bool tc_dirty = true;
+    bool use_tma = true;                                             // TMA-fed conv kernel (else load ring)
     // training activations (FP32); zeroed whenever the dims change so every halo is zero
     float* buf = nullptr;
     size_t buf_bytes = 0;
@@ -851,6 +1044,59 @@ cudaError_t launch_tc(const nn::Dims& d, const __nv_bfloat16* X, const uint8_t* 
     return cudaGetLastError();
 }
 
+// cuTensorMapEncodeTiled from the driver, without linking libcuda
+using EncodeTiled = CUresult (*)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                 const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                 CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+EncodeTiled encode_tiled() {
+    static EncodeTiled fn = nullptr;
+    static bool tried = false;
+    if (!tried) {
+        tried = true;
+        void* p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess && q == cudaDriverEntryPointSuccess)
+            fn = reinterpret_cast<EncodeTiled>(p);
+    }
+    return fn;
+}
+
+// tensor map of a channels-last BF16 activation: rows = padded cells, Cin channels per row,
+// box = 8 channels x WR rows; loads past either end read zeros
+bool make_act_map(CUtensorMap* m, const __nv_bfloat16* X, int CI, long long rows) {
+    EncodeTiled enc = encode_tiled();
+    if (!enc) return false;
+    const cuuint64_t dims[2] = {(cuuint64_t)CI, (cuuint64_t)rows};
+    const cuuint64_t strides[1] = {(cuuint64_t)CI * 2};
+    const cuuint32_t box[2] = {8, (cuuint32_t)nn::WR};
+    const cuuint32_t estr[2] = {1, 1};
+    return enc(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<__nv_bfloat16*>(X), dims, strides, box, estr,
+               CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+               CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+template <int CI, int CO, bool RELU, bool OUTF32>
+cudaError_t launch_tma(const nn::Dims& d, const __nv_bfloat16* X, const uint8_t* W, const float* b,
+                       const __nv_bfloat16* skip, __nv_bfloat16* Y, float* Yf, int* err, cudaStream_t st, int sms) {
+    using Sm = nn::TmaSmem<CI, CO < 16 ? 16 : CO>;
+    CUtensorMap map;
+    if (!make_act_map(&map, X, CI, d.padded())) return cudaErrorNotSupported;
+    auto kfn = nn::conv_tma_kernel<CI, CO, RELU, OUTF32>;
+    cudaError_t e = cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, Sm::TOTAL);
+    if (e != cudaSuccess) return e;
+    const long long tiles = (long long)((d.nx + nn::kM - 1) / nn::kM) * d.ny * d.nz * d.B;
+    const int per_sm = Sm::TOTAL <= 110 * 1024 ? 2 : 1;
+    const int grid = int(tiles < (long long)per_sm * sms ? tiles : (long long)per_sm * sms);
+    { kfn<<<grid, 128, Sm::TOTAL, st>>>(map, d, W, b, skip, Y, Yf, err); ia::note_launch(); }
+    return cudaGetLastError();
+}
+
+// one layer: the TMA-fed kernel, or the load-ring kernel where no tensor-map encoder is available
+#define conv_layer(CI_, CO_, RELU_, F32_, dims, X_, W_, B_, SK_, Y_, YF_)                                  \
+    (tma ? launch_tma<CI_, CO_, RELU_, F32_>(dims, X_, W_, B_, SK_, Y_, YF_, s->derr, st, sms)               \
+         : launch_tc<CI_, CO_, RELU_, F32_>(dims, X_, W_, B_, SK_, Y_, YF_, s->derr, st, sms))
+
 // inference with the tensor-core kernels; x16 = BF16 16-channel input, out = FP32 channel
 int forward_tc(ia_handle* h, NNState* s, const nn::Dims& f, const __nv_bfloat16* x16, float* out) {
     cudaStream_t st = h->stream;
@@ -878,16 +1124,17 @@ int forward_tc(ia_handle* h, NNState* s, const nn::Dims& f, const __nv_bfloat16*
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, h->device);
     const float* b = s->bias_tc;
     cudaError_t e = cudaSuccess;
-    e = e ? e : launch_tc<16, 16, true, false>(f, x16, s->wtc[0], b + 0, nullptr, a1, nullptr, s->derr, st, sms);
+    const bool tma = s->use_tma && encode_tiled() != nullptr;
+    e = e ? e : conv_layer(16, 16, true, false, f, x16, s->wtc[0], b + 0, nullptr, a1, nullptr);
     if (!e) { nn::pool_bf16<<<nblk(hf.cells()), 256, 0, st>>>(hf, 16, a1, p1); ia::note_launch(); }
-    e = e ? e : launch_tc<16, 32, true, false>(hf, p1, s->wtc[1], b + 32, nullptr, a2, nullptr, s->derr, st, sms);
+    e = e ? e : conv_layer(16, 32, true, false, hf, p1, s->wtc[1], b + 32, nullptr, a2, nullptr);
     if (!e) { nn::pool_bf16<<<nblk(qt.cells()), 256, 0, st>>>(qt, 32, a2, p2); ia::note_launch(); }
-    e = e ? e : launch_tc<32, 32, true, false>(qt, p2, s->wtc[2], b + 64, nullptr, a3, nullptr, s->derr, st, sms);
+    e = e ? e : conv_layer(32, 32, true, false, qt, p2, s->wtc[2], b + 64, nullptr, a3, nullptr);
     if (!e) { nn::up_bf16<<<nblk(hf.cells()), 256, 0, st>>>(hf, 32, a3, a2, u2); ia::note_launch(); }
-    e = e ? e : launch_tc<32, 32, true, false>(hf, u2, s->wtc[3], b + 96, nullptr, a4, nullptr, s->derr, st, sms);
+    e = e ? e : conv_layer(32, 32, true, false, hf, u2, s->wtc[3], b + 96, nullptr, a4, nullptr);
     if (!e) { nn::up_bf16<<<nblk(f.cells()), 256, 0, st>>>(f, 32, a4, nullptr, u1); ia::note_launch(); }
-    e = e ? e : launch_tc<32, 16, true, false>(f, u1, s->wtc[4], b + 128, a1, a5, nullptr, s->derr, st, sms);
-    e = e ? e : launch_tc<16, 1, false, true>(f, a5, s->wtc[5], b + 160, nullptr, nullptr, out, s->derr, st, sms);
+    e = e ? e : conv_layer(32, 16, true, false, f, u1, s->wtc[4], b + 128, a1, a5, nullptr);
+    e = e ? e : conv_layer(16, 1, false, true, f, a5, s->wtc[5], b + 160, nullptr, nullptr, out);
     return e == cudaSuccess ? IA_OK : IA_ERR_CUDA;
 }
 
@@ -993,7 +1240,10 @@ int ia_nn_forward(ia_handle* h, const float* x0, float* out, int32_t B, int32_t 
     cudaMemsetAsync(x16, 0, 2 * 16 * (size_t)f.padded(), st);
     { nn::in_to_bf16<<<nblk(f.cells()), 256, 0, st>>>(f, x0, x16); ia::note_launch(); }
     cudaMemsetAsync(s->derr, 0, 4, st);
+    const bool keep = s->use_tma;
+    s->use_tma = tensor_cores != 2;
     int rc = forward_tc(h, s, f, x16, out);
+    s->use_tma = keep;
     cudaError_t e = cudaStreamSynchronize(st);
     cudaFree(x16);
     if (rc != IA_OK || e != cudaSuccess) return IA_ERR_CUDA;
