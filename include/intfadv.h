@@ -261,9 +261,8 @@ int64_t ia_nn_param_count(void);
 /* copy host parameters into / out of the handle's net (set resets the Adam moments) */
 int ia_nn_set_params(ia_handle* h, const float* params);
 int ia_nn_get_params(ia_handle* h, float* params);
-/* forward pass on the handle's stream: tensor_cores = 0 FP32 training kernels, 1 BF16 tcgen05
- * inference kernels fed by TMA row windows (the solver's path), 2 the same MMAs fed by a
- * per-tap load ring (the path used where no tensor-map encoder is available) */
+/* forward pass on the handle's stream: tensor_cores = 0 FP32 training kernels, 1 the BF16
+ * tcgen05 inference kernels fed by TMA row windows (the solver's path) */
 int ia_nn_forward(ia_handle* h, const float* x0, float* out, int32_t B, int32_t nx, int32_t ny, int32_t nz,
                   int32_t tensor_cores);
 /* training loss (mean over interior cells) and its gradient (device, NULL = keep in the handle) */

@@ -357,177 +357,18 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16]) {
     for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
 }
 
-constexpr int kStages = 4;
-constexpr int kM = 128;
-
-template <int CI, int CO>
-struct ConvSmem {
-    static constexpr int W_BYTES = 27 * CO * CI * 2;
-    static constexpr int A_BYTES = kM * CI * 2;
-    static constexpr int W_OFF = 0;
-    static constexpr int A_OFF = (W_BYTES + 1023) / 1024 * 1024;
-    static constexpr int BAR_OFF = A_OFF + kStages * A_BYTES;
-    static constexpr int TOTAL = BAR_OFF + 8 * kStages + 16;
-};
-
-// Y = act(conv(X) + bias) (+ skip); X, Y, skip BF16 channels-last with halo; Wg = weights already in
-// the shared-memory layout (27 taps x [COP x CI] core-matrix tiles, COP = Cout padded to 16);
-// OUTF32: write channel 0 as FP32 instead (the last layer).
-//
-// One CTA = 4 warps = 128 rows of the M = 128 tile: thread t stages output cell t's input
-// channels for each tap and later reads accumulator lane t.  Stage s of the A ring is
-// released by the tcgen05.commit of its previous use (mbarrier s); every wait is bounded
-// and its outcome is agreed block-wide, so a timeout ends the kernel cleanly (error flag,
-// drain, TMEM released) instead of hanging.
-template <int CI, int CO, bool RELU, bool OUTF32>
-__global__ void __launch_bounds__(128) conv_tc_kernel(Dims d, const __nv_bfloat16* __restrict__ X,
-                                                      const uint8_t* __restrict__ Wg, const float* __restrict__ bias,
-                                                      const __nv_bfloat16* __restrict__ skip,
-                                                      __nv_bfloat16* __restrict__ Y, float* __restrict__ Yf,
-                                                      int* __restrict__ err) {
-    constexpr int COP = CO < 16 ? 16 : CO;
-    using S = ConvSmem<CI, COP>;
-    static_assert(CI % 16 == 0 && COP % 16 == 0 && COP <= 32, "tile shape");
-    extern __shared__ __align__(1024) uint8_t smem[];
-    __shared__ uint32_t tmem_holder;
-    const int tid = threadIdx.x, warp = tid >> 5;
-    for (int i = tid; i < S::W_BYTES / 16; i += blockDim.x)
-        reinterpret_cast<uint4*>(smem + S::W_OFF)[i] = __ldg(reinterpret_cast<const uint4*>(Wg) + i);
-    const uint32_t bar0 = smem_u32(smem + S::BAR_OFF);
-    if (tid == 0) {
-        for (int s = 0; s < kStages; ++s) asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar0 + 8 * s));
-        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-    }
-    if (warp == 0) {
-        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmem_holder)),
-                     "r"(32));
-        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
-    }
-    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
-    __syncthreads();
-    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-    const uint32_t tmem = tmem_holder;
-    constexpr uint32_t SBO = CI * 16;   // byte distance of 8-row groups (a row holds CI bf16 = CI/8 core matrices)
-    constexpr uint32_t idesc = idesc_bf16(kM, COP);
-    const uint32_t wbase = smem_u32(smem + S::W_OFF);
-    const uint32_t abase = smem_u32(smem + S::A_OFF);
-    const long long total = d.cells();
-    const long long ntiles = (total + kM - 1) / kM;
-    long long use = 0;   // stage uses issued so far (all tiles)
-    bool failed = false;
-    float bias_r[CO];
-#pragma unroll
-    for (int o = 0; o < CO; ++o) bias_r[o] = __ldg(bias + o);
-
-    for (long long tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
-        const long long cell = tile * kM + tid;
-        const bool valid = cell < total;
-        long long p = 0;
-        if (valid) {
-            int b, x, y, z;
-            d.decode(cell, b, x, y, z);
-            p = d.pos(b, x, y, z);
-        }
-        for (int t = 0; t < 27; ++t, ++use) {
-            const int s = int(use % kStages);
-            bool ok = true;
-            if (use >= kStages) ok = mbar_wait(bar0 + 8 * s, uint32_t(((use / kStages) - 1) & 1));
-            uint8_t* As = smem + S::A_OFF + s * S::A_BYTES;
-            const uint4* src = reinterpret_cast<const uint4*>(X + (p + d.tap(t)) * CI);
-            if (ok) {
-#pragma unroll
-                for (int j = 0; j < CI / 8; ++j) {
-                    const uint4 v = valid ? __ldg(src + j) : make_uint4(0, 0, 0, 0);
-                    *reinterpret_cast<uint4*>(As + (tid >> 3) * SBO + j * 128 + (tid & 7) * 16) = v;
-                }
-            }
-            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-            if (__syncthreads_or(!ok)) {
-                failed = true;
-                break;
-            }
-            if (tid == 0) {
-                asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-#pragma unroll
-                for (int ks = 0; ks < CI / 16; ++ks) {
-                    const uint64_t ad = smem_desc(abase + s * S::A_BYTES + ks * 256, 128, SBO);
-                    const uint64_t bd = smem_desc(wbase + t * COP * CI * 2 + ks * 256, 128, SBO);
-                    const uint32_t acc = (t > 0 || ks > 0) ? 1u : 0u;
-                    asm volatile(
-                        "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
-                        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(tmem),
-                        "l"(ad), "l"(bd), "r"(idesc), "r"(acc));
-                }
-                asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
-                                 bar0 + 8 * s)
-                             : "memory");
-            }
-        }
-        if (failed) break;
-        // the last commit tracks every MMA issued before it
-        const long long last = use - 1;
-        const bool ok = mbar_wait(bar0 + 8 * int(last % kStages), uint32_t((last / kStages) & 1));
-        if (__syncthreads_or(!ok)) {
-            failed = true;
-            break;
-        }
-        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-        const uint32_t trow = tmem + ((uint32_t)(warp * 32) << 16);
-        if (OUTF32) {
-            float v[16];
-            tmem_ld16(trow, v);
-            if (valid) Yf[p] = v[0] + bias_r[0];
-        } else {
-#pragma unroll
-            for (int c0 = 0; c0 < CO; c0 += 16) {
-                float v[16];
-                tmem_ld16(trow + c0, v);
-                if (valid) {
-                    uint32_t packed[8];
-#pragma unroll
-                    for (int i = 0; i < 16; i += 2) {
-                        float a = v[i] + bias_r[c0 + i], b2 = v[i + 1] + bias_r[c0 + i + 1];
-                        if (RELU) {
-                            a = fmaxf(a, 0.f);
-                            b2 = fmaxf(b2, 0.f);
-                        }
-                        if (skip) {
-                            const __nv_bfloat162 sk = reinterpret_cast<const __nv_bfloat162*>(skip + p * CO + c0)[i / 2];
-                            a += __low2float(sk);
-                            b2 += __high2float(sk);
-                        }
-                        const __nv_bfloat162 o2 = __floats2bfloat162_rn(a, b2);
-                        packed[i / 2] = *reinterpret_cast<const uint32_t*>(&o2);
-                    }
-                    uint4* dst = reinterpret_cast<uint4*>(Y + p * CO + c0);
-                    dst[0] = make_uint4(packed[0], packed[1], packed[2], packed[3]);
-                    dst[1] = make_uint4(packed[4], packed[5], packed[6], packed[7]);
-                }
-            }
-        }
-        asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
-        __syncthreads();
-    }
-    if (failed) {
-        if (tid == 0) atomicExch(err, 1);
-        // bounded drain of the MMAs in flight before their accumulator columns are released
-        const long long last = use - 1;
-        if (last >= 0) mbar_wait(bar0 + 8 * int(last % kStages), uint32_t((last / kStages) & 1));
-    }
-    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
-    __syncthreads();
-    if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(32));
-}
-
 // ------------------------------------------------------------------ TMA-fed tensor-core convolution
+// Inference activations are stored as 8-channel planes: plane j holds channels 8j..8j+7 of every
+// (padded, halo-included) cell, 16 B per cell, so a run of cells of one plane is contiguous.
 // A tile is M = 128 consecutive cells of one x-row (rows shorter than 128 leave the tail masked).
-// For each of the 9 (dy, dz) neighbour rows, one TMA box of WR = 136 consecutive cells x 8
-// channels per 8-channel chunk lands in shared memory as 136 rows of 16 B: the chunk column of a
+// For each of the 9 (dy, dz) neighbour rows and each plane, one TMA box of WR = 136 consecutive
+// cells (2176 contiguous bytes) lands in shared memory as 136 rows of 16 B: the chunk column of a
 // K-major no-swizzle operand whose 8-row core matrices are contiguous (SBO 128 B) and whose
 // K-neighbour chunks are one box apart (LBO = 2176 B).  The A operand of tap (dx, dy, dz) is the
 // (dy, dz) window started dx + 1 rows in, so all 27 taps are read from one set of 9·Cin/8 boxes.
 // Two stages: thread 0 issues the next tile's boxes before the MMAs of this one; one commit per
 // tile releases the epilogue (all four warps, tcgen05.ld) and the stage.
+constexpr int kM = 128;   // output cells per tile (the MMA M)
 constexpr int WR = 136;
 constexpr int BOX_BYTES = WR * 16;
 
@@ -585,6 +426,7 @@ __global__ void __launch_bounds__(128) conv_tma_kernel(const __grid_constant__ C
     const long long ntiles = (long long)xtiles * d.ny * d.nz * d.B;
     const int rowp = d.nx + 2;
     const long long planep = (long long)(d.nx + 2) * (d.ny + 2);
+    const long long plane = d.padded() * 8;   // elements per 8-channel plane
     float bias_r[CO];
 #pragma unroll
     for (int o = 0; o < CO; ++o) bias_r[o] = __ldg(bias + o);
@@ -608,7 +450,8 @@ __global__ void __launch_bounds__(128) conv_tma_kernel(const __grid_constant__ C
             const long long row = p0 - 1 + (long long)(w % 3 - 1) * rowp + (long long)(w / 3 - 1) * planep;
 #pragma unroll
             for (int j = 0; j < CI / 8; ++j)
-                tma_load_2d(abase + s * S::STAGE_BYTES + (w * (CI / 8) + j) * BOX_BYTES, &tmap, 8 * j, int(row), bar);
+                tma_load_2d(abase + s * S::STAGE_BYTES + (w * (CI / 8) + j) * BOX_BYTES, &tmap, 0,
+                            int(row + (long long)j * d.padded()), bar);
         }
     };
     int issued[2] = {0, 0}, waited[2] = {0, 0}, commits = 0, commits_waited = 0;
@@ -682,16 +525,18 @@ __global__ void __launch_bounds__(128) conv_tma_kernel(const __grid_constant__ C
                             b2 = fmaxf(b2, 0.f);
                         }
                         if (skip) {
-                            const __nv_bfloat162 sk = reinterpret_cast<const __nv_bfloat162*>(skip + p * CO + c0)[k / 2];
+                            const long long sp = (long long)((c0 + k) / 8) * plane + p * 8 + (k % 8);
+                            const __nv_bfloat162 sk = *reinterpret_cast<const __nv_bfloat162*>(skip + sp);
                             a += __low2float(sk);
                             b2 += __high2float(sk);
                         }
                         const __nv_bfloat162 o2 = __floats2bfloat162_rn(a, b2);
                         packed[k / 2] = *reinterpret_cast<const uint32_t*>(&o2);
                     }
-                    uint4* dst = reinterpret_cast<uint4*>(Y + p * CO + c0);
-                    dst[0] = make_uint4(packed[0], packed[1], packed[2], packed[3]);
-                    dst[1] = make_uint4(packed[4], packed[5], packed[6], packed[7]);
+                    *reinterpret_cast<uint4*>(Y + (long long)(c0 / 8) * plane + p * 8) =
+                        make_uint4(packed[0], packed[1], packed[2], packed[3]);
+                    *reinterpret_cast<uint4*>(Y + (long long)(c0 / 8 + 1) * plane + p * 8) =
+                        make_uint4(packed[4], packed[5], packed[6], packed[7]);
                 }
             }
         }
@@ -711,40 +556,74 @@ __global__ void __launch_bounds__(128) conv_tma_kernel(const __grid_constant__ C
 }
 
 // ------------------------------------------------------------------ BF16 glue kernels (inference)
+// 8-channel planes: element (cell p, channel c) at (c/8)·8·padded + 8p + c%8; 16 B per cell and plane
+__device__ __forceinline__ void acc8(float (&a)[8], const uint4& v) {
+    const __nv_bfloat162* h = reinterpret_cast<const __nv_bfloat162*>(&v);
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+        a[2 * i] += __low2float(h[i]);
+        a[2 * i + 1] += __high2float(h[i]);
+    }
+}
+__device__ __forceinline__ uint4 pack8(const float (&a)[8]) {
+    uint4 v;
+    __nv_bfloat162* h = reinterpret_cast<__nv_bfloat162*>(&v);
+#pragma unroll
+    for (int i = 0; i < 4; ++i) h[i] = __floats2bfloat162_rn(a[2 * i], a[2 * i + 1]);
+    return v;
+}
+
+// out (coarse dims dc) = mean of the 8 children of in (fine dims 2dc), C/8 planes
 __global__ void pool_bf16(Dims dc, int C, const __nv_bfloat16* __restrict__ in, __nv_bfloat16* __restrict__ out) {
     const Dims df{dc.B, 2 * dc.nx, 2 * dc.ny, 2 * dc.nz};
+    const long long pin = df.padded() * 8, pout = dc.padded() * 8;
     FOR_CELLS(dc) {
         int b, x, y, z;
         dc.decode(q, b, x, y, z);
-        const long long P = dc.pos(b, x, y, z) * C;
-        for (int c = 0; c < C; ++c) {
-            float s = 0.f;
-            for (int k = 0; k < 8; ++k) s += __bfloat162float(in[child_pos(df, b, x, y, z, k) * C + c]);
-            out[P + c] = __float2bfloat16_rn(s * 0.125f);
+        const long long P = dc.pos(b, x, y, z);
+        for (int j = 0; j < C / 8; ++j) {
+            float a[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+            for (int k = 0; k < 8; ++k)
+                acc8(a, *reinterpret_cast<const uint4*>(in + j * pin + child_pos(df, b, x, y, z, k) * 8));
+#pragma unroll
+            for (int i = 0; i < 8; ++i) a[i] *= 0.125f;
+            *reinterpret_cast<uint4*>(out + j * pout + P * 8) = pack8(a);
         }
     }
 }
+// out[child] = in[parent] (+ skip[child])  (fine dims df), C/8 planes
 __global__ void up_bf16(Dims df, int C, const __nv_bfloat16* __restrict__ in, const __nv_bfloat16* __restrict__ skip,
                         __nv_bfloat16* __restrict__ out) {
     const Dims dc = df.half();
+    const long long pf = df.padded() * 8, pc = dc.padded() * 8;
     FOR_CELLS(df) {
         int b, x, y, z;
         df.decode(q, b, x, y, z);
-        const long long p = df.pos(b, x, y, z) * C, P = dc.pos(b, x / 2, y / 2, z / 2) * C;
-        for (int c = 0; c < C; ++c) {
-            float v = __bfloat162float(in[P + c]);
-            if (skip) v += __bfloat162float(skip[p + c]);
-            out[p + c] = __float2bfloat16_rn(v);
+        const long long p = df.pos(b, x, y, z), P = dc.pos(b, x / 2, y / 2, z / 2);
+        for (int j = 0; j < C / 8; ++j) {
+            const uint4 v = *reinterpret_cast<const uint4*>(in + j * pc + P * 8);
+            if (skip) {
+                float a[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+                acc8(a, v);
+                acc8(a, *reinterpret_cast<const uint4*>(skip + j * pf + p * 8));
+                *reinterpret_cast<uint4*>(out + j * pf + p * 8) = pack8(a);
+            } else {
+                *reinterpret_cast<uint4*>(out + j * pf + p * 8) = v;
+            }
         }
     }
 }
-// FP32 4-channel input (training layout) -> BF16 16-channel (channels 4..15 zero)
+// FP32 4-channel input (training layout) -> BF16 planes 0 (channels 0-3, 4-7 zero) and 1 (zero)
 __global__ void in_to_bf16(Dims d, const float* __restrict__ x4, __nv_bfloat16* __restrict__ x16) {
+    const long long pl = d.padded() * 8;
     FOR_CELLS(d) {
         int b, x, y, z;
         d.decode(q, b, x, y, z);
         const long long p = d.pos(b, x, y, z);
-        for (int c = 0; c < 16; ++c) x16[p * 16 + c] = __float2bfloat16_rn(c < 4 ? x4[p * 4 + c] : 0.f);
+        const float4 v = *reinterpret_cast<const float4*>(x4 + p * 4);
+        const float a[8] = {v.x, v.y, v.z, v.w, 0.f, 0.f, 0.f, 0.f};
+        *reinterpret_cast<uint4*>(x16 + p * 8) = pack8(a);
+        *reinterpret_cast<uint4*>(x16 + pl + p * 8) = make_uint4(0u, 0u, 0u, 0u);
     }
 }
 
@@ -769,7 +648,8 @@ __global__ void absmax_k(Dims d, const float* __restrict__ r, unsigned int* __re
     if (threadIdx.x == 0) atomicMax(out, sm[0]);
 }
 
-// channels: r / max|r|, λρ·L_x, λρ·L_y, λρ·L_z (lower-face coefficients of the cell), zeros
+// channels: r / max|r|, λρ·L_x, λρ·L_y, λρ·L_z (lower-face coefficients of the cell), zeros;
+// written as 8-channel planes
 __global__ void prep_k(Dims d, const float* __restrict__ r, const float* __restrict__ L, long long ncomp, float lrho,
                        const unsigned int* __restrict__ scale, __nv_bfloat16* __restrict__ x16) {
     const float sc = __uint_as_float(*scale);
@@ -780,9 +660,9 @@ __global__ void prep_k(Dims d, const float* __restrict__ r, const float* __restr
         const long long p = d.pos(b, x, y, z);
         const __nv_bfloat162 c01 = __floats2bfloat162_rn(r[p] * inv, lrho * L[p]);
         const __nv_bfloat162 c23 = __floats2bfloat162_rn(lrho * L[p + ncomp], lrho * L[p + 2 * ncomp]);
-        uint4* dst = reinterpret_cast<uint4*>(x16 + p * 16);
-        dst[0] = make_uint4(*reinterpret_cast<const uint32_t*>(&c01), *reinterpret_cast<const uint32_t*>(&c23), 0u, 0u);
-        dst[1] = make_uint4(0u, 0u, 0u, 0u);
+        // plane 0; plane 1 (channels 8-15) stays zero from the allocation
+        *reinterpret_cast<uint4*>(x16 + p * 8) =
+            make_uint4(*reinterpret_cast<const uint32_t*>(&c01), *reinterpret_cast<const uint32_t*>(&c23), 0u, 0u);
     }
 }
 
@@ -796,7 +676,6 @@ struct NNState {
     uint8_t* wtc[nn::NLAYER] = {nullptr};                            // BF16 weights, shared-memory layout
     float* bias_tc = nullptr;                                        // padded biases (16 or 32 per layer)
     bool tc_dirty = true;
-    bool use_tma = true;                                             // TMA-fed conv kernel (else load ring)
     // training activations (FP32); zeroed whenever the dims change so every halo is zero
     float* buf = nullptr;
     size_t buf_bytes = 0;
@@ -1031,19 +910,6 @@ int build_tc_weights(ia_handle* h, NNState* s) {
     return IA_OK;
 }
 
-template <int CI, int CO, bool RELU, bool OUTF32>
-cudaError_t launch_tc(const nn::Dims& d, const __nv_bfloat16* X, const uint8_t* W, const float* b,
-                      const __nv_bfloat16* skip, __nv_bfloat16* Y, float* Yf, int* err, cudaStream_t st, int sms) {
-    using Sm = nn::ConvSmem<CI, CO < 16 ? 16 : CO>;
-    auto kfn = nn::conv_tc_kernel<CI, CO, RELU, OUTF32>;
-    cudaError_t e = cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, Sm::TOTAL);
-    if (e != cudaSuccess) return e;
-    const long long tiles = (d.cells() + nn::kM - 1) / nn::kM;
-    const int grid = int(tiles < 2LL * sms ? tiles : 2LL * sms);
-    { kfn<<<grid, 128, Sm::TOTAL, st>>>(d, X, W, b, skip, Y, Yf, err); ia::note_launch(); }
-    return cudaGetLastError();
-}
-
 // cuTensorMapEncodeTiled from the driver, without linking libcuda
 using EncodeTiled = CUresult (*)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
                                  const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
@@ -1062,13 +928,13 @@ EncodeTiled encode_tiled() {
     return fn;
 }
 
-// tensor map of a channels-last BF16 activation: rows = padded cells, Cin channels per row,
-// box = 8 channels x WR rows; loads past either end read zeros
+// tensor map of a BF16 activation stored as Cin/8 planes of 8 channels: a 2D view of
+// (Cin/8)·rows cells x 8 channels, box = 8 channels x WR cells; loads past either end read zeros
 bool make_act_map(CUtensorMap* m, const __nv_bfloat16* X, int CI, long long rows) {
     EncodeTiled enc = encode_tiled();
     if (!enc) return false;
-    const cuuint64_t dims[2] = {(cuuint64_t)CI, (cuuint64_t)rows};
-    const cuuint64_t strides[1] = {(cuuint64_t)CI * 2};
+    const cuuint64_t dims[2] = {8, (cuuint64_t)rows * (CI / 8)};
+    const cuuint64_t strides[1] = {16};
     const cuuint32_t box[2] = {8, (cuuint32_t)nn::WR};
     const cuuint32_t estr[2] = {1, 1};
     return enc(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<__nv_bfloat16*>(X), dims, strides, box, estr,
@@ -1092,10 +958,9 @@ cudaError_t launch_tma(const nn::Dims& d, const __nv_bfloat16* X, const uint8_t*
     return cudaGetLastError();
 }
 
-// one layer: the TMA-fed kernel, or the load-ring kernel where no tensor-map encoder is available
-#define conv_layer(CI_, CO_, RELU_, F32_, dims, X_, W_, B_, SK_, Y_, YF_)                                  \
-    (tma ? launch_tma<CI_, CO_, RELU_, F32_>(dims, X_, W_, B_, SK_, Y_, YF_, s->derr, st, sms)               \
-         : launch_tc<CI_, CO_, RELU_, F32_>(dims, X_, W_, B_, SK_, Y_, YF_, s->derr, st, sms))
+// one convolution layer of the inference path
+#define conv_layer(CI_, CO_, RELU_, F32_, dims, X_, W_, B_, SK_, Y_, YF_) \
+    launch_tma<CI_, CO_, RELU_, F32_>(dims, X_, W_, B_, SK_, Y_, YF_, s->derr, st, sms)
 
 // inference with the tensor-core kernels; x16 = BF16 16-channel input, out = FP32 channel
 int forward_tc(ia_handle* h, NNState* s, const nn::Dims& f, const __nv_bfloat16* x16, float* out) {
@@ -1124,7 +989,6 @@ int forward_tc(ia_handle* h, NNState* s, const nn::Dims& f, const __nv_bfloat16*
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, h->device);
     const float* b = s->bias_tc;
     cudaError_t e = cudaSuccess;
-    const bool tma = s->use_tma && encode_tiled() != nullptr;
     e = e ? e : conv_layer(16, 16, true, false, f, x16, s->wtc[0], b + 0, nullptr, a1, nullptr);
     if (!e) { nn::pool_bf16<<<nblk(hf.cells()), 256, 0, st>>>(hf, 16, a1, p1); ia::note_launch(); }
     e = e ? e : conv_layer(16, 32, true, false, hf, p1, s->wtc[1], b + 32, nullptr, a2, nullptr);
@@ -1240,10 +1104,7 @@ int ia_nn_forward(ia_handle* h, const float* x0, float* out, int32_t B, int32_t 
     cudaMemsetAsync(x16, 0, 2 * 16 * (size_t)f.padded(), st);
     { nn::in_to_bf16<<<nblk(f.cells()), 256, 0, st>>>(f, x0, x16); ia::note_launch(); }
     cudaMemsetAsync(s->derr, 0, 4, st);
-    const bool keep = s->use_tma;
-    s->use_tma = tensor_cores != 2;
     int rc = forward_tc(h, s, f, x16, out);
-    s->use_tma = keep;
     cudaError_t e = cudaStreamSynchronize(st);
     cudaFree(x16);
     if (rc != IA_OK || e != cudaSuccess) return IA_ERR_CUDA;

@@ -107,12 +107,11 @@ class Net:
         assert c == 4 and x0.dtype == torch.float32
         return B, nxp - 2, nyp - 2, nzp - 2
 
-    def forward(self, x0: torch.Tensor, tensor_cores=False) -> torch.Tensor:
-        """FP32 training kernels, or (tensor_cores True / "tma") the BF16 tcgen05 kernels fed by
-        TMA, or ("ring") the same MMAs fed by the per-tap load ring."""
+    def forward(self, x0: torch.Tensor, tensor_cores: bool = False) -> torch.Tensor:
+        """FP32 training kernels, or the BF16 tcgen05 inference kernels (the solver's path)."""
         B, nx, ny, nz = self._dims(x0)
         out = torch.zeros(x0.shape[:-1], dtype=torch.float32, device=x0.device)
-        mode = {False: 0, True: 1, "tma": 1, "ring": 2}[tensor_cores]
+        mode = 1 if tensor_cores else 0
         _lib.check(self.handle.call("ia_nn_forward", _dev_ptr(x0), _dev_ptr(out), B, nx, ny, nz, mode),
                    "ia_nn_forward")
         return out

@@ -117,16 +117,15 @@ def test_training_reduces_loss(net):
     assert last < 0.5 * first, (first, last)
 
 
-@pytest.mark.parametrize("kernel", ["tma", "ring"])
 @pytest.mark.parametrize("dims", [(1, 12, 12, 12), (2, 16, 8, 8), (1, 8, 20, 12), (1, 136, 8, 4)])
-def test_tensor_core_forward_matches_oracle(net, dims, kernel):
+def test_tensor_core_forward_matches_oracle(net, dims):
     # (1, 136, 8, 4): rows longer than one 128-cell tile (a full tile plus a masked 8-cell tail)
     B, nx, ny, nz = dims
     w = params(10)
     net.set_params(w)
     x0, _, gx, _ = rand_case(B, nx, ny, nz, seed=12)
     ref = O.nn_forward(w.astype(np.float64), x0.astype(np.float64))
-    out = net.forward(gx, tensor_cores=kernel).cpu().numpy()
+    out = net.forward(gx, tensor_cores=True).cpu().numpy()
     assert np.isfinite(out).all()
     assert np.all(out[:, 0] == 0) and np.all(out[:, :, 0] == 0)
     d = out - ref
@@ -135,15 +134,14 @@ def test_tensor_core_forward_matches_oracle(net, dims, kernel):
     assert rel2 < 2e-2 and relmax < 6e-2, (rel2, relmax)
 
 
-@pytest.mark.parametrize("kernel", ["tma", "ring"])
-def test_tensor_core_forward_many_tiles(net, kernel):
+def test_tensor_core_forward_many_tiles(net):
     # 64³ and 256 x 32 x 16: thousands of tiles over the persistent CTAs (stages reused across tiles)
     w = params(11)
     net.set_params(w)
     for dims in ((1, 64, 64, 64), (1, 256, 32, 16)):
         _, _, gx, _ = rand_case(*dims, seed=13)
         ref = net.forward(gx).cpu().numpy()
-        out = net.forward(gx, tensor_cores=kernel).cpu().numpy()
+        out = net.forward(gx, tensor_cores=True).cpu().numpy()
         rel2 = np.linalg.norm(out - ref) / np.linalg.norm(ref)
         assert rel2 < 2e-2, (dims, rel2)
 
