@@ -223,6 +223,17 @@ int ia_visc_surften(ia_handle* h, const double* f);
  * reference checks with sum(f[inside(f)]), test/maintests.jl:209,215. */
 int ia_mass(ia_handle* h, const double* f, double* mass_out);
 
+/* Level-set reinitialisation (src/redistaning.jl).  Buffers are caller-owned scalar fields
+ * (the reference reuses f⁰ for ϕ, α for ϕ⁰, fᶠ for ϕ_ini and σ for L).
+ * ia_levelset_init: ϕ = 2f - 1 and ϕ_ini = ϕ on every cell (LevelSet, :13-25; phi_ini may be NULL).
+ * ia_levelset_rhs:  L = ϕ_ini (1 - |∇ϕ|) with ENO2 one-sided derivatives (computeL!, :64-143).
+ * ia_redistance:    round(d/dτ) SSP-RK3 pseudo-time steps of ∂τϕ = L(ϕ) with BCf! ghosts after
+ *                   each stage (redistaning!, :42-54). */
+int ia_levelset_init(ia_handle* h, const double* f, double* phi, double* phi_ini);
+int ia_levelset_rhs(ia_handle* h, double* L, const double* phi, const double* phi_ini);
+int ia_redistance(ia_handle* h, double* phi, double* phi0, const double* phi_ini, double* L, double d,
+                  double dtau);
+
 /* Step diagnostics of src/metrics.jl summed over interior cells, in one pass:
  * out[0] = Σ ρkeI(I,u,f,λρ,U) (:13-15), out[1] = Σ ρgh(I,g,f,λρ,StatWL) (:23),
  * out[2] = Σ EnsI(I,ω) (:32-39; 0 when omega is NULL), out[3+i] = Σ ρuI(i,I,u,f,λρ,U) (:56-58).

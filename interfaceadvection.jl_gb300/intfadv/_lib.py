@@ -92,6 +92,9 @@ _SIGS = {
     "ia_poisson_stats": (C.c_int, [C.c_void_p, C.c_void_p]),
     "ia_poisson_residual": (C.c_int, [C.c_void_p] * 5 + [C.POINTER(C.c_double)]),
     "ia_metrics": (C.c_int, [C.c_void_p] * 8),
+    "ia_levelset_init": (C.c_int, [C.c_void_p] * 4),
+    "ia_levelset_rhs": (C.c_int, [C.c_void_p] * 4),
+    "ia_redistance": (C.c_int, [C.c_void_p] * 5 + [C.c_double, C.c_double]),
 }
 
 _lib = None

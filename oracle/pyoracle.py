@@ -20,6 +20,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 SRC = os.path.join(HERE, "oracle.cpp")
 SRC_NN = os.path.join(HERE, "nn_oracle.cpp")
 SRC_MET = os.path.join(HERE, "metrics_oracle.cpp")
+SRC_LS = os.path.join(HERE, "levelset_oracle.cpp")
 LIB = os.path.join(HERE, "liboracle.so")
 
 SCHEMES = {"WH": 0, "WY": 1, "MYC": 2, "Y": 3, "Column": 4, "PCD": 5, "SLIC": 6, "CD": 7, "XYLIC": 8}
@@ -30,10 +31,10 @@ LIMITERS = {"Koren": 0, "upwind": 1, "minmod": 2, "vanAlbada1": 3, "Sweby": 4, "
 def build(force: bool = False) -> str:
     """Compile liboracle.so with g++ (OpenMP, IEEE FP64, no FMA contraction)."""
     if force or not os.path.exists(LIB) or os.path.getmtime(LIB) < max(
-            os.path.getmtime(SRC), os.path.getmtime(SRC_NN), os.path.getmtime(SRC_MET),
+            os.path.getmtime(SRC), os.path.getmtime(SRC_NN), os.path.getmtime(SRC_MET), os.path.getmtime(SRC_LS),
             os.path.getmtime(os.path.join(HERE, "oracle.h"))):
         cmd = ["g++", "-std=c++17", "-O2", "-fopenmp", "-ffp-contract=off", "-fPIC", "-shared",
-               SRC, SRC_NN, SRC_MET, "-o", LIB + ".tmp"]
+               SRC, SRC_NN, SRC_MET, SRC_LS, "-o", LIB + ".tmp"]
         subprocess.run(cmd, check=True)
         os.replace(LIB + ".tmp", LIB)
     return LIB
@@ -93,6 +94,9 @@ def lib():
             "orc_rhoke": (d, [p, i64, p, p, d, p]), "orc_rhou": (d, [p, i, i64, p, p, d, p]),
             "orc_rhogh": (d, [p, i64, p, p, d, p]), "orc_ens": (d, [p, i64, p]),
             "orc_metrics": (None, [p, p, p, p, d, p, p, p, p]),
+            "orc_levelset_init": (None, [p, p, p, p]), "orc_levelset_rhs": (None, [p, p, p, p]),
+            "orc_levelset_stage": (None, [p, p, p, p, p, d, d]),
+            "orc_redistance": (None, [p, p, p, p, p, d, d]),
             "orc_nn_param_count": (i64, []),
             "orc_nn_forward": (None, [p, p, i, i, i, i, p]),
             "orc_nn_loss_grad": (d, [p, p, p, i, i, i, i, p]),
@@ -250,3 +254,26 @@ def metrics(u, f, lrho, U=None, g=None, statwl=None, omega=None, per=()):
     lib().orc_metrics(C.byref(gr), ptr(u), ptr(f), ptr(omega), float(lrho), Ua.ctypes.data, ga.ctypes.data,
                       wa.ctypes.data, out.ctypes.data)
     return {"ke": out[0], "pe": out[1], "ens": out[2], "rhou": out[3:].tolist()}
+
+
+# ---- level-set reinitialisation (levelset_oracle.cpp) -----------------------------------------
+
+def levelset_rhs(phi, ini, per=()):
+    L = zeros(phi.shape)
+    lib().orc_levelset_rhs(C.byref(grid(phi.shape, per)), ptr(L), ptr(phi), ptr(ini))
+    return L
+
+
+def levelset_stage(phi, phi0, ini, L, dtau, alpha, per=()):
+    """In place on phi (and L), like _redistaningStage!; ini may be phi itself."""
+    lib().orc_levelset_stage(C.byref(grid(phi.shape, per)), ptr(phi), ptr(phi0), ptr(ini), ptr(L), float(dtau),
+                             float(alpha))
+
+
+def redistance(f, d=5.0, dtau=0.5, per=()):
+    """LevelSet from f, then redistaning!; returns ϕ."""
+    g = grid(f.shape, per)
+    phi, ini, phi0, L = zeros(f.shape), zeros(f.shape), zeros(f.shape), zeros(f.shape)
+    lib().orc_levelset_init(C.byref(g), ptr(f), ptr(phi), ptr(ini))
+    lib().orc_redistance(C.byref(g), ptr(phi), ptr(phi0), ptr(ini), ptr(L), float(d), float(dtau))
+    return phi
