@@ -287,8 +287,13 @@ int ia_nn_set_loss(ia_handle* h, int32_t kind);
 int ia_nn_train_step(ia_handle* h, const float* x0, const float* target, int32_t B, int32_t nx, int32_t ny,
                      int32_t nz, float lr, double* loss);
 /* inner preconditioner of an IA_POISSON_LEARNED handle and the inner FCG limits
- * (inner_max iterations, relative inner residual target) */
+ * (inner_max iterations, relative inner residual target); an IA_POISSON_MIXED handle accepts
+ * IA_PRECOND_VCYCLE only (to set its inner limits) */
 int ia_poisson_precond(ia_handle* h, int32_t precond, int32_t inner_max, double inner_rtol);
+/* V-cycle smoothing of the handle's multigrid (no reference counterpart; the reference's
+ * MultiLevelPoisson settings are WaterLily's): nu1 red-black sweeps before and nu2 after the
+ * coarse correction, nuc symmetric sweeps on the coarsest level (defaults 2, 2, 16) */
+int ia_poisson_mg_params(ia_handle* h, int32_t nu1, int32_t nu2, int32_t nuc);
 /* counters since the handle's creation: [0] net applications, [1] V-cycles, [2] fallbacks
  * to the V-cycle, [3] inner FCG iterations, [4] outer corrections */
 int ia_poisson_stats(ia_handle* h, int64_t* out5);

@@ -75,19 +75,34 @@ __global__ void u2rhou_kern(MomConsts k, double* __restrict__ rhou, const double
     for (int i = 0; i < g.D; ++i) rhou[I + i * g.N] = mul_rho(k, u[I + i * g.N], f[I], f[I - g.s[i]]);
 }
 
-__global__ void bcvel_kern(MomConsts k, double* a, double A0, double A1, double A2) {
-    const Grid& g = k.g;
-    CELL_XYZ
-    const int c0[3] = {x, y, z};
+// BC! at one cell: Dirichlet A[i] on the normal faces, ghost copies elsewhere
+__device__ __forceinline__ void bcvel_cell(const Grid& g, double* a, const double A[3], const int c0[3]) {
     const bool inner = is_interior(g, c0);
-    const long long O = lin(g, x, y, z);
-    const double A[3] = {A0, A1, A2};
+    const long long O = lin3(g, c0);
     for (int i = 0; i < g.D; ++i) {
-        int c[3] = {x, y, z};
+        int c[3] = {c0[0], c0[1], c0[2]};
         if (vel_bc(g, i, c)) { a[O + i * g.N] = A[i]; continue; }
         if (inner) continue;
         a[O + i * g.N] = a[lin3(g, c) + i * g.N];
     }
+}
+
+// Only cells with a coordinate in the boundary layers of its dimension can change ({0, 1, n-1}
+// along a wall dimension, {0, n-1} along a periodic one): one launch per dimension e covers the
+// slabs c[e] = layer (blockIdx.z) over the other two dimensions; a cell in two slabs gets the
+// same value twice, and every copy source is a cell no thread writes.
+__global__ void bcvel_slab_kern(MomConsts k, double* a, double A0, double A1, double A2, int e) {
+    const Grid& g = k.g;
+    const int da = e == 0 ? 1 : 0, db = e == 2 ? 1 : 2;
+    const int u = blockIdx.x * blockDim.x + threadIdx.x, v = blockIdx.y * blockDim.y + threadIdx.y;
+    if (u >= g.n[da] || v >= (g.D == 3 ? g.n[db] : 1)) return;
+    const int layer = blockIdx.z;
+    int c[3];
+    c[e] = layer == 0 ? 0 : (layer == 1 ? g.n[e] - 1 : 1);
+    c[da] = u;
+    c[db] = g.D == 3 ? v : 0;
+    const double A[3] = {A0, A1, A2};
+    bcvel_cell(g, a, A, c);
 }
 
 // ------------------------------------------------------------------ limiters (src/flow.jl:5-15)
@@ -407,26 +422,41 @@ __device__ __forceinline__ int pair_index(int D, int i, int j) {
     return D + (a == 0 ? (b - 1) : 2);   // (0,1)->D, (0,2)->D+1, (1,2)->D+2
 }
 
+template <int D>
 __global__ void viscflux_kern(ViscCtx V, double* __restrict__ Phi6) {
     const Grid& g = V.k.g;
     CELL_XYZ
     const int c[3] = {x, y, z};
     const long long K = lin(g, x, y, z);
     bool inner = true;
-    for (int e = 0; e < g.D; ++e)
+#pragma unroll
+    for (int e = 0; e < D; ++e)
         if (c[e] < 3 || c[e] > g.n[e] - 3) inner = false;
-    for (int i = 0; i < g.D; ++i)
-        for (int j = i; j < g.D; ++j) {
+    if (inner) {
+        // every face and edge of this cell is a flux position, no boundary rule applies
+#pragma unroll
+        for (int i = 0; i < D; ++i)
+#pragma unroll
+            for (int j = i; j < D; ++j) {
+                const double mu = get_mu_inner(V, i, j, c, K);
+                const double sji = V.u[K + i * g.N] - V.u[K - g.s[j] + i * g.N];
+                const double sij = V.u[K + j * g.N] - V.u[K - g.s[i] + j * g.N];
+                Phi6[pair_index(D, i, j) * g.N + K] = -(mu * (sji + sij));
+            }
+        return;
+    }
+    for (int i = 0; i < D; ++i)
+        for (int j = i; j < D; ++j) {
             bool ok = true;
-            for (int e = 0; e < g.D; ++e) {
+            for (int e = 0; e < D; ++e) {
                 const int hi = (e == i || e == j) ? g.n[e] - 1 : g.n[e] - 2;
                 if (c[e] < 1 || c[e] > hi) ok = false;
             }
             if (!ok) continue;
-            const double mu = inner ? get_mu_inner(V, i, j, c, K) : get_mu(V, i, j, c);
+            const double mu = get_mu(V, i, j, c);
             const double sji = V.u[K + i * g.N] - V.u[K - g.s[j] + i * g.N];
             const double sij = V.u[K + j * g.N] - V.u[K - g.s[i] + j * g.N];
-            Phi6[pair_index(g.D, i, j) * g.N + K] = -(mu * (sji + sij));
+            Phi6[pair_index(D, i, j) * g.N + K] = -(mu * (sji + sij));
         }
 }
 
@@ -628,39 +658,56 @@ __device__ __forceinline__ unsigned long long nonneg_bits(double v) {
     return (b == 0x8000000000000000ull) ? 0ull : b;
 }
 
+// -u with the sign bit flipped (no FP64 instruction)
+__device__ __forceinline__ double dneg(double v) { return __longlong_as_double(__double_as_longlong(v) ^ (1ll << 63)); }
+
+__device__ __forceinline__ unsigned long long warp_umax(unsigned long long v) {
+    for (int o = 16; o > 0; o >>= 1) {
+        const unsigned long long w = __shfl_down_sync(0xffffffffu, v, o);
+        v = w > v ? w : v;
+    }
+    return v;
+}
+
+// max over interior cells of WaterLily flux_out (Σ max(0,u_hi) + max(0,-u_lo)) and of
+// maxTotalFlux (Σ max(|u_lo|,|u_hi|), src/flow.jl:283-289), as non-negative FP64 bit patterns;
+// whole x-rows per block, warp-shuffle maxima
 __global__ void cfl_kern(Grid g, const double* __restrict__ u, unsigned long long* out) {
-    __shared__ unsigned long long s1[256], s2[256];
-    const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y;
-    const int z = blockIdx.z;
-    const int t = threadIdx.y * blockDim.x + threadIdx.x;
+    __shared__ unsigned long long s1[32], s2[32];
     unsigned long long a1 = 0ull, a2 = 0ull;
-    if (x < g.n[0] && y < g.n[1]) {
-        const int c[3] = {x, y, z};
-        if (is_interior(g, c)) {
+    const int nxi = g.n[0] - 2, nyi = g.n[1] - 2;
+    const long long rows = (long long)nyi * (g.D == 3 ? g.n[2] - 2 : 1);
+    for (long long rw = blockIdx.x; rw < rows; rw += gridDim.x) {
+        const int y = 1 + int(rw % nyi), z = g.D == 3 ? 1 + int(rw / nyi) : 0;
+        for (int x = 1 + threadIdx.x; x <= nxi; x += blockDim.x) {
             const long long I = lin(g, x, y, z);
             double fo = 0.0, mt = 0.0;
             for (int i = 0; i < g.D; ++i) {
                 const double lo = u[I + i * g.N], hi = u[I + g.s[i] + i * g.N];
-                fo += dmax(0.0, hi) + dmax(0.0, -lo);        // WaterLily flux_out
-                mt += dmax(dabs(lo), dabs(hi));              // maxTotalFlux, src/flow.jl:283-289
+                fo += dmax(0.0, hi) + dmax(0.0, dneg(lo));   // WaterLily flux_out
+                mt += dmax(dabs(lo), dabs(hi));              // maxTotalFlux
             }
-            a1 = nonneg_bits(fo);
-            a2 = nonneg_bits(mt);
+            const unsigned long long b1 = nonneg_bits(fo), b2 = nonneg_bits(mt);
+            a1 = b1 > a1 ? b1 : a1;
+            a2 = b2 > a2 ? b2 : a2;
         }
     }
-    s1[t] = a1;
-    s2[t] = a2;
+    a1 = warp_umax(a1);
+    a2 = warp_umax(a2);
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    if (lane == 0) {
+        s1[w] = a1;
+        s2[w] = a2;
+    }
     __syncthreads();
-    for (int w = 128; w > 0; w >>= 1) {
-        if (t < w) {
-            s1[t] = s1[t] > s1[t + w] ? s1[t] : s1[t + w];
-            s2[t] = s2[t] > s2[t + w] ? s2[t] : s2[t + w];
+    if (w == 0) {
+        const int nw = blockDim.x >> 5;
+        a1 = warp_umax(lane < nw ? s1[lane] : 0ull);
+        a2 = warp_umax(lane < nw ? s2[lane] : 0ull);
+        if (lane == 0) {
+            atomicMax(out, a1);
+            atomicMax(out + 1, a2);
         }
-        __syncthreads();
-    }
-    if (t == 0) {
-        atomicMax(&out[0], s1[0]);
-        atomicMax(&out[1], s2[0]);
     }
 }
 
@@ -675,7 +722,12 @@ cudaError_t k_u2rhou(const MomConsts& k, double* rhou, const double* u, const do
     return cudaGetLastError();
 }
 cudaError_t k_bc_vel(const MomConsts& k, double* a, const double* A, cudaStream_t s) {
-    { bcvel_kern<<<grd(k.g), blk(), 0, s>>>(k, a, A[0], A[1], A[2]); ia::note_launch(); }
+    const Grid& g = k.g;
+    for (int e = 0; e < g.D; ++e) {
+        const int da = e == 0 ? 1 : 0, db = e == 2 ? 1 : 2;
+        const dim3 gr((g.n[da] + 31) / 32, g.D == 3 ? (g.n[db] + 7) / 8 : 1, g.isper(e) ? 2 : 3);
+        { bcvel_slab_kern<<<gr, blk(), 0, s>>>(k, a, A[0], A[1], A[2], e); ia::note_launch(); }
+    }
     return cudaGetLastError();
 }
 cudaError_t k_momflux(const MomConsts& k, int j, int limiter, const double* ustar, const double* rhouf_j,
@@ -732,7 +784,8 @@ cudaError_t k_visc(const MomConsts& k, const double* u, const double* f, double 
     };
     V.mu_face0 = mu_at(0.0);
     V.mu_face1 = mu_at(1.0);
-    { viscflux_kern<<<grd(k.g), blk(), 0, s>>>(V, Phi6); ia::note_launch(); }
+    if (k.g.D == 3) { viscflux_kern<3><<<grd(k.g), blk(), 0, s>>>(V, Phi6); ia::note_launch(); }
+    else { viscflux_kern<2><<<grd(k.g), blk(), 0, s>>>(V, Phi6); ia::note_launch(); }
     { viscacc_kern<<<grd(k.g), blk(), 0, s>>>(k.g, Phi6, r); ia::note_launch(); }
     return cudaGetLastError();
 }
@@ -766,7 +819,8 @@ cudaError_t k_correct(const MomConsts& k, double* u, const double* L, double* xx
     return cudaGetLastError();
 }
 cudaError_t k_cfl(const MomConsts& k, const double* u, unsigned long long* out2, cudaStream_t s) {
-    { cfl_kern<<<grd(k.g), blk(), 0, s>>>(k.g, u, out2); ia::note_launch(); }
+    const long long rows = (long long)(k.g.n[1] - 2) * (k.g.D == 3 ? k.g.n[2] - 2 : 1);
+    { cfl_kern<<<int(rows < 1216 ? rows : 1216), 256, 0, s>>>(k.g, u, out2); ia::note_launch(); }
     return cudaGetLastError();
 }
 cudaError_t k_average(double* a, const double* b, long long n, cudaStream_t s) {

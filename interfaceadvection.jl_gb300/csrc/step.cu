@@ -290,11 +290,22 @@ int ia_poisson_precond(ia_handle* h, int32_t precond, int32_t inner_max, double 
     if (!h || precond < IA_PRECOND_HYBRID || precond > IA_PRECOND_VCYCLE || inner_max < 1 ||
         !(inner_rtol > 0.0 && inner_rtol < 1.0))
         return IA_ERR_INVALID;
-    if (h->cfg.poisson_mode != IA_POISSON_LEARNED) return IA_ERR_UNSUPPORTED;
+    // the mixed solver takes only the inner FCG limits (its preconditioner is the V-cycle)
+    if (h->cfg.poisson_mode == IA_POISSON_FP64) return IA_ERR_UNSUPPORTED;
+    if (h->cfg.poisson_mode == IA_POISSON_MIXED && precond != IA_PRECOND_VCYCLE) return IA_ERR_UNSUPPORTED;
     if (ensure_scratch(h) != IA_OK) return IA_ERR_CUDA;
     h->mg->precond = precond;
     h->mg->inner_max = inner_max;
     h->mg->inner_rtol = inner_rtol;
+    return IA_OK;
+}
+
+int ia_poisson_mg_params(ia_handle* h, int32_t nu1, int32_t nu2, int32_t nuc) {
+    if (!h || nu1 < 1 || nu2 < 0 || nuc < 1 || nu1 > 16 || nu2 > 16 || nuc > 256) return IA_ERR_INVALID;
+    if (ensure_scratch(h) != IA_OK) return IA_ERR_CUDA;
+    h->mg->nu1 = nu1;
+    h->mg->nu2 = nu2;
+    h->mg->nuc = nuc;
     return IA_OK;
 }
 
