@@ -87,22 +87,12 @@ __device__ __forceinline__ void bcvel_cell(const Grid& g, double* a, const doubl
     }
 }
 
-// Only cells with a coordinate in the boundary layers of its dimension can change ({0, 1, n-1}
-// along a wall dimension, {0, n-1} along a periodic one): one launch per dimension e covers the
-// slabs c[e] = layer (blockIdx.z) over the other two dimensions; a cell in two slabs gets the
-// same value twice, and every copy source is a cell no thread writes.
-__global__ void bcvel_slab_kern(MomConsts k, double* a, double A0, double A1, double A2, int e) {
+__global__ void bcvel_kern(MomConsts k, double* a, double A0, double A1, double A2) {
     const Grid& g = k.g;
-    const int da = e == 0 ? 1 : 0, db = e == 2 ? 1 : 2;
-    const int u = blockIdx.x * blockDim.x + threadIdx.x, v = blockIdx.y * blockDim.y + threadIdx.y;
-    if (u >= g.n[da] || v >= (g.D == 3 ? g.n[db] : 1)) return;
-    const int layer = blockIdx.z;
-    int c[3];
-    c[e] = layer == 0 ? 0 : (layer == 1 ? g.n[e] - 1 : 1);
-    c[da] = u;
-    c[db] = g.D == 3 ? v : 0;
+    CELL_XYZ
+    const int c0[3] = {x, y, z};
     const double A[3] = {A0, A1, A2};
-    bcvel_cell(g, a, A, c);
+    bcvel_cell(g, a, A, c0);
 }
 
 // ------------------------------------------------------------------ limiters (src/flow.jl:5-15)
@@ -722,12 +712,7 @@ cudaError_t k_u2rhou(const MomConsts& k, double* rhou, const double* u, const do
     return cudaGetLastError();
 }
 cudaError_t k_bc_vel(const MomConsts& k, double* a, const double* A, cudaStream_t s) {
-    const Grid& g = k.g;
-    for (int e = 0; e < g.D; ++e) {
-        const int da = e == 0 ? 1 : 0, db = e == 2 ? 1 : 2;
-        const dim3 gr((g.n[da] + 31) / 32, g.D == 3 ? (g.n[db] + 7) / 8 : 1, g.isper(e) ? 2 : 3);
-        { bcvel_slab_kern<<<gr, blk(), 0, s>>>(k, a, A[0], A[1], A[2], e); ia::note_launch(); }
-    }
+    { bcvel_kern<<<grd(k.g), blk(), 0, s>>>(k, a, A[0], A[1], A[2]); ia::note_launch(); }
     return cudaGetLastError();
 }
 cudaError_t k_momflux(const MomConsts& k, int j, int limiter, const double* ustar, const double* rhouf_j,

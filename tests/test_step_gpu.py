@@ -178,3 +178,24 @@ def test_every_limiter_matches_oracle(cuda, limiter):
         orc.step()
     ef, eu, ep = compare(sim, orc, 2)
     assert ef < 1e-10 and eu < 1e-10 and ep < 1e-6, (limiter, ef, eu, ep)
+
+
+@pytest.mark.parametrize("dims,per", [((10, 7), ()), ((10, 7), (0, 1)), ((10, 7), (1,)), ((8, 6, 5), (0, 2)),
+                                      ((8, 6, 5), ())])
+def test_velocity_bc_matches_oracle(cuda, dims, per):
+    # WaterLily BC!(a, u_BC, false, perdir) on a random vector field, the C-ABI ia_bc_velocity
+    import ctypes as C
+    from oracle import pyoracle as O
+    rng = np.random.default_rng(len(dims) * 7 + len(per))
+    D = len(dims)
+    ng = tuple(n + 2 for n in dims)
+    a = np.asfortranarray(rng.standard_normal(ng + (D,)))
+    uBC = (0.3, -0.2, 0.1)[:D]
+    h = ia.Handle(ia.make_config(dims, perdir=per, uBC=uBC))
+    ga = ia.ffrom(a)
+    _lib.check(h.call("ia_bc_velocity", ia.fields.ptr(ga)), "ia_bc_velocity")
+    ref = a.copy(order="F")
+    A = np.zeros(3)
+    A[:D] = uBC
+    O.lib().orc_bc_vel(C.byref(O.grid(ng, per)), O.ptr(ref), A.ctypes.data)
+    assert np.array_equal(npf(ga), ref)
