@@ -56,6 +56,7 @@ __device__ __forceinline__ long long lin(const Grid& g, int x, int y, int z) {
 // Host-side count of kernel launches issued by this library (every launch site
 // calls note_launch after issuing its kernel).
 void note_launch();
+void note_launches(long long n);   // kernels of a graph launch (or, negative, of a capture)
 long long launch_count();
 
 // Order-preserving map of a double onto uint64 (for atomicMax / atomicMin).

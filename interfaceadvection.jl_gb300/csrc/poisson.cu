@@ -627,6 +627,45 @@ static cudaError_t vcycle(ia_handle* h, PoissonMG* mg, int l, cudaStream_t st, i
     return cudaGetLastError();
 }
 
+// The finest-level V-cycle through its CUDA graph (plain launches while per-launch timing is on)
+template <class T>
+static cudaError_t vcycle_run(ia_handle* h, PoissonMG* mg, cudaStream_t st) {
+    if (h->timing.on) return vcycle<T>(h, mg, 0, st, mg->nu1, mg->nu2, mg->nuc);
+    const int k = sizeof(T) == 4 ? 0 : 1;
+    int* nu = mg->vgraph_nu[k];
+    if (mg->vgraph[k] && (nu[0] != mg->nu1 || nu[1] != mg->nu2 || nu[2] != mg->nuc)) {
+        cudaGraphExecDestroy(mg->vgraph[k]);
+        mg->vgraph[k] = nullptr;
+    }
+    if (!mg->vgraph[k]) {
+        if (!mg->capture && cudaStreamCreateWithFlags(&mg->capture, cudaStreamNonBlocking) != cudaSuccess)
+            return vcycle<T>(h, mg, 0, st, mg->nu1, mg->nu2, mg->nuc);
+        const long long n0 = launch_count();
+        cudaGraph_t gr = nullptr;
+        cudaError_t e = cudaStreamBeginCapture(mg->capture, cudaStreamCaptureModeThreadLocal);
+        if (e == cudaSuccess) {
+            const cudaError_t ek = vcycle<T>(h, mg, 0, mg->capture, mg->nu1, mg->nu2, mg->nuc);
+            e = cudaStreamEndCapture(mg->capture, &gr);
+            if (e == cudaSuccess) e = ek;
+        }
+        const long long captured = launch_count() - n0;
+        note_launches(-captured);   // captured, not launched
+        if (e == cudaSuccess) e = cudaGraphInstantiate(&mg->vgraph[k], gr, 0);
+        if (gr) cudaGraphDestroy(gr);
+        if (e != cudaSuccess) {
+            mg->vgraph[k] = nullptr;
+            cudaGetLastError();
+            return vcycle<T>(h, mg, 0, st, mg->nu1, mg->nu2, mg->nuc);
+        }
+        mg->vgraph_kernels[k] = captured;
+        nu[0] = mg->nu1;
+        nu[1] = mg->nu2;
+        nu[2] = mg->nuc;
+    }
+    note_launches(mg->vgraph_kernels[k]);
+    return cudaGraphLaunch(mg->vgraph[k], st);
+}
+
 int mg_create(ia_handle* h) {
     PoissonMG* mg = new PoissonMG();
     h->mg = mg;
@@ -734,6 +773,9 @@ void mg_destroy(ia_handle* h) {
     cudaFree(mg->p32); cudaFree(mg->q32); cudaFree(mg->e32);
     cudaFree(mg->rl32); cudaFree(mg->nl32); cudaFree(mg->t32);
     cudaFree(mg->partial); cudaFree(mg->dsc); cudaFree(mg->diag64);
+    for (int k = 0; k < 2; ++k)
+        if (mg->vgraph[k]) cudaGraphExecDestroy(mg->vgraph[k]);
+    if (mg->capture) cudaStreamDestroy(mg->capture);
     if (mg->hsc) cudaFreeHost(mg->hsc);
     delete mg;
     h->mg = nullptr;
@@ -779,14 +821,14 @@ static cudaError_t mg_precondition(ia_handle* h) {
         { to_f32_k<<<1216, 256, 0, st>>>(N, mg->r, F.b32); ia::note_launch(); }
         timing_end(h, tk);
         tk = timing_begin(h, TK_MG_SMOOTH);
-        e = vcycle<float>(h, mg, 0, st, mg->nu1, mg->nu2, mg->nuc);
+        e = vcycle_run<float>(h, mg, st);
         timing_end(h, tk);
         if (e != cudaSuccess) return e;
         { to_f64_k<<<1216, 256, 0, st>>>(N, F.x32, mg->s); ia::note_launch(); }
     } else {
         cudaMemcpyAsync(F.b, mg->r, 8 * N, cudaMemcpyDeviceToDevice, st);
         int tk = timing_begin(h, TK_MG_SMOOTH);
-        e = vcycle<double>(h, mg, 0, st, mg->nu1, mg->nu2, mg->nuc);
+        e = vcycle_run<double>(h, mg, st);
         timing_end(h, tk);
         if (e != cudaSuccess) return e;
         cudaMemcpyAsync(mg->s, F.x, 8 * N, cudaMemcpyDeviceToDevice, st);
@@ -838,7 +880,7 @@ static int poisson_solve_mixed(ia_handle* h, double* xv, const double* zz, const
     int mode = learned ? mg->precond : IA_PRECOND_VCYCLE;
     auto vcyc = [&]() -> cudaError_t {
         const int tk = timing_begin(h, TK_MG_SMOOTH);
-        const cudaError_t e = vcycle<float>(h, mg, 0, st, mg->nu1, mg->nu2, mg->nuc);
+        const cudaError_t e = vcycle_run<float>(h, mg, st);
         timing_end(h, tk);
         mg->stats[1]++;
         return e;
