@@ -227,35 +227,21 @@ __device__ __forceinline__ double phiq_inner(const FluxCtx& F, double Psi, doubl
     return Psi * fma(l2, cc - vd, vd);
 }
 
-// Cells at least three cells inside the grid in every dimension (the inner box): no ghost, wall,
-// periodic-image or boundary-face rule reaches their stencils.  Kernels run the inner box with a
-// grid of its own, so no warp mixes inner and boundary-shell cells, and the shell separately.
-__device__ __forceinline__ bool in_inner_box(const Grid& g, const int c[3]) {
-    for (int e = 0; e < g.D; ++e)
-        if (c[e] < 3 || c[e] > g.n[e] - 3) return false;
-    return true;
-}
-inline bool inner_box_empty(const Grid& g) {
-    for (int e = 0; e < g.D; ++e)
-        if (g.n[e] - 5 <= 0) return true;
-    return false;
-}
-inline dim3 inner_grid(const Grid& g) {
-    return dim3((g.n[0] - 5 + 31) / 32, (g.n[1] - 5 + 7) / 8, g.D == 3 ? g.n[2] - 5 : 1);
-}
-#define INNER_BOX_XYZ(g)                                                   \
-    const int x = 3 + blockIdx.x * blockDim.x + threadIdx.x;               \
-    const int y = 3 + blockIdx.y * blockDim.y + threadIdx.y;               \
-    const int z = (g).D == 3 ? 3 + int(blockIdx.z) : 0;                    \
-    if (x > (g).n[0] - 3 || y > (g).n[1] - 3) return;
-
-template <int LIM, bool SHELL>
+template <int LIM>
 __global__ void momflux_kern(FluxCtx F, double* __restrict__ Phi) {
     const Grid& g = F.k.g;
+    CELL_XYZ
     const int j = F.j;
-    if (!SHELL) {
-        INNER_BOX_XYZ(g)
-        const long long K = lin(g, x, y, z);
+    int c[3] = {x, y, z};
+    bool inner = true;
+    for (int e = 0; e < g.D; ++e) {
+        const int hi = (e == j) ? g.n[e] - 1 : g.n[e] - 2;
+        if (c[e] < 1 || c[e] > hi) return;
+        if (c[e] < 3 || c[e] > g.n[e] - 3) inner = false;
+    }
+    const long long K = lin(g, x, y, z);
+    if (inner) {
+        // no ghost, wall, periodic-image or boundary-face rule reaches this face's stencil
         const long long sj = g.s[j];
         for (int i = 0; i < g.D; ++i) {
             const long long si = g.s[i];
@@ -270,14 +256,6 @@ __global__ void momflux_kern(FluxCtx F, double* __restrict__ Phi) {
         }
         return;
     }
-    CELL_XYZ
-    int c[3] = {x, y, z};
-    for (int e = 0; e < g.D; ++e) {
-        const int hi = (e == j) ? g.n[e] - 1 : g.n[e] - 2;
-        if (c[e] < 1 || c[e] > hi) return;
-    }
-    if (in_inner_box(g, c)) return;   // done by the inner-box launch
-    const long long K = lin(g, x, y, z);
     const bool per = g.isper(j);
     if (per && c[j] == g.n[j] - 1) c[j] = 1;              // periodic upper face = lower face
     const long long Kk = lin3(g, c);
@@ -434,14 +412,18 @@ __device__ __forceinline__ int pair_index(int D, int i, int j) {
     return D + (a == 0 ? (b - 1) : 2);   // (0,1)->D, (0,2)->D+1, (1,2)->D+2
 }
 
-template <int D, bool SHELL>
+template <int D>
 __global__ void viscflux_kern(ViscCtx V, double* __restrict__ Phi6) {
     const Grid& g = V.k.g;
-    if (!SHELL) {
-        // inner box: every face and edge of the cell is a flux position, no boundary rule applies
-        INNER_BOX_XYZ(g)
-        const int c[3] = {x, y, z};
-        const long long K = lin(g, x, y, z);
+    CELL_XYZ
+    const int c[3] = {x, y, z};
+    const long long K = lin(g, x, y, z);
+    bool inner = true;
+#pragma unroll
+    for (int e = 0; e < D; ++e)
+        if (c[e] < 3 || c[e] > g.n[e] - 3) inner = false;
+    if (inner) {
+        // every face and edge of this cell is a flux position, no boundary rule applies
 #pragma unroll
         for (int i = 0; i < D; ++i)
 #pragma unroll
@@ -453,10 +435,6 @@ __global__ void viscflux_kern(ViscCtx V, double* __restrict__ Phi6) {
             }
         return;
     }
-    CELL_XYZ
-    const int c[3] = {x, y, z};
-    if (in_inner_box(g, c)) return;   // done by the inner-box launch
-    const long long K = lin(g, x, y, z);
     for (int i = 0; i < D; ++i)
         for (int j = i; j < D; ++j) {
             bool ok = true;
@@ -737,13 +715,6 @@ cudaError_t k_bc_vel(const MomConsts& k, double* a, const double* A, cudaStream_
     { bcvel_kern<<<grd(k.g), blk(), 0, s>>>(k, a, A[0], A[1], A[2]); ia::note_launch(); }
     return cudaGetLastError();
 }
-template <int LIM>
-void launch_momflux(const FluxCtx& F, double* Phi, cudaStream_t s) {
-    const Grid& g = F.k.g;
-    if (!inner_box_empty(g)) { momflux_kern<LIM, false><<<inner_grid(g), blk(), 0, s>>>(F, Phi); ia::note_launch(); }
-    { momflux_kern<LIM, true><<<grd(g), blk(), 0, s>>>(F, Phi); ia::note_launch(); }
-}
-
 cudaError_t k_momflux(const MomConsts& k, int j, int limiter, const double* ustar, const double* rhouf_j,
                       const double* fold, double dt, double* Phi, cudaStream_t s) {
     FluxCtx F;
@@ -761,14 +732,14 @@ cudaError_t k_momflux(const MomConsts& k, int j, int limiter, const double* usta
     F.kl_l = dt * k.inv_lrho;
     F.kl_1 = dt * k.inv_rho1;
     switch (limiter) {
-        case IA_LIMITER_UPWIND: launch_momflux<IA_LIMITER_UPWIND>(F, Phi, s); break;
-        case IA_LIMITER_MINMOD: launch_momflux<IA_LIMITER_MINMOD>(F, Phi, s); break;
-        case IA_LIMITER_VANALBADA1: launch_momflux<IA_LIMITER_VANALBADA1>(F, Phi, s); break;
-        case IA_LIMITER_SWEBY: launch_momflux<IA_LIMITER_SWEBY>(F, Phi, s); break;
-        case IA_LIMITER_SUPERBEE: launch_momflux<IA_LIMITER_SUPERBEE>(F, Phi, s); break;
-        case IA_LIMITER_TVDCEN: launch_momflux<IA_LIMITER_TVDCEN>(F, Phi, s); break;
-        case IA_LIMITER_TVDDOWN: launch_momflux<IA_LIMITER_TVDDOWN>(F, Phi, s); break;
-        default: launch_momflux<IA_LIMITER_KOREN>(F, Phi, s); break;
+        case IA_LIMITER_UPWIND: { momflux_kern<IA_LIMITER_UPWIND><<<grd(k.g), blk(), 0, s>>>(F, Phi); ia::note_launch(); } break;
+        case IA_LIMITER_MINMOD: { momflux_kern<IA_LIMITER_MINMOD><<<grd(k.g), blk(), 0, s>>>(F, Phi); ia::note_launch(); } break;
+        case IA_LIMITER_VANALBADA1: { momflux_kern<IA_LIMITER_VANALBADA1><<<grd(k.g), blk(), 0, s>>>(F, Phi); ia::note_launch(); } break;
+        case IA_LIMITER_SWEBY: { momflux_kern<IA_LIMITER_SWEBY><<<grd(k.g), blk(), 0, s>>>(F, Phi); ia::note_launch(); } break;
+        case IA_LIMITER_SUPERBEE: { momflux_kern<IA_LIMITER_SUPERBEE><<<grd(k.g), blk(), 0, s>>>(F, Phi); ia::note_launch(); } break;
+        case IA_LIMITER_TVDCEN: { momflux_kern<IA_LIMITER_TVDCEN><<<grd(k.g), blk(), 0, s>>>(F, Phi); ia::note_launch(); } break;
+        case IA_LIMITER_TVDDOWN: { momflux_kern<IA_LIMITER_TVDDOWN><<<grd(k.g), blk(), 0, s>>>(F, Phi); ia::note_launch(); } break;
+        default: { momflux_kern<IA_LIMITER_KOREN><<<grd(k.g), blk(), 0, s>>>(F, Phi); ia::note_launch(); } break;
     }
     return cudaGetLastError();
 }
@@ -798,14 +769,8 @@ cudaError_t k_visc(const MomConsts& k, const double* u, const double* f, double 
     };
     V.mu_face0 = mu_at(0.0);
     V.mu_face1 = mu_at(1.0);
-    const bool box = !inner_box_empty(k.g);
-    if (k.g.D == 3) {
-        if (box) { viscflux_kern<3, false><<<inner_grid(k.g), blk(), 0, s>>>(V, Phi6); ia::note_launch(); }
-        { viscflux_kern<3, true><<<grd(k.g), blk(), 0, s>>>(V, Phi6); ia::note_launch(); }
-    } else {
-        if (box) { viscflux_kern<2, false><<<inner_grid(k.g), blk(), 0, s>>>(V, Phi6); ia::note_launch(); }
-        { viscflux_kern<2, true><<<grd(k.g), blk(), 0, s>>>(V, Phi6); ia::note_launch(); }
-    }
+    if (k.g.D == 3) { viscflux_kern<3><<<grd(k.g), blk(), 0, s>>>(V, Phi6); ia::note_launch(); }
+    else { viscflux_kern<2><<<grd(k.g), blk(), 0, s>>>(V, Phi6); ia::note_launch(); }
     { viscacc_kern<<<grd(k.g), blk(), 0, s>>>(k.g, Phi6, r); ia::note_launch(); }
     return cudaGetLastError();
 }
