@@ -174,50 +174,25 @@ __global__ void restrict_L_k(Grid gc, Grid gf, const T* __restrict__ Lf, T* __re
 // lane idles; the diagonal comes from the face coefficients the update reads anyway
 // (same value and zero-diagonal rule as set_diag_k).
 template <class T, int D>
-__device__ __forceinline__ bool rb_cell(const Grid& g, const T* __restrict__ L, const T* __restrict__ b,
-                                       const T* xv, int xp, int y, int z, int color, int& I, T& v) {
-    int x = xp;
+__global__ void rbgs_pair_k(Grid g, const T* __restrict__ L, const T* __restrict__ b, T* __restrict__ xv,
+                            int color) {
+    const int y = 1 + blockIdx.y * blockDim.y + threadIdx.y;
+    const int z = D == 3 ? 1 + int(blockIdx.z) : 0;
+    if (y > g.n[1] - 2) return;
+    int x = 1 + 2 * (blockIdx.x * blockDim.x + threadIdx.x);
     if (((x + y + z) & 1) != color) ++x;
-    if (x > g.n[0] - 2 || z > (D == 3 ? g.n[2] - 2 : 0)) return false;
-    I = x + y * int(g.s[1]) + z * int(g.s[2]);
+    if (x > g.n[0] - 2) return;
+    const int I = x + y * int(g.s[1]) + z * int(g.s[2]);
     const Nb o = nb_of<D>(g, x, y, z);
     const T off = off7<D>(g, L, xv, I, o);
     const T dd = diag7<D>(g, L, I);
     const T eps = sizeof(T) == 8 ? T(2.220446049250313e-16) : T(1.1920929e-7);
     const T iD = (dd * dd < T(2) * eps) ? T(0) : T(1) / dd;
-    v = (b[I] - off) * iD;
-    return true;
-}
-
-// Red-black Gauss-Seidel half-sweep, one thread per cell of the colour: thread tx takes the pair of
-// interior cells (1 + 2tx, 2 + 2tx) of its row and updates the one of this colour, so no lane idles;
-// the diagonal comes from the face coefficients the update reads anyway (same value and
-// zero-diagonal rule as set_diag_k).  In 3D a thread does the pair in two consecutive planes and
-// stores after both updates (a cell's z-neighbours have the other colour, so the two updates are
-// independent), keeping twice the loads in flight.
-template <class T, int D>
-__global__ void rbgs_pair_k(Grid g, const T* __restrict__ L, const T* __restrict__ b, T* __restrict__ xv,
-                            int color) {
-    const int y = 1 + blockIdx.y * blockDim.y + threadIdx.y;
-    if (y > g.n[1] - 2) return;
-    const int xp = 1 + 2 * (blockIdx.x * blockDim.x + threadIdx.x);
-    if (D == 3) {
-        const int z0 = 1 + 2 * int(blockIdx.z);
-        int I0 = 0, I1 = 0;
-        T v0 = T(0), v1 = T(0);
-        const bool a0 = rb_cell<T, D>(g, L, b, xv, xp, y, z0, color, I0, v0);
-        const bool a1 = rb_cell<T, D>(g, L, b, xv, xp, y, z0 + 1, color, I1, v1);
-        if (a0) xv[I0] = v0;
-        if (a1) xv[I1] = v1;
-    } else {
-        int I = 0;
-        T v = T(0);
-        if (rb_cell<T, D>(g, L, b, xv, xp, y, 0, color, I, v)) xv[I] = v;
-    }
+    xv[I] = (b[I] - off) * iD;
 }
 inline dim3 pair_grid(const Grid& g) {
     const int pairs = (g.n[0] - 2 + 1) / 2;
-    return dim3((pairs + 31) / 32, (g.n[1] - 2 + 7) / 8, g.D == 3 ? (g.n[2] - 2 + 1) / 2 : 1);
+    return dim3((pairs + 31) / 32, (g.n[1] - 2 + 7) / 8, g.D == 3 ? g.n[2] - 2 : 1);
 }
 
 // first red sweep from x = 0: neighbours are zero
