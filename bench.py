@@ -41,6 +41,7 @@ B_RBGS_PER_CELL_F32 = 18   # one FP32 red-black half-sweep: L (12) + x read/writ
 # DRAM bytes per cell of that launch from an ncu capture of the same kernel at 160x320x160
 # (profiles/kernel_counters_bubble160.md), scaled by the cells of the launch
 TRAFFIC_RBGS_PER_CELL_F32 = 22.6
+TRAFFIC_VOF_BULK_PER_CELL = 31.1   # vof_bulk, ncu capture at 192³ (profiles/vof_bulk_sphere192.md)
 B_BULK_PER_CELL = 33       # vof_bulk: read f, u_d, u0_d (24) + c̄ (1); write ρuf_d (8)
 TK = {"vof_bulk": 0, "vof_cells": 1, "ustar": 2, "forcing": 3, "mg_vcycle": 4, "mg_transfer": 6, "krylov": 7,
       "vof_faces": 9, "momflux": 10, "momupdate": 11, "update_project": 12, "mg_fine_rbgs": 13, "nn_precond": 14}
@@ -384,6 +385,8 @@ def run_vof(args, world, local_rank, steps=200):
             "value": world * N ** 3 * steps / (ms / 1e3) / 1e6, "ms_per_step": ms / steps,
             "mass_drift": abs(intf.mass() - m0) / m0,
             "roofline": {"bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s", "frac": ach / peak,
+                         "traffic": TRAFFIC_VOF_BULK_PER_CELL * N ** 3,
+                         "traffic_note": "ncu dram bytes of one launch at 192^3 (31.1 B/cell), scaled",
                          "kernel": "vof_bulk", "peak_kind": peak_kind, "avg_launch_ms": bulk_ms}}
 
 
