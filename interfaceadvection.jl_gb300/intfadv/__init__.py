@@ -11,6 +11,8 @@ from .core import (Flow, Handle, advect, advect_vof_raw, advectVOF, apply_vof, a
 from .diagnostics import metrics, sim_metrics
 from .fields import cell_coords, face_coords, ffrom, fones, fzeros, is_fortran
 from .levelset import LevelSet, computeL, redistaning
+from .vtk import VTKWriter
+from .vtk import load as load_vtk
 from .simulation import (MPCFL, MPFMomStep, NoBody, TwoPhaseSimulation, poisson_stats, set_learned, sim_info,
                          sim_step)
 
@@ -18,4 +20,4 @@ __all__ = ["Flow", "Handle", "advect", "advect_vof_raw", "advectVOF", "apply_vof
            "get_vof_flux", "getVOFFlux", "make_config", "reconstruct_interface", "reconstructInterface", "build",
            "cell_coords", "face_coords", "ffrom", "fones", "fzeros", "is_fortran", "MPCFL", "MPFMomStep", "NoBody",
            "TwoPhaseSimulation", "sim_info", "sim_step", "poisson_stats", "set_learned", "metrics", "sim_metrics", "LevelSet", "redistaning",
-           "computeL"]
+           "computeL", "VTKWriter", "load_vtk"]
