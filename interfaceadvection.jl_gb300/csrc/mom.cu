@@ -21,6 +21,42 @@ namespace {
 inline dim3 blk() { return dim3(32, 8, 1); }
 inline dim3 grd(const Grid& g) { return dim3((g.n[0] + 31) / 32, (g.n[1] + 7) / 8, g.n[2]); }
 
+// Interior-cell launch: lane 0 of the first block sits on cell 1, so a row of 32k interior
+// cells fills k warps exactly and no warp spends FP64 issue slots on a ghost-cell lane.
+inline dim3 igrd(const Grid& g) {
+    return dim3((g.n[0] - 2 + 31) / 32, (g.n[1] - 2 + 7) / 8, g.D == 3 ? g.n[2] - 2 : 1);
+}
+#define ICELL_XYZ                                                                     \
+    const int x = 1 + blockIdx.x * blockDim.x + threadIdx.x;                          \
+    const int y = 1 + blockIdx.y * blockDim.y + threadIdx.y;                          \
+    const int z = g.D == 3 ? 1 + int(blockIdx.z) : 0;                                 \
+    if (x > g.n[0] - 2 || y > g.n[1] - 2) return;
+
+// Face-flux launch (momentum flux, viscous flux): the x-range [3, n-3], whose faces and
+// edges need no boundary rule, one cell per lane; then one more block column whose first
+// warp takes the x-boundary cells {1, 2, n-2, n-1} of the block's 8 rows.  A warp then runs
+// either the bulk path or the boundary path for all its lanes: FP64 issues per warp
+// instruction, whatever the number of active lanes, so a warp that mixes the two pays for both.
+inline dim3 split_grid(const Grid& g) {
+    const int wi = g.n[0] > 5 ? (g.n[0] - 5 + 31) / 32 : 0;
+    return dim3(wi + 1, (g.n[1] + 7) / 8, g.n[2]);
+}
+#define SPLIT_XYZ                                                                     \
+    int x, y;                                                                         \
+    const int z = blockIdx.z;                                                         \
+    if (blockIdx.x + 1 < gridDim.x) {                                                 \
+        x = 3 + int(blockIdx.x) * 32 + int(threadIdx.x);                              \
+        y = int(blockIdx.y) * 8 + int(threadIdx.y);                                   \
+        if (x > g.n[0] - 3) return;                                                   \
+    } else {                                                                          \
+        if (threadIdx.y != 0) return;                                                 \
+        const int kb = int(threadIdx.x) & 3;                                          \
+        x = kb < 2 ? 1 + kb : g.n[0] - 4 + kb;                                        \
+        if (kb >= 2 && x <= 2) return;                                                \
+        y = int(blockIdx.y) * 8 + (int(threadIdx.x) >> 2);                            \
+    }                                                                                 \
+    if (y >= g.n[1]) return;
+
 #define CELL_XYZ                                                                                   \
     const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y; \
     const int z = blockIdx.z;                                                                      \
@@ -230,7 +266,7 @@ __device__ __forceinline__ double phiq_inner(const FluxCtx& F, double Psi, doubl
 template <int LIM>
 __global__ void momflux_kern(FluxCtx F, double* __restrict__ Phi) {
     const Grid& g = F.k.g;
-    CELL_XYZ
+    SPLIT_XYZ
     const int j = F.j;
     int c[3] = {x, y, z};
     bool inner = true;
@@ -415,7 +451,7 @@ __device__ __forceinline__ int pair_index(int D, int i, int j) {
 template <int D>
 __global__ void viscflux_kern(ViscCtx V, double* __restrict__ Phi6) {
     const Grid& g = V.k.g;
-    CELL_XYZ
+    SPLIT_XYZ
     const int c[3] = {x, y, z};
     const long long K = lin(g, x, y, z);
     bool inner = true;
@@ -451,9 +487,8 @@ __global__ void viscflux_kern(ViscCtx V, double* __restrict__ Phi6) {
 }
 
 __global__ void viscacc_kern(Grid g, const double* __restrict__ Phi6, double* __restrict__ r) {
-    CELL_XYZ
+    ICELL_XYZ
     const int c[3] = {x, y, z};
-    if (!is_interior(g, c)) return;
     const long long I = lin(g, x, y, z);
     for (int i = 0; i < g.D; ++i) {
         double acc = 0.0;
@@ -560,9 +595,8 @@ template <int D>
 __global__ void surften_kern(MomConsts k, int d, const double* __restrict__ f, const double* __restrict__ fb,
                              double eta, double* __restrict__ r) {
     const Grid& g = k.g;
-    CELL_XYZ
+    ICELL_XYZ
     const int c[3] = {x, y, z};
-    if (!is_interior(g, c)) return;
     const long long I = lin(g, x, y, z);
     if (!mixed(fb[I])) return;
     Stencil S;
@@ -585,9 +619,8 @@ __global__ void updateu_kern(MomConsts k, double* __restrict__ u, double* __rest
                              const double* __restrict__ fref, const double* __restrict__ fupd, double w, double a,
                              bool write_rhou) {
     const Grid& g = k.g;
-    CELL_XYZ
+    ICELL_XYZ
     const int c[3] = {x, y, z};
-    if (!is_interior(g, c)) return;
     const long long I = lin(g, x, y, z);
     for (int i = 0; i < g.D; ++i) {
         const long long q = I + i * g.N;
@@ -626,9 +659,8 @@ __global__ void div_scale_kern(Grid g, const double* __restrict__ u, double* __r
 
 __global__ void correct_kern(Grid g, double* __restrict__ u, const double* __restrict__ L,
                              const double* __restrict__ xx) {
-    CELL_XYZ
+    ICELL_XYZ
     const int c[3] = {x, y, z};
-    if (!is_interior(g, c)) return;
     const long long I = lin(g, x, y, z);
     for (int i = 0; i < g.D; ++i) u[I + i * g.N] -= L[I + i * g.N] * (xx[I] - xx[I - g.s[i]]);
 }
@@ -732,14 +764,14 @@ cudaError_t k_momflux(const MomConsts& k, int j, int limiter, const double* usta
     F.kl_l = dt * k.inv_lrho;
     F.kl_1 = dt * k.inv_rho1;
     switch (limiter) {
-        case IA_LIMITER_UPWIND: { momflux_kern<IA_LIMITER_UPWIND><<<grd(k.g), blk(), 0, s>>>(F, Phi); ia::note_launch(); } break;
-        case IA_LIMITER_MINMOD: { momflux_kern<IA_LIMITER_MINMOD><<<grd(k.g), blk(), 0, s>>>(F, Phi); ia::note_launch(); } break;
-        case IA_LIMITER_VANALBADA1: { momflux_kern<IA_LIMITER_VANALBADA1><<<grd(k.g), blk(), 0, s>>>(F, Phi); ia::note_launch(); } break;
-        case IA_LIMITER_SWEBY: { momflux_kern<IA_LIMITER_SWEBY><<<grd(k.g), blk(), 0, s>>>(F, Phi); ia::note_launch(); } break;
-        case IA_LIMITER_SUPERBEE: { momflux_kern<IA_LIMITER_SUPERBEE><<<grd(k.g), blk(), 0, s>>>(F, Phi); ia::note_launch(); } break;
-        case IA_LIMITER_TVDCEN: { momflux_kern<IA_LIMITER_TVDCEN><<<grd(k.g), blk(), 0, s>>>(F, Phi); ia::note_launch(); } break;
-        case IA_LIMITER_TVDDOWN: { momflux_kern<IA_LIMITER_TVDDOWN><<<grd(k.g), blk(), 0, s>>>(F, Phi); ia::note_launch(); } break;
-        default: { momflux_kern<IA_LIMITER_KOREN><<<grd(k.g), blk(), 0, s>>>(F, Phi); ia::note_launch(); } break;
+        case IA_LIMITER_UPWIND: { momflux_kern<IA_LIMITER_UPWIND><<<split_grid(k.g), blk(), 0, s>>>(F, Phi); ia::note_launch(); } break;
+        case IA_LIMITER_MINMOD: { momflux_kern<IA_LIMITER_MINMOD><<<split_grid(k.g), blk(), 0, s>>>(F, Phi); ia::note_launch(); } break;
+        case IA_LIMITER_VANALBADA1: { momflux_kern<IA_LIMITER_VANALBADA1><<<split_grid(k.g), blk(), 0, s>>>(F, Phi); ia::note_launch(); } break;
+        case IA_LIMITER_SWEBY: { momflux_kern<IA_LIMITER_SWEBY><<<split_grid(k.g), blk(), 0, s>>>(F, Phi); ia::note_launch(); } break;
+        case IA_LIMITER_SUPERBEE: { momflux_kern<IA_LIMITER_SUPERBEE><<<split_grid(k.g), blk(), 0, s>>>(F, Phi); ia::note_launch(); } break;
+        case IA_LIMITER_TVDCEN: { momflux_kern<IA_LIMITER_TVDCEN><<<split_grid(k.g), blk(), 0, s>>>(F, Phi); ia::note_launch(); } break;
+        case IA_LIMITER_TVDDOWN: { momflux_kern<IA_LIMITER_TVDDOWN><<<split_grid(k.g), blk(), 0, s>>>(F, Phi); ia::note_launch(); } break;
+        default: { momflux_kern<IA_LIMITER_KOREN><<<split_grid(k.g), blk(), 0, s>>>(F, Phi); ia::note_launch(); } break;
     }
     return cudaGetLastError();
 }
@@ -769,9 +801,9 @@ cudaError_t k_visc(const MomConsts& k, const double* u, const double* f, double 
     };
     V.mu_face0 = mu_at(0.0);
     V.mu_face1 = mu_at(1.0);
-    if (k.g.D == 3) { viscflux_kern<3><<<grd(k.g), blk(), 0, s>>>(V, Phi6); ia::note_launch(); }
-    else { viscflux_kern<2><<<grd(k.g), blk(), 0, s>>>(V, Phi6); ia::note_launch(); }
-    { viscacc_kern<<<grd(k.g), blk(), 0, s>>>(k.g, Phi6, r); ia::note_launch(); }
+    if (k.g.D == 3) { viscflux_kern<3><<<split_grid(k.g), blk(), 0, s>>>(V, Phi6); ia::note_launch(); }
+    else { viscflux_kern<2><<<split_grid(k.g), blk(), 0, s>>>(V, Phi6); ia::note_launch(); }
+    { viscacc_kern<<<igrd(k.g), blk(), 0, s>>>(k.g, Phi6, r); ia::note_launch(); }
     return cudaGetLastError();
 }
 cudaError_t k_zero(double* a, long long n, cudaStream_t s) {
@@ -780,14 +812,14 @@ cudaError_t k_zero(double* a, long long n, cudaStream_t s) {
 }
 cudaError_t k_surften(const MomConsts& k, int d, const double* f, double eta, double* fb, double* r, cudaStream_t s) {
     { fbuffer_kern<<<grd(k.g), blk(), 0, s>>>(k, d, f, fb); ia::note_launch(); }
-    if (k.g.D == 2) { surften_kern<2><<<grd(k.g), blk(), 0, s>>>(k, d, f, fb, eta, r); ia::note_launch(); }
-    else { surften_kern<3><<<grd(k.g), blk(), 0, s>>>(k, d, f, fb, eta, r); ia::note_launch(); }
+    if (k.g.D == 2) { surften_kern<2><<<igrd(k.g), blk(), 0, s>>>(k, d, f, fb, eta, r); ia::note_launch(); }
+    else { surften_kern<3><<<igrd(k.g), blk(), 0, s>>>(k, d, f, fb, eta, r); ia::note_launch(); }
     return cudaGetLastError();
 }
 cudaError_t k_updateu(const MomConsts& k, double* u, double* rhou, const double* u0, const double* F, double dt,
                       const double* fref, const double* fupd, double w, bool write_rhou, cudaStream_t s) {
     const double a = 1.0 / w - 1.0;
-    { updateu_kern<<<grd(k.g), blk(), 0, s>>>(k, u, rhou, u0, F, dt, fref, fupd, w, a, write_rhou); ia::note_launch(); }
+    { updateu_kern<<<igrd(k.g), blk(), 0, s>>>(k, u, rhou, u0, F, dt, fref, fupd, w, a, write_rhou); ia::note_launch(); }
     return cudaGetLastError();
 }
 cudaError_t k_updatel(const MomConsts& k, double* mu0, const double* f, cudaStream_t s) {
@@ -799,7 +831,7 @@ cudaError_t k_div_scale(const MomConsts& k, const double* u, double* zz, double*
     return cudaGetLastError();
 }
 cudaError_t k_correct(const MomConsts& k, double* u, const double* L, double* xx, double dt, cudaStream_t s) {
-    { correct_kern<<<grd(k.g), blk(), 0, s>>>(k.g, u, L, xx); ia::note_launch(); }
+    { correct_kern<<<igrd(k.g), blk(), 0, s>>>(k.g, u, L, xx); ia::note_launch(); }
     { scale_kern<<<1216, 256, 0, s>>>(xx, k.g.N, 1.0 / dt); ia::note_launch(); }
     return cudaGetLastError();
 }
