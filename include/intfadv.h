@@ -76,6 +76,11 @@ extern "C" {
 #define IA_PRECOND_NONE    2   /* s = r (plain CG; the ablation baseline)               */
 #define IA_PRECOND_VCYCLE  3   /* s = Vcycle(r) (the fallback)                          */
 
+/* Smoother of the FP32 V-cycle (ia_poisson_smoother) */
+#define IA_SMOOTHER_HALFSWEEP 0   /* one launch per red-black half-sweep (the default)    */
+#define IA_SMOOTHER_BLOCKED   1   /* all half-sweeps of a smoothing in one z-wavefront launch
+                                     (3D); same arithmetic                                 */
+
 typedef struct ia_handle ia_handle;
 
 /* Construction parameters: TwoPhaseSimulation / cVOF keywords
@@ -294,6 +299,10 @@ int ia_poisson_precond(ia_handle* h, int32_t precond, int32_t inner_max, double 
  * MultiLevelPoisson settings are WaterLily's): nu1 red-black sweeps before and nu2 after the
  * coarse correction, nuc symmetric sweeps on the coarsest level (defaults 2, 2, 16) */
 int ia_poisson_mg_params(ia_handle* h, int32_t nu1, int32_t nu2, int32_t nuc);
+/* smoother of the FP32 V-cycle (no reference counterpart: the reference smooths in FP64 with
+ * WaterLily's MultiLevelPoisson): IA_SMOOTHER_*.  The blocked smoother is used where it applies
+ * (3D levels, nu1 and nu2 in {1, 2}) and the half-sweeps elsewhere */
+int ia_poisson_smoother(ia_handle* h, int32_t kind);
 /* counters since the handle's creation: [0] net applications, [1] V-cycles, [2] fallbacks
  * to the V-cycle, [3] inner FCG iterations, [4] outer corrections */
 int ia_poisson_stats(ia_handle* h, int64_t* out5);

@@ -28,9 +28,11 @@ __global__ void metrics_k(MetricArgs a, double* __restrict__ partial) {
     const Grid& g = a.g;
     double acc[NQ] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
     const int nxi = g.n[0] - 2, nyi = g.n[1] - 2;
-    const long long rows = (long long)nyi * (g.D == 3 ? g.n[2] - 2 : 1);
-    for (long long rw = blockIdx.x; rw < rows; rw += gridDim.x) {
-        const int y = 1 + int(rw % nyi), z = g.D == 3 ? 1 + int(rw / nyi) : 0;
+    const int rows = nyi * (g.D == 3 ? g.n[2] - 2 : 1);
+    // rows b, b + G, ...: (y, z) advance incrementally
+    const int dy = int(gridDim.x) % nyi, dz = int(gridDim.x) / nyi;
+    int y = 1 + int(blockIdx.x) % nyi, z = (g.D == 3 ? 1 : 0) + int(blockIdx.x) / nyi;
+    for (int rw = blockIdx.x; rw < rows; rw += gridDim.x, y += dy, z += dz + (y > nyi ? 1 : 0), y -= (y > nyi ? nyi : 0)) {
         for (int x = 1 + threadIdx.x; x <= nxi; x += blockDim.x) {
             const long long I = lin(g, x, y, z);
             const double rho = a.lrho + a.one_m * a.f[I];

@@ -488,7 +488,6 @@ __global__ void viscflux_kern(ViscCtx V, double* __restrict__ Phi6) {
 
 __global__ void viscacc_kern(Grid g, const double* __restrict__ Phi6, double* __restrict__ r) {
     ICELL_XYZ
-    const int c[3] = {x, y, z};
     const long long I = lin(g, x, y, z);
     for (int i = 0; i < g.D; ++i) {
         double acc = 0.0;
@@ -620,7 +619,6 @@ __global__ void updateu_kern(MomConsts k, double* __restrict__ u, double* __rest
                              bool write_rhou) {
     const Grid& g = k.g;
     ICELL_XYZ
-    const int c[3] = {x, y, z};
     const long long I = lin(g, x, y, z);
     for (int i = 0; i < g.D; ++i) {
         const long long q = I + i * g.N;
@@ -660,7 +658,6 @@ __global__ void div_scale_kern(Grid g, const double* __restrict__ u, double* __r
 __global__ void correct_kern(Grid g, double* __restrict__ u, const double* __restrict__ L,
                              const double* __restrict__ xx) {
     ICELL_XYZ
-    const int c[3] = {x, y, z};
     const long long I = lin(g, x, y, z);
     for (int i = 0; i < g.D; ++i) u[I + i * g.N] -= L[I + i * g.N] * (xx[I] - xx[I - g.s[i]]);
 }
@@ -698,9 +695,11 @@ __global__ void cfl_kern(Grid g, const double* __restrict__ u, unsigned long lon
     __shared__ unsigned long long s1[32], s2[32];
     unsigned long long a1 = 0ull, a2 = 0ull;
     const int nxi = g.n[0] - 2, nyi = g.n[1] - 2;
-    const long long rows = (long long)nyi * (g.D == 3 ? g.n[2] - 2 : 1);
-    for (long long rw = blockIdx.x; rw < rows; rw += gridDim.x) {
-        const int y = 1 + int(rw % nyi), z = g.D == 3 ? 1 + int(rw / nyi) : 0;
+    const int rows = nyi * (g.D == 3 ? g.n[2] - 2 : 1);
+    // rows b, b + G, ...: (y, z) advance incrementally
+    const int dy = int(gridDim.x) % nyi, dz = int(gridDim.x) / nyi;
+    int y = 1 + int(blockIdx.x) % nyi, z = (g.D == 3 ? 1 : 0) + int(blockIdx.x) / nyi;
+    for (int rw = blockIdx.x; rw < rows; rw += gridDim.x, y += dy, z += dz + (y > nyi ? 1 : 0), y -= (y > nyi ? nyi : 0)) {
         for (int x = 1 + threadIdx.x; x <= nxi; x += blockDim.x) {
             const long long I = lin(g, x, y, z);
             double fo = 0.0, mt = 0.0;

@@ -190,6 +190,196 @@ __global__ void rbgs_pair_k(Grid g, const T* __restrict__ L, const T* __restrict
     const T iD = (dd * dd < T(2) * eps) ? T(0) : T(1) / dd;
     xv[I] = (b[I] - off) * iD;
 }
+
+// ---- temporally blocked red-black Gauss-Seidel (3D, FP32): S half-sweeps in one launch.
+// A block owns a TB_X x TB_Y column of interior cells and a range of z-planes and marches up
+// z as a wavefront: at step t half-sweep s works on plane t - s over the column widened by
+// S-1-s cells on every side, so that half-sweep s+1 finds every neighbour it reads in shared
+// memory (three planes per half-sweep).  The widened parts are recomputed by every block that
+// needs them, from the same inputs with the same arithmetic, so a cell has one value whichever
+// block computes it; only its owner writes it.  Half-sweep s updates colour (c0 + s) & 1 with
+// rbgs_pair_k's sums in rbgs_pair_k's order and the stored inverse diagonal (set_diag_k, the
+// same formula).  A cell ends in x_out with the value of the last half-sweep of its colour.
+// The input is zero (pre-smoothing: the V-cycle starts from x = 0) or x_in plus the injection
+// prolongation of a coarse correction (post-smoothing).  Periodic dimensions wrap the widened
+// column onto the grid (an even number of interior cells keeps the colouring); along a wall
+// the cells outside the interior hold zero and their face coefficients are zero.
+constexpr int TB_X = 32, TB_Y = 16, TB_T = 256;
+
+struct TbArgs {
+    Grid g, gc;            // level, coarse level (prolongation)
+    const float* L;
+    const float* b;
+    const float* iD;
+    const float* xin;      // post-smoothing input (null: start from zero)
+    const float* xc;       // coarse correction added to xin (or null)
+    float* xout;
+    int c0;                // colour of the first half-sweep
+    int zchunk;            // z-planes owned by a block
+};
+
+// grid coordinate of the logical coordinate l along e: periodic images wrap onto the
+// interior, wall cells outside the interior are not valid
+__device__ __forceinline__ int tb_wrap(const Grid& g, int e, int l, bool& ok) {
+    const int m = g.n[e] - 2;
+    if (g.isper(e)) {
+        int p = l;
+        while (p < 1) p += m;
+        while (p > m) p -= m;
+        ok = true;
+        return p;
+    }
+    ok = l >= 1 && l <= m;
+    return l;
+}
+
+__device__ __forceinline__ int tb_slot(int zl) { return (zl + 3 * 64) % 3; }
+
+template <int S, bool ZERO>
+__global__ void __launch_bounds__(TB_T, 4) rbgs_tb_k(TbArgs a) {
+    // frame position (fx, fy) <-> logical cell (ox - S + fx, oy - S + fy).  A frame row is
+    // stored as its even-fx half then its odd-fx half, so that the cells of one colour in a row
+    // are contiguous.  Threads own pairs (2p, 2p+1) of a row: the frame starts on an odd logical
+    // x and every level has an even number of interior cells per dimension, so the two cells of
+    // a pair are both interior or both not, and a periodic wrap never falls between them.
+    constexpr int FX = TB_X + 2 * S, FY = TB_Y + 2 * S, FN = FX * FY, HX = FX / 2;
+    constexpr int RIN = ZERO ? 0 : 1;                 // ring 0 holds the input planes (post)
+    constexpr int NIN = (FN + TB_T - 1) / TB_T;       // input cells per thread
+    constexpr int F_VALID = 1, F_OWNED = 2, F_PAR = 4, F_LO = 8, F_HI = 16, F_USE = 32;
+    __shared__ float ring[RIN + S - 1][3][FN];
+    const Grid& g = a.g;
+    const int tid = threadIdx.x;
+    const int ox = 1 + int(blockIdx.x) * TB_X, oy = 1 + int(blockIdx.y) * TB_Y;
+    const int nzi = g.n[2] - 2;
+    const int z0 = 1 + int(blockIdx.z) * a.zchunk;
+    if (z0 > nzi) return;
+    const int z1 = min(z0 + a.zchunk, nzi + 1);
+    const int s1 = int(g.s[1]), s2 = int(g.s[2]);
+    const float* __restrict__ L0 = a.L;
+    const float* __restrict__ L1 = a.L + g.N;
+    const float* __restrict__ L2 = a.L + 2 * g.N;
+
+    // pair slots of each half-sweep: frame index of the even cell, grid offset (x, y) of the
+    // even cell, flags (valid, owned by this block, (x + y) parity, region edge pairs)
+    int sq[S][2], sxy[S][2], sfl[S][2];
+#pragma unroll
+    for (int s = 0; s < S; ++s) {
+        const int hs = S - 1 - s;
+        const int plo = (S - hs) / 2, phi = (S + TB_X + hs + 1) / 2;
+        const int np = phi - plo, rows = TB_Y + 2 * hs;
+#pragma unroll
+        for (int k = 0; k < 2; ++k) {
+            const int it = tid + k * TB_T;
+            sfl[s][k] = 0;
+            sq[s][k] = 0;
+            sxy[s][k] = 0;
+            if (it >= np * rows) continue;
+            const int r = it / np, p = plo + (it - r * np);
+            const int fy = S - hs + r;
+            const int x0 = ox - S + 2 * p, y = oy - S + fy;
+            bool okx, oky;
+            const int px = tb_wrap(g, 0, x0, okx), py = tb_wrap(g, 1, y, oky);
+            int fl = F_USE | (((x0 + y) & 1) ? F_PAR : 0);
+            if (okx && oky) fl |= F_VALID;
+            if (fy >= S && fy < S + TB_Y && 2 * p >= S && 2 * p < S + TB_X && x0 <= g.n[0] - 2 && y <= g.n[1] - 2)
+                fl |= F_OWNED;
+            if (2 * p < S - hs) fl |= F_LO;                   // only the odd cell is in the region
+            if (2 * p + 1 >= S + TB_X + hs) fl |= F_HI;       // only the even cell is in the region
+            sfl[s][k] = fl;
+            sq[s][k] = fy * FX + p;
+            sxy[s][k] = px + py * s1;
+        }
+    }
+    // input cells of this thread: grid offset (x, y) (-1: outside a wall) and coarse offset
+    int ixy[NIN], icxy[NIN];
+#pragma unroll
+    for (int k = 0; k < NIN; ++k) {
+        const int e = tid + k * TB_T;
+        ixy[k] = -1;
+        icxy[k] = 0;
+        if (ZERO || e >= FN) continue;
+        const int fy = e / FX, fx = e - fy * FX;
+        bool okx, oky;
+        const int px = tb_wrap(g, 0, ox - S + fx, okx), py = tb_wrap(g, 1, oy - S + fy, oky);
+        if (okx && oky) {
+            ixy[k] = px + py * s1;
+            icxy[k] = (px + 1) / 2 + ((py + 1) / 2) * int(a.gc.s[1]);
+        }
+    }
+
+    auto stage_in = [&](int zl) {
+        bool okz;
+        const int pz = tb_wrap(g, 2, zl, okz);
+        float* dst = ring[0][tb_slot(zl)];
+        const int cz = ((pz + 1) / 2) * int(a.gc.s[2]);
+#pragma unroll
+        for (int k = 0; k < NIN; ++k) {
+            const int e = tid + k * TB_T;
+            if (e >= FN) continue;
+            float v = 0.f;
+            if (okz && ixy[k] >= 0) {
+                v = a.xin[ixy[k] + pz * s2];
+                if (a.xc) v += a.xc[icxy[k] + cz];
+            }
+            const int fy = e / FX, fx = e - fy * FX;
+            dst[fy * FX + (fx & 1) * HX + (fx >> 1)] = v;
+        }
+    };
+
+    const int T0 = z0 - S + 1, T1 = z1 + S - 2;
+    if (!ZERO) {
+        stage_in(T0 - 1);
+        stage_in(T0);
+    }
+    for (int t = T0; t <= T1; ++t) {
+        if (!ZERO) stage_in(t + 1);
+        __syncthreads();
+#pragma unroll
+        for (int s = 0; s < S; ++s) {
+            if (t >= T0 + 2 * s) {
+                const int zl = t - s;
+                const int col = (a.c0 + s) & 1;
+                bool okz;
+                const int pz = tb_wrap(g, 2, zl, okz);
+                const bool own_z = zl >= z0 && zl < z1;
+                const int zo = pz * s2;
+                float* outp = ZERO ? ring[s < S - 1 ? s : 0][tb_slot(zl)] : ring[s < S - 1 ? s + 1 : 0][tb_slot(zl)];
+                const int pin = ZERO ? (s > 0 ? s - 1 : 0) : s;
+                const float* pc = ring[pin][tb_slot(zl)];
+                const float* pd = ring[pin][tb_slot(zl - 1)];
+                const float* pu = ring[pin][tb_slot(zl + 1)];
+#pragma unroll
+                for (int k = 0; k < 2; ++k) {
+                    const int fl = sfl[s][k];
+                    if (!(fl & F_USE)) continue;
+                    const int e = ((fl & F_PAR ? 1 : 0) + zl + col) & 1;   // which cell of the pair
+                    if ((fl & F_LO) && e == 0) continue;
+                    if ((fl & F_HI) && e == 1) continue;
+                    const int q = sq[s][k] + e * HX;
+                    float v = 0.f;
+                    if ((fl & F_VALID) && okz) {
+                        const int I = sxy[s][k] + e + zo;
+                        if (ZERO && s == 0) {
+                            v = a.b[I] * a.iD[I];
+                        } else {
+                            const int qxl = q + (e ? -HX : HX - 1);
+                            const float vxl = pc[qxl], vxh = pc[qxl + 1];
+                            const float vyl = pc[q - FX], vyh = pc[q + FX];
+                            const float vzl = pd[q], vzh = pu[q];
+                            float off = L0[I] * vxl + L0[I + 1] * vxh;
+                            off += L1[I] * vyl + L1[I + s1] * vyh;
+                            off += L2[I] * vzl + L2[I + s2] * vzh;
+                            v = (a.b[I] - off) * a.iD[I];
+                        }
+                        if (s >= S - 2 && (fl & F_OWNED) && own_z) a.xout[I] = v;
+                    }
+                    if (s < S - 1) outp[q] = v;
+                }
+            }
+            __syncthreads();
+        }
+    }
+}
 inline dim3 pair_grid(const Grid& g) {
     const int pairs = (g.n[0] - 2 + 1) / 2;
     return dim3((pairs + 31) / 32, (g.n[1] - 2 + 7) / 8, g.D == 3 ? g.n[2] - 2 : 1);
@@ -297,12 +487,18 @@ __global__ void to_f64_k(long long n, const float* __restrict__ a, double* __res
 constexpr int KTHREADS = 256;
 constexpr int KBLOCKS = 1216;   // 8 blocks on each of 152 SMs
 
+// Row loops: block b takes rows b, b + G, b + 2G, ... (G blocks) of the interior; the row's
+// (y, z) advance incrementally (a grid holds < 2^31 cells, so 32-bit row numbers suffice)
+#define ROWS_FOR(g, DD)                                                                              \
+    const int nxi_ = (g).n[0] - 2, nyi_ = (g).n[1] - 2;                                              \
+    const int nrows_ = nyi_ * ((DD) == 3 ? (g).n[2] - 2 : 1);                                        \
+    const int dy_ = int(gridDim.x) % nyi_, dz_ = int(gridDim.x) / nyi_;                              \
+    int y = 1 + int(blockIdx.x) % nyi_, z = ((DD) == 3 ? 1 : 0) + int(blockIdx.x) / nyi_;           \
+    for (int rw_ = blockIdx.x; rw_ < nrows_;                                                         \
+         rw_ += gridDim.x, y += dy_, z += dz_ + (y > nyi_ ? 1 : 0), y -= (y > nyi_ ? nyi_ : 0))
 #define ROWS_BEGIN(g)                                                                      \
     {                                                                                      \
-        const int nxi_ = (g).n[0] - 2, nyi_ = (g).n[1] - 2;                                \
-        const long long nrows_ = (long long)nyi_ * ((g).D == 3 ? (g).n[2] - 2 : 1);        \
-        for (long long rw_ = blockIdx.x; rw_ < nrows_; rw_ += gridDim.x) {                 \
-            const int y = 1 + int(rw_ % nyi_), z = (g).D == 3 ? 1 + int(rw_ / nyi_) : 0;   \
+        ROWS_FOR(g, (g).D) {                                                               \
             for (int x = 1 + threadIdx.x; x <= nxi_; x += blockDim.x) {                    \
                 const int c[3] = {x, y, z};                                                \
                 const long long I = lin(g, x, y, z);
@@ -314,11 +510,8 @@ constexpr int KBLOCKS = 1216;   // 8 blocks on each of 152 SMs
 // the same with a 32-bit cell index and the dimension fixed at compile time
 #define ROWS_BEGIN_D(g)                                                                    \
     {                                                                                      \
-        const int nxi_ = (g).n[0] - 2, nyi_ = (g).n[1] - 2;                                \
         const int s1_ = int((g).s[1]), s2_ = int((g).s[2]);                                \
-        const long long nrows_ = (long long)nyi_ * (D == 3 ? (g).n[2] - 2 : 1);            \
-        for (long long rw_ = blockIdx.x; rw_ < nrows_; rw_ += gridDim.x) {                 \
-            const int y = 1 + int(rw_ % nyi_), z = D == 3 ? 1 + int(rw_ / nyi_) : 0;       \
+        ROWS_FOR(g, D) {                                                                   \
             const int row_ = y * s1_ + z * s2_;                                            \
             for (int x = 1 + threadIdx.x; x <= nxi_; x += blockDim.x) {                    \
                 const int I = row_ + x;
@@ -590,17 +783,85 @@ __global__ void zero_k(long long n, T* a) {
 
 // ------------------------------------------------------------------ host side
 
+// z-planes per block of the blocked smoother: about eight blocks per multiprocessor in all,
+// each block marching at least 4 S planes
+static int tb_zchunk(const Grid& g, int S, int nsm) {
+    const int tiles = ((g.n[0] - 2 + TB_X - 1) / TB_X) * ((g.n[1] - 2 + TB_Y - 1) / TB_Y);
+    const int nzi = g.n[2] - 2;
+    const int want = std::max(1, (8 * std::max(nsm, 1)) / std::max(tiles, 1));
+    int zc = (nzi + want - 1) / want;
+    zc = std::max(zc, std::min(nzi, 4 * S));
+    return std::max(zc, 1);
+}
+
+// the blocked smoother runs the FP32 V-cycle of a 3D level with an even number of interior
+// cells in every dimension (every level but the coarsest), for nu1, nu2 in {1, 2}
+static bool tb_usable(const PoissonMG* mg, const Grid& g) {
+    if (mg->smoother != IA_SMOOTHER_BLOCKED || g.D != 3) return false;
+    if (mg->nu1 < 1 || mg->nu1 > 2 || mg->nu2 < 1 || mg->nu2 > 2) return false;
+    for (int e = 0; e < 3; ++e)
+        if ((g.n[e] - 2) % 2 != 0) return false;
+    return true;
+}
+
+static void tb_launch(const PoissonMG* mg, const TbArgs& a, int S, cudaStream_t st) {
+    TbArgs b = a;
+    b.zchunk = tb_zchunk(a.g, S, mg->nsm);
+    const dim3 grid((a.g.n[0] - 2 + TB_X - 1) / TB_X, (a.g.n[1] - 2 + TB_Y - 1) / TB_Y,
+                    (a.g.n[2] - 2 + b.zchunk - 1) / b.zchunk);
+    const bool zero = a.xin == nullptr;
+    if (S == 4) {
+        if (zero) rbgs_tb_k<4, true><<<grid, TB_T, 0, st>>>(b);
+        else rbgs_tb_k<4, false><<<grid, TB_T, 0, st>>>(b);
+    } else {
+        if (zero) rbgs_tb_k<2, true><<<grid, TB_T, 0, st>>>(b);
+        else rbgs_tb_k<2, false><<<grid, TB_T, 0, st>>>(b);
+    }
+    ia::note_launch();
+}
+
 template <class T>
 static cudaError_t vcycle(ia_handle* h, PoissonMG* mg, int l, cudaStream_t st, int nu1, int nu2, int nuc) {
     auto& L = mg->lev[l];
     T* x = L.template x_<T>();
     T* b = L.template b_<T>();
-    T* r = L.template r_<T>();
     const T* Lc = L.template L_<T>();
     const T* iD = L.template iD_<T>();
     if (l == mg->nlev - 1) {
         { coarse_k<T><<<1, 1024, 0, st>>>(L.g, Lc, iD, b, x, nuc); ia::note_launch(); }
         return cudaGetLastError();
+    }
+    if constexpr (sizeof(T) == 4) {
+        if (tb_usable(mg, L.g)) {
+            // pre-smoothing from zero into the level's scratch vector, residual restriction
+            // from it, then post-smoothing of scratch + prolongated correction into x
+            auto& C = mg->lev[l + 1];
+            TbArgs ta;
+            ta.g = L.g;
+            ta.gc = C.g;
+            ta.L = Lc;
+            ta.b = b;
+            ta.iD = iD;
+            ta.xin = nullptr;
+            ta.xc = nullptr;
+            ta.xout = L.r32;
+            ta.c0 = 0;
+            ta.zchunk = 1;
+            int tk = (l == 0) ? timing_begin(h, TK_MG_FINE) : -1;
+            tb_launch(mg, ta, 2 * nu1, st);
+            timing_end(h, tk);
+            { resid_restrict_k<T, 3><<<cell_grid(C.g), blk(), 0, st>>>(C.g, L.g, Lc, b, L.r32, C.template b_<T>()); ia::note_launch(); }
+            cudaError_t e = vcycle<T>(h, mg, l + 1, st, nu1, nu2, nuc);
+            if (e != cudaSuccess) return e;
+            ta.xin = L.r32;
+            ta.xc = C.x32;
+            ta.xout = x;
+            ta.c0 = 1;
+            tk = (l == 0) ? timing_begin(h, TK_MG_FINE) : -1;
+            tb_launch(mg, ta, 2 * nu2, st);
+            timing_end(h, tk);
+            return cudaGetLastError();
+        }
     }
     auto half = [&](int color) {
         const int tk = (l == 0) ? timing_begin(h, TK_MG_FINE) : -1;
@@ -633,7 +894,7 @@ static cudaError_t vcycle_run(ia_handle* h, PoissonMG* mg, cudaStream_t st) {
     if (h->timing.on) return vcycle<T>(h, mg, 0, st, mg->nu1, mg->nu2, mg->nuc);
     const int k = sizeof(T) == 4 ? 0 : 1;
     int* nu = mg->vgraph_nu[k];
-    if (mg->vgraph[k] && (nu[0] != mg->nu1 || nu[1] != mg->nu2 || nu[2] != mg->nuc)) {
+    if (mg->vgraph[k] && (nu[0] != mg->nu1 || nu[1] != mg->nu2 || nu[2] != mg->nuc || nu[3] != mg->smoother)) {
         cudaGraphExecDestroy(mg->vgraph[k]);
         mg->vgraph[k] = nullptr;
     }
@@ -661,6 +922,7 @@ static cudaError_t vcycle_run(ia_handle* h, PoissonMG* mg, cudaStream_t st) {
         nu[0] = mg->nu1;
         nu[1] = mg->nu2;
         nu[2] = mg->nuc;
+        nu[3] = mg->smoother;
     }
     note_launches(mg->vgraph_kernels[k]);
     return cudaGraphLaunch(mg->vgraph[k], st);
@@ -758,6 +1020,11 @@ int mg_create(ia_handle* h) {
     mg->nu1 = 2;
     mg->nu2 = 2;
     mg->nuc = 16;
+    {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&mg->nsm, cudaDevAttrMultiProcessorCount, dev);
+    }
     return IA_OK;
 }
 

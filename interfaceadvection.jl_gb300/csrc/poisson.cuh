@@ -51,12 +51,14 @@ struct PoissonMG {
     double* dsc = nullptr;                                            // device scalars
     double* hsc = nullptr;                                            // pinned host scalars
     int nu1 = 2, nu2 = 2, nuc = 16;
+    int smoother = 0;                                                 // IA_SMOOTHER_* (FP32 V-cycle)
+    int nsm = 0;                                                      // multiprocessors of the device
     // each precision's finest-level V-cycle is captured once into a CUDA graph (its launch
     // sequence and arguments are fixed for the handle) and replayed; recaptured when the
     // smoothing parameters change
     cudaGraphExec_t vgraph[2] = {nullptr, nullptr};   // FP32, FP64
     long long vgraph_kernels[2] = {0, 0};
-    int vgraph_nu[2][3] = {{0, 0, 0}, {0, 0, 0}};
+    int vgraph_nu[2][4] = {{0, 0, 0, 0}, {0, 0, 0, 0}};
     cudaStream_t capture = nullptr;
 };
 

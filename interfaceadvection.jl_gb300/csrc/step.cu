@@ -309,6 +309,13 @@ int ia_poisson_mg_params(ia_handle* h, int32_t nu1, int32_t nu2, int32_t nuc) {
     return IA_OK;
 }
 
+int ia_poisson_smoother(ia_handle* h, int32_t kind) {
+    if (!h || (kind != IA_SMOOTHER_HALFSWEEP && kind != IA_SMOOTHER_BLOCKED)) return IA_ERR_INVALID;
+    if (ensure_scratch(h) != IA_OK) return IA_ERR_CUDA;
+    h->mg->smoother = kind;
+    return IA_OK;
+}
+
 int ia_poisson_stats(ia_handle* h, int64_t* out5) {
     if (!h || !out5) return IA_ERR_INVALID;
     for (int i = 0; i < 5; ++i) out5[i] = h->mg ? h->mg->stats[i] : 0;

@@ -31,6 +31,7 @@ LIMITERS = {"Koren": 0, "upwind": 1, "minmod": 2, "vanAlbada1": 3, "Sweby": 4, "
             "TVDcen": 6, "TVDdown": 7}
 POISSON_MODES = {"fp64": 0, "mixed": 1, "learned": 2}
 PRECONDS = {"hybrid": 0, "net": 1, "none": 2, "vcycle": 3}
+SMOOTHERS = {"halfsweep": 0, "blocked": 1}
 TIMED_KERNELS = ["vof_bulk", "vof_cells", "ustar", "forcing", "mg_vcycle", "mg_residual", "mg_transfer",
                  "krylov", "other", "vof_faces", "momflux", "momupdate", "update_project", "mg_fine_rbgs", "nn_precond"]
 
@@ -91,6 +92,7 @@ _SIGS = {
     "ia_poisson_precond": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.c_double]),
     "ia_poisson_stats": (C.c_int, [C.c_void_p, C.c_void_p]),
     "ia_poisson_mg_params": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.c_int32]),
+    "ia_poisson_smoother": (C.c_int, [C.c_void_p, C.c_int32]),
     "ia_poisson_residual": (C.c_int, [C.c_void_p] * 5 + [C.POINTER(C.c_double)]),
     "ia_metrics": (C.c_int, [C.c_void_p] * 8),
     "ia_levelset_init": (C.c_int, [C.c_void_p] * 4),

@@ -101,6 +101,12 @@ def set_learned(handle, precond="hybrid", weights=None, inner_max=30, inner_rtol
                            int(inner_max), float(inner_rtol)), "ia_poisson_precond")
 
 
+def set_smoother(handle, kind: str = "halfsweep") -> None:
+    """Smoother of the FP32 V-cycle: "halfsweep" (one launch per red-black half-sweep, the default)
+    or "blocked" (all half-sweeps of a smoothing in one z-wavefront launch); same arithmetic."""
+    _lib.check(handle.call("ia_poisson_smoother", _lib.SMOOTHERS[kind]), "ia_poisson_smoother")
+
+
 def poisson_stats(handle) -> dict:
     """Counters of the Poisson solver: net applications, V-cycles, fallbacks, inner and outer iterations."""
     out = (C.c_int64 * 5)()

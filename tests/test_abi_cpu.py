@@ -54,6 +54,8 @@ def test_config_validation_is_host_side(lib):
     cfg = core.make_config((8, 8), exitBC=True)
     assert lib.ia_create(C.byref(cfg), C.byref(C.c_void_p())) == _lib.IA_ERR_UNSUPPORTED
     assert lib.ia_advect_vof(None, None, None, None, 0.1, 1, None) == _lib.IA_ERR_INVALID
+    assert lib.ia_poisson_smoother(None, _lib.SMOOTHERS["blocked"]) == _lib.IA_ERR_INVALID
+    assert lib.ia_poisson_mg_params(None, 2, 2, 16) == _lib.IA_ERR_INVALID
 
 
 def test_split_order_matches_reference():

@@ -1,0 +1,69 @@
+"""GPU checks of the FP32 V-cycle smoothers.
+
+The blocked smoother (all half-sweeps of a smoothing in one z-wavefront launch,
+with the widened tile recomputed in shared memory) does the half-sweep kernels'
+arithmetic in their order, so a mixed-precision solve must take the same
+iterations and land on the same pressure whichever smoother runs, on periodic
+and wall dimensions, on sizes that are not multiples of the 32 x 16 tile and
+on every level of the hierarchy.
+"""
+import ctypes as C
+
+import numpy as np
+import pytest
+import torch
+
+import intfadv as ia
+from intfadv import _lib, learned
+from intfadv.fields import fzeros, ptr
+
+pytestmark = pytest.mark.gpu
+
+
+def system(dims, perdir):
+    """Face coefficients and right-hand side of a bubbly pressure system (after one step)."""
+    N = min(dims)
+    sim = ia.TwoPhaseSimulation(dims, (0.0, 0.0, 0.0), float(N), perdir=perdir, λρ=1e-3, λμ=1e-2, ν=0.01,
+                                η=0.02, g=(0.0, -1e-3, 0.0),
+                                InterfaceSDF=learned.bubbles_sdf(learned.bubble_layout(1003, N)),
+                                poisson="mixed", poisson_tol=1e-9, poisson_itmx=300)
+    ia.sim_step(sim)
+    return sim.flow.mu0.clone(), sim.flow.sigma.clone()
+
+
+def solve(dims, perdir, L, z, smoother, nu=(2, 2)):
+    h = ia.Handle(ia.make_config(dims, perdir=perdir, poisson="mixed", lrho=1e-3))
+    ia.set_smoother(h, smoother)
+    _lib.check(h.call("ia_poisson_mg_params", nu[0], nu[1], 16), "ia_poisson_mg_params")
+    x = fzeros(z.shape)
+    it, res = C.c_int32(), C.c_double()
+    _lib.check(h.call("ia_poisson_solve", ptr(x), ptr(z), ptr(L), 1e-8, 2000, C.byref(it), C.byref(res)),
+               "ia_poisson_solve")
+    return x, it.value, res.value, ia.poisson_stats(h)
+
+
+@pytest.mark.parametrize("dims,perdir", [((32, 32, 32), (0, 2)), ((40, 24, 36), ()), ((48, 40, 24), (0, 1, 2))])
+@pytest.mark.parametrize("nu", [(2, 2), (1, 1), (1, 2)])
+def test_blocked_smoother_matches_halfsweeps(cuda, dims, perdir, nu):
+    L, z = system(dims, perdir)
+    xa, ita, resa, sta = solve(dims, perdir, L, z, "halfsweep", nu)
+    xb, itb, resb, stb = solve(dims, perdir, L, z, "blocked", nu)
+    assert resa <= 1e-8 and resb <= 1e-8
+    assert abs(ita - itb) <= 1, (ita, itb)
+    assert sta["vcycles"] > 0 and stb["vcycles"] > 0
+    xi = lambda x: x[1:-1, 1:-1, 1:-1] - x[1:-1, 1:-1, 1:-1].mean()
+    e = float((xi(xa) - xi(xb)).abs().max() / xi(xa).abs().max())
+    assert e < 1e-6, e
+
+
+def test_blocked_smoother_is_deterministic(cuda):
+    dims, perdir = (32, 32, 32), (0, 2)
+    L, z = system(dims, perdir)
+    x1, it1, _, _ = solve(dims, perdir, L, z, "blocked")
+    x2, it2, _, _ = solve(dims, perdir, L, z, "blocked")
+    assert it1 == it2 and torch.equal(x1, x2)
+
+
+def test_smoother_switch_rejects_unknown_kind(cuda):
+    h = ia.Handle(ia.make_config((16, 16, 16), poisson="mixed"))
+    assert h.call("ia_poisson_smoother", 7) == _lib.IA_ERR_INVALID
