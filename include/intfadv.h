@@ -251,9 +251,12 @@ int ia_metrics(ia_handle* h, const double* u, const double* f, const double* ome
  * roofline figures (no reference counterpart: instrumentation only).
  * Folds finished records into per-family totals, copies the first n totals
  * (milliseconds, launch counts; families: 0 VOF bulk sweep, 1 VOF list sweep,
- * 2 momentum sweep, 3 forcing/update, 4 MG smoother, 5 MG residual,
- * 6 MG transfer, 7 Krylov vector ops, 8 other), then, if enable >= 0, resets
- * the totals and switches recording on (1) or off (0). */
+ * 2 momentum sweep, 3 forcing/update, 4 MG V-cycle, 5 MG residual,
+ * 6 MG transfer, 7 Krylov vector ops, 8 other, 9 VOF faces, 10 momentum flux,
+ * 11 momentum update, 12 update/projection, 13 finest-level red-black
+ * half-sweeps, 14 learned preconditioner, 15 finest-level first half-sweeps),
+ * then, if enable >= 0, resets the totals and switches recording on (1) or
+ * off (0). */
 int ia_timing(ia_handle* h, int32_t enable, double* ms_out, int64_t* launches_out, int32_t n);
 
 /* Number of CUDA kernels this library has launched in the process so far

@@ -10,7 +10,7 @@
 // Kernel families timed by the optional per-launch event instrumentation.
 enum TimedKernel { TK_VOF_BULK = 0, TK_VOF_LIST = 1, TK_MOM = 2, TK_FORCE = 3, TK_MG_SMOOTH = 4,
                    TK_MG_RESID = 5, TK_MG_TRANSFER = 6, TK_KRYLOV = 7, TK_OTHER = 8, TK_VOF_FACES = 9,
-                   TK_MOM_FLUX = 10, TK_MOM_UPDATE = 11, TK_UPDATE = 12, TK_MG_FINE = 13, TK_NN = 14,
+                   TK_MOM_FLUX = 10, TK_MOM_UPDATE = 11, TK_UPDATE = 12, TK_MG_FINE = 13, TK_NN = 14, TK_MG_FIRST = 15,
                    TK_COUNT = 16 };
 
 struct Timing {

@@ -19,7 +19,6 @@ namespace ia {
 namespace {
 
 inline dim3 blk() { return dim3(32, 8, 1); }
-inline dim3 grd(const Grid& g) { return dim3((g.n[0] + 31) / 32, (g.n[1] + 7) / 8, g.n[2]); }
 
 // Interior-cell launch: lane 0 of the first block sits on cell 1, so a row of 32k interior
 // cells fills k warps exactly and no warp spends FP64 issue slots on a ghost-cell lane.
@@ -31,6 +30,24 @@ inline dim3 igrd(const Grid& g) {
     const int y = 1 + blockIdx.y * blockDim.y + threadIdx.y;                          \
     const int z = g.D == 3 ? 1 + int(blockIdx.z) : 0;                                 \
     if (x > g.n[0] - 2 || y > g.n[1] - 2) return;
+
+// Whole-grid launch: the x-range [1, n-2] one cell per lane, then one more block column whose
+// first warp takes the ghost cells x = 0 and x = n-1 of the block's 8 rows, so that a row of
+// 32k interior cells fills k warps and no warp of FP64 work runs with two lanes.
+inline dim3 ggrd(const Grid& g) { return dim3((g.n[0] - 2 + 31) / 32 + 1, (g.n[1] + 7) / 8, g.n[2]); }
+#define GCELL_XYZ                                                                     \
+    int x, y;                                                                         \
+    const int z = blockIdx.z;                                                         \
+    if (blockIdx.x + 1 < gridDim.x) {                                                 \
+        x = 1 + int(blockIdx.x) * 32 + int(threadIdx.x);                              \
+        y = int(blockIdx.y) * 8 + int(threadIdx.y);                                   \
+        if (x > g.n[0] - 2) return;                                                   \
+    } else {                                                                          \
+        if (threadIdx.y != 0 || threadIdx.x >= 16) return;                            \
+        x = (threadIdx.x & 1) ? g.n[0] - 1 : 0;                                       \
+        y = int(blockIdx.y) * 8 + (int(threadIdx.x) >> 1);                            \
+    }                                                                                 \
+    if (y >= g.n[1]) return;
 
 // Face-flux launch (momentum flux, viscous flux): the x-range [3, n-3], whose faces and
 // edges need no boundary rule, one cell per lane; then one more block column whose first
@@ -56,11 +73,6 @@ inline dim3 split_grid(const Grid& g) {
         y = int(blockIdx.y) * 8 + (int(threadIdx.x) >> 2);                            \
     }                                                                                 \
     if (y >= g.n[1]) return;
-
-#define CELL_XYZ                                                                                   \
-    const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y; \
-    const int z = blockIdx.z;                                                                      \
-    if (x >= g.n[0] || y >= g.n[1]) return;
 
 // x / getρ and x · getρ for a face between cells with fractions fa, fb (src/VOFutil.jl:176,
 // 198-201).  The mixed-face forms stay out of line: inlined, they are if-converted and their
@@ -88,7 +100,7 @@ __device__ __forceinline__ double mul_rho(const MomConsts& k, double v, double f
 __global__ void ustar_kern(MomConsts k, const double* __restrict__ rhou, const double* __restrict__ f,
                            double* __restrict__ us) {
     const Grid& g = k.g;
-    CELL_XYZ
+    GCELL_XYZ
     const long long O = lin(g, x, y, z);
     for (int i = 0; i < g.D; ++i) {
         int c[3] = {x, y, z};
@@ -104,7 +116,7 @@ __global__ void ustar_kern(MomConsts k, const double* __restrict__ rhou, const d
 __global__ void u2rhou_kern(MomConsts k, double* __restrict__ rhou, const double* __restrict__ u,
                             const double* __restrict__ f) {
     const Grid& g = k.g;
-    CELL_XYZ
+    GCELL_XYZ
     const int c[3] = {x, y, z};
     if (!is_interior(g, c)) return;
     const long long I = lin(g, x, y, z);
@@ -125,7 +137,7 @@ __device__ __forceinline__ void bcvel_cell(const Grid& g, double* a, const doubl
 
 __global__ void bcvel_kern(MomConsts k, double* a, double A0, double A1, double A2) {
     const Grid& g = k.g;
-    CELL_XYZ
+    GCELL_XYZ
     const int c0[3] = {x, y, z};
     const double A[3] = {A0, A1, A2};
     bcvel_cell(g, a, A, c0);
@@ -507,7 +519,7 @@ __global__ void zero_kern(double* a, long long n) {
 // ------------------------------------------------------------------ surface tension
 __global__ void fbuffer_kern(MomConsts k, int d, const double* __restrict__ f, double* __restrict__ fb) {
     const Grid& g = k.g;
-    CELL_XYZ
+    GCELL_XYZ
     int c[3] = {x, y, z};
     // BCf!(d, ·): the high ghost along a zero-gradient d is not written by the
     // reference (it keeps older buffer contents); it is taken as a zero-gradient copy here.
@@ -633,7 +645,7 @@ __global__ void updateu_kern(MomConsts k, double* __restrict__ u, double* __rest
 
 __global__ void updatel_kern(MomConsts k, double* __restrict__ mu0, const double* __restrict__ f) {
     const Grid& g = k.g;
-    CELL_XYZ
+    GCELL_XYZ
     const long long O = lin(g, x, y, z);
     for (int i = 0; i < g.D; ++i) {
         int c[3] = {x, y, z};
@@ -645,7 +657,7 @@ __global__ void updatel_kern(MomConsts k, double* __restrict__ mu0, const double
 
 __global__ void div_scale_kern(Grid g, const double* __restrict__ u, double* __restrict__ zz,
                                double* __restrict__ xx, double dt) {
-    CELL_XYZ
+    GCELL_XYZ
     const long long I = lin(g, x, y, z);
     xx[I] *= dt;
     const int c[3] = {x, y, z};
@@ -735,15 +747,15 @@ __global__ void cfl_kern(Grid g, const double* __restrict__ u, unsigned long lon
 }  // namespace
 
 cudaError_t k_ustar(const MomConsts& k, const double* rhou, const double* f, double* ustar, cudaStream_t s) {
-    { ustar_kern<<<grd(k.g), blk(), 0, s>>>(k, rhou, f, ustar); ia::note_launch(); }
+    { ustar_kern<<<ggrd(k.g), blk(), 0, s>>>(k, rhou, f, ustar); ia::note_launch(); }
     return cudaGetLastError();
 }
 cudaError_t k_u2rhou(const MomConsts& k, double* rhou, const double* u, const double* f, cudaStream_t s) {
-    { u2rhou_kern<<<grd(k.g), blk(), 0, s>>>(k, rhou, u, f); ia::note_launch(); }
+    { u2rhou_kern<<<ggrd(k.g), blk(), 0, s>>>(k, rhou, u, f); ia::note_launch(); }
     return cudaGetLastError();
 }
 cudaError_t k_bc_vel(const MomConsts& k, double* a, const double* A, cudaStream_t s) {
-    { bcvel_kern<<<grd(k.g), blk(), 0, s>>>(k, a, A[0], A[1], A[2]); ia::note_launch(); }
+    { bcvel_kern<<<ggrd(k.g), blk(), 0, s>>>(k, a, A[0], A[1], A[2]); ia::note_launch(); }
     return cudaGetLastError();
 }
 cudaError_t k_momflux(const MomConsts& k, int j, int limiter, const double* ustar, const double* rhouf_j,
@@ -810,7 +822,7 @@ cudaError_t k_zero(double* a, long long n, cudaStream_t s) {
     return cudaGetLastError();
 }
 cudaError_t k_surften(const MomConsts& k, int d, const double* f, double eta, double* fb, double* r, cudaStream_t s) {
-    { fbuffer_kern<<<grd(k.g), blk(), 0, s>>>(k, d, f, fb); ia::note_launch(); }
+    { fbuffer_kern<<<ggrd(k.g), blk(), 0, s>>>(k, d, f, fb); ia::note_launch(); }
     if (k.g.D == 2) { surften_kern<2><<<igrd(k.g), blk(), 0, s>>>(k, d, f, fb, eta, r); ia::note_launch(); }
     else { surften_kern<3><<<igrd(k.g), blk(), 0, s>>>(k, d, f, fb, eta, r); ia::note_launch(); }
     return cudaGetLastError();
@@ -822,11 +834,11 @@ cudaError_t k_updateu(const MomConsts& k, double* u, double* rhou, const double*
     return cudaGetLastError();
 }
 cudaError_t k_updatel(const MomConsts& k, double* mu0, const double* f, cudaStream_t s) {
-    { updatel_kern<<<grd(k.g), blk(), 0, s>>>(k, mu0, f); ia::note_launch(); }
+    { updatel_kern<<<ggrd(k.g), blk(), 0, s>>>(k, mu0, f); ia::note_launch(); }
     return cudaGetLastError();
 }
 cudaError_t k_div_scale(const MomConsts& k, const double* u, double* zz, double* xx, double dt, cudaStream_t s) {
-    { div_scale_kern<<<grd(k.g), blk(), 0, s>>>(k.g, u, zz, xx, dt); ia::note_launch(); }
+    { div_scale_kern<<<ggrd(k.g), blk(), 0, s>>>(k.g, u, zz, xx, dt); ia::note_launch(); }
     return cudaGetLastError();
 }
 cudaError_t k_correct(const MomConsts& k, double* u, const double* L, double* xx, double dt, cudaStream_t s) {

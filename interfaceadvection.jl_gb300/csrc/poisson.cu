@@ -191,6 +191,60 @@ __global__ void rbgs_pair_k(Grid g, const T* __restrict__ L, const T* __restrict
     xv[I] = (b[I] - off) * iD;
 }
 
+// ---- first half-sweep of a smoothing, fused with the pass before it.  A red update reads only
+// black neighbours, so the red values that precede a smoothing's first (black) half-sweep are
+// consumed by that half-sweep alone: they are computed here where read, b (1/D) for the
+// pre-smoothing from x = 0 (the first red sweep, whose neighbours are zero) and x + the
+// injected coarse correction for the post-smoothing (prolong_k's values, interior cells only).  The red cells are written only for
+// a pre-smoothing of one sweep (write_red), whose red values are part of its result.
+template <class T, bool PROL>
+__device__ __forceinline__ T first_nb(const Grid& g, const Grid& gc, const T* __restrict__ b,
+                                      const T* __restrict__ iD, const T* __restrict__ xc, const T* xv, int J,
+                                      int cx, int cy, int cz) {
+    // J, (cx, cy, cz): index and (periodically wrapped) coordinates of the neighbour
+    const bool in = cx >= 1 && cx <= g.n[0] - 2 && cy >= 1 && cy <= g.n[1] - 2 &&
+                    (g.D == 2 || (cz >= 1 && cz <= g.n[2] - 2));
+    if (!in) return xv[J];
+    if (PROL) return xv[J] + xc[lin(gc, (cx + 1) / 2, (cy + 1) / 2, g.D == 3 ? (cz + 1) / 2 : 0)];
+    return b[J] * iD[J];
+}
+
+template <class T, int D, bool PROL>
+__global__ void rbgs_first_k(Grid g, Grid gc, const T* __restrict__ L, const T* __restrict__ b,
+                             const T* __restrict__ iD, const T* __restrict__ xc, T* __restrict__ xv, int write_red) {
+    const int y = 1 + blockIdx.y * blockDim.y + threadIdx.y;
+    const int z = D == 3 ? 1 + int(blockIdx.z) : 0;
+    if (y > g.n[1] - 2) return;
+    const int x0 = 1 + 2 * (blockIdx.x * blockDim.x + threadIdx.x);
+    const bool blk0 = ((x0 + y + z) & 1) == 1;
+    const int x = blk0 ? x0 : x0 + 1, xr = blk0 ? x0 + 1 : x0;   // black and red cell of the pair
+    const int s1 = int(g.s[1]), s2 = int(g.s[2]);
+    if (!PROL && write_red && xr <= g.n[0] - 2) {
+        const int Ir = xr + y * s1 + z * s2;
+        xv[Ir] = b[Ir] * iD[Ir];
+    }
+    if (x > g.n[0] - 2) return;
+    const int I = x + y * s1 + z * s2;
+    const Nb o = nb_of<D>(g, x, y, z);
+    const int xl = (g.isper(0) && x == 1) ? g.n[0] - 2 : x - 1, xh = (g.isper(0) && x == g.n[0] - 2) ? 1 : x + 1;
+    const int yl = (g.isper(1) && y == 1) ? g.n[1] - 2 : y - 1, yh = (g.isper(1) && y == g.n[1] - 2) ? 1 : y + 1;
+    const T* L1 = L + g.N;
+    T a = L[I] * first_nb<T, PROL>(g, gc, b, iD, xc, xv, I + o.xl, xl, y, z) +
+          L[I + 1] * first_nb<T, PROL>(g, gc, b, iD, xc, xv, I + o.xh, xh, y, z);
+    a += L1[I] * first_nb<T, PROL>(g, gc, b, iD, xc, xv, I + o.yl, x, yl, z) +
+         L1[I + s1] * first_nb<T, PROL>(g, gc, b, iD, xc, xv, I + o.yh, x, yh, z);
+    if (D == 3) {
+        const int zl = (g.isper(2) && z == 1) ? g.n[2] - 2 : z - 1, zh = (g.isper(2) && z == g.n[2] - 2) ? 1 : z + 1;
+        const T* L2 = L1 + g.N;
+        a += L2[I] * first_nb<T, PROL>(g, gc, b, iD, xc, xv, I + o.zl, x, y, zl) +
+             L2[I + s2] * first_nb<T, PROL>(g, gc, b, iD, xc, xv, I + o.zh, x, y, zh);
+    }
+    const T dd = diag7<D>(g, L, I);
+    const T eps = sizeof(T) == 8 ? T(2.220446049250313e-16) : T(1.1920929e-7);
+    const T iDI = (dd * dd < T(2) * eps) ? T(0) : T(1) / dd;
+    xv[I] = (b[I] - a) * iDI;
+}
+
 // ---- temporally blocked red-black Gauss-Seidel (3D, FP32): S half-sweeps in one launch.
 // A block owns a TB_X x TB_Y column of interior cells and a range of z-planes and marches up
 // z as a wavefront: at step t half-sweep s works on plane t - s over the column widened by
@@ -385,12 +439,6 @@ inline dim3 pair_grid(const Grid& g) {
     return dim3((pairs + 31) / 32, (g.n[1] - 2 + 7) / 8, g.D == 3 ? g.n[2] - 2 : 1);
 }
 
-// first red sweep from x = 0: neighbours are zero
-template <class T>
-__global__ void rb_first_k(Grid g, const T* __restrict__ iD, const T* __restrict__ b, T* __restrict__ xv) {
-    INTERIOR_XYZ
-    xv[I] = (((x + y + z) & 1) == 0) ? b[I] * iD[I] : T(0);
-}
 
 template <class T, int D>
 __global__ void residual_k(Grid g, const T* __restrict__ L, const T* __restrict__ b, const T* __restrict__ xv,
@@ -869,19 +917,37 @@ static cudaError_t vcycle(ia_handle* h, PoissonMG* mg, int l, cudaStream_t st, i
         else { rbgs_pair_k<T, 2><<<pair_grid(L.g), blk(), 0, st>>>(L.g, Lc, b, x, color); ia::note_launch(); }
         timing_end(h, tk);
     };
-    { rb_first_k<T><<<grd(L.g), blk(), 0, st>>>(L.g, iD, b, x); ia::note_launch(); }
-    half(1);
+    auto& C = mg->lev[l + 1];
+    // first black half-sweep: from x = 0 (pre) or from x + P(x_coarse) (post)
+    auto first = [&](bool prol) {
+        const int tk = (l == 0) ? timing_begin(h, TK_MG_FIRST) : -1;
+        const T* xc = C.template x_<T>();
+        if (L.g.D == 3) {
+            if (prol) rbgs_first_k<T, 3, true><<<pair_grid(L.g), blk(), 0, st>>>(L.g, C.g, Lc, b, iD, xc, x, 0);
+            else rbgs_first_k<T, 3, false><<<pair_grid(L.g), blk(), 0, st>>>(L.g, C.g, Lc, b, iD, xc, x, nu1 == 1);
+        } else {
+            if (prol) rbgs_first_k<T, 2, true><<<pair_grid(L.g), blk(), 0, st>>>(L.g, C.g, Lc, b, iD, xc, x, 0);
+            else rbgs_first_k<T, 2, false><<<pair_grid(L.g), blk(), 0, st>>>(L.g, C.g, Lc, b, iD, xc, x, nu1 == 1);
+        }
+        ia::note_launch();
+        timing_end(h, tk);
+    };
+    first(false);
     for (int k = 1; k < nu1; ++k) {
         half(0);
         half(1);
     }
-    auto& C = mg->lev[l + 1];
     if (L.g.D == 3) { resid_restrict_k<T, 3><<<cell_grid(C.g), blk(), 0, st>>>(C.g, L.g, Lc, b, x, C.template b_<T>()); ia::note_launch(); }
     else { resid_restrict_k<T, 2><<<cell_grid(C.g), blk(), 0, st>>>(C.g, L.g, Lc, b, x, C.template b_<T>()); ia::note_launch(); }
     cudaError_t e = vcycle<T>(h, mg, l + 1, st, nu1, nu2, nuc);
     if (e != cudaSuccess) return e;
-    { prolong_k<T><<<grd(L.g), blk(), 0, st>>>(L.g, C.g, C.template x_<T>(), x); ia::note_launch(); }
-    for (int k = 0; k < nu2; ++k) {
+    if (nu2 == 0) {
+        { prolong_k<T><<<grd(L.g), blk(), 0, st>>>(L.g, C.g, C.template x_<T>(), x); ia::note_launch(); }
+        return cudaGetLastError();
+    }
+    first(true);
+    half(0);
+    for (int k = 1; k < nu2; ++k) {
         half(1);
         half(0);
     }

@@ -33,7 +33,8 @@ POISSON_MODES = {"fp64": 0, "mixed": 1, "learned": 2}
 PRECONDS = {"hybrid": 0, "net": 1, "none": 2, "vcycle": 3}
 SMOOTHERS = {"halfsweep": 0, "blocked": 1}
 TIMED_KERNELS = ["vof_bulk", "vof_cells", "ustar", "forcing", "mg_vcycle", "mg_residual", "mg_transfer",
-                 "krylov", "other", "vof_faces", "momflux", "momupdate", "update_project", "mg_fine_rbgs", "nn_precond"]
+                 "krylov", "other", "vof_faces", "momflux", "momupdate", "update_project", "mg_fine_rbgs", "nn_precond",
+                 "mg_fine_first"]
 
 
 class Config(C.Structure):
