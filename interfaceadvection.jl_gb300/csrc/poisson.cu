@@ -125,7 +125,7 @@ inline dim3 cell_grid(const Grid& g) {
     const int z = blockIdx.z;                                                                            \
     if (x < 1 || y < 1 || x > g.n[0] - 2 || y > g.n[1] - 2) return;                                      \
     if (g.D == 3 && (z < 1 || z > g.n[2] - 2)) return;                                                   \
-    const int c[3] = {x, y, z};                                                                          \
+    [[maybe_unused]] const int c[3] = {x, y, z};                                                         \
     const long long I = lin(g, x, y, z);
 
 template <class T>
@@ -519,6 +519,11 @@ __global__ void coarse_k(Grid g, const T* __restrict__ L, const T* __restrict__ 
     }
 }
 
+template <class T>
+__global__ void zero_k(long long n, T* a) {
+    for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < n; q += (long long)gridDim.x * blockDim.x)
+        a[q] = T(0);
+}
 __global__ void to_f32_k(long long n, const double* __restrict__ a, float* __restrict__ b) {
     for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < n; q += (long long)gridDim.x * blockDim.x)
         b[q] = float(a[q]);
@@ -548,7 +553,7 @@ constexpr int KBLOCKS = 1216;   // 8 blocks on each of 152 SMs
     {                                                                                      \
         ROWS_FOR(g, (g).D) {                                                               \
             for (int x = 1 + threadIdx.x; x <= nxi_; x += blockDim.x) {                    \
-                const int c[3] = {x, y, z};                                                \
+                [[maybe_unused]] const int c[3] = {x, y, z};                               \
                 const long long I = lin(g, x, y, z);
 #define ROWS_END \
     }            \
@@ -639,6 +644,24 @@ __global__ void true_resid_k(Grid g, const double* __restrict__ L, const double*
     ROWS_END
     m = block_max(m);
     if (threadIdx.x == 0) atomicMax(linf, m);
+}
+
+// finest-level set-up of the mixed solver in one pass: FP32 face coefficients of every cell and
+// ghost (to_f32_k), and on interior cells the FP64 diagonal (set_diag64_k) and the FP32 inverse
+// diagonal of the converted coefficients (set_diag_k<float>)
+__global__ void setup_mixed_k(Grid g, const double* __restrict__ L, double* __restrict__ diag64,
+                              float* __restrict__ L32, float* __restrict__ iD32) {
+    const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y;
+    const int z = blockIdx.z;
+    if (x >= g.n[0] || y >= g.n[1]) return;
+    const long long I = lin(g, x, y, z);
+    for (int i = 0; i < g.D; ++i) L32[I + i * g.N] = float(L[I + i * g.N]);
+    const int c[3] = {x, y, z};
+    if (!is_interior(g, c)) return;
+    diag64[I] = diag_of(g, L, I);
+    float dd = 0.f;
+    for (int i = 0; i < g.D; ++i) dd -= float(L[I + i * g.N]) + float(L[I + g.s[i] + i * g.N]);
+    iD32[I] = (dd * dd < 2.f * 1.1920929e-7f) ? 0.f : 1.f / dd;
 }
 
 // q = A p and partial dot p·q
@@ -819,12 +842,6 @@ __global__ void perbc_k(Grid g, double* a) {
     // only read positions that no thread writes: the mapped position must have
     // no periodic ghost coordinate left (it has none after mapping)
     a[lin(g, x, y, z)] = a[lin3(g, c)];
-}
-
-template <class T>
-__global__ void zero_k(long long n, T* a) {
-    for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < n; q += (long long)gridDim.x * blockDim.x)
-        a[q] = T(0);
 }
 
 }  // namespace
@@ -1121,8 +1138,8 @@ static cudaError_t mg_setup(ia_handle* h, const double* L0) {
     const bool mixed = h->cfg.poisson_mode != IA_POISSON_FP64;
     MGLevel& F = mg->lev[0];
     const long long nv = F.g.N * F.g.D;
-    { set_diag64_k<<<mg->kb, KTHREADS, 0, st>>>(F.g, L0, mg->diag64); ia::note_launch(); }
     if (!mixed) {
+        { set_diag64_k<<<mg->kb, KTHREADS, 0, st>>>(F.g, L0, mg->diag64); ia::note_launch(); }
         cudaMemcpyAsync(F.L, L0, 8 * nv, cudaMemcpyDeviceToDevice, st);
         { set_diag_k<double><<<grd(F.g), blk(), 0, st>>>(F.g, F.L, F.iD); ia::note_launch(); }
         for (int l = 1; l < mg->nlev; ++l) {
@@ -1131,8 +1148,7 @@ static cudaError_t mg_setup(ia_handle* h, const double* L0) {
             { set_diag_k<double><<<grd(mg->lev[l].g), blk(), 0, st>>>(mg->lev[l].g, mg->lev[l].L, mg->lev[l].iD); ia::note_launch(); }
         }
     } else {
-        { to_f32_k<<<1216, 256, 0, st>>>(nv, L0, F.L32); ia::note_launch(); }
-        { set_diag_k<float><<<grd(F.g), blk(), 0, st>>>(F.g, F.L32, F.iD32); ia::note_launch(); }
+        { setup_mixed_k<<<grd(F.g), blk(), 0, st>>>(F.g, L0, mg->diag64, F.L32, F.iD32); ia::note_launch(); }
         for (int l = 1; l < mg->nlev; ++l) {
             { restrict_L_k<float><<<grd(mg->lev[l].g), blk(), 0, st>>>(mg->lev[l].g, mg->lev[l - 1].g,
                                                                       mg->lev[l - 1].L32, mg->lev[l].L32); ia::note_launch(); }
