@@ -517,21 +517,36 @@ __global__ void zero_kern(double* a, long long n) {
 }
 
 // ------------------------------------------------------------------ surface tension
-__global__ void fbuffer_kern(MomConsts k, int d, const double* __restrict__ f, double* __restrict__ fb) {
+__device__ __forceinline__ bool mixed(double v) {
+    const unsigned long long b = dbits(v);
+    return b != 0ull && b < kOneBits;   // 0 < v < 1 (sign bit set → huge, excluded)
+}
+
+// fᶠ along d, and the list of interior cells where it is mixed (the only cells surften_kern
+// changes), appended one warp at a time
+__global__ void fbuffer_kern(MomConsts k, int d, const double* __restrict__ f, double* __restrict__ fb,
+                             int* __restrict__ list, unsigned int* __restrict__ count) {
     const Grid& g = k.g;
     GCELL_XYZ
     int c[3] = {x, y, z};
+    const bool inner = is_interior(g, c);
     // BCf!(d, ·): the high ghost along a zero-gradient d is not written by the
     // reference (it keeps older buffer contents); it is taken as a zero-gradient copy here.
     if (face_bc(g, d, c)) c[d] = g.n[d] - 2;
     const long long P = lin3(g, c);
     const double fa = f[P], fm = f[P - g.s[d]];
-    fb[lin(g, x, y, z)] = (dbits(fa) == dbits(fm)) ? fa : (fa + fm) / 2.0;
-}
-
-__device__ __forceinline__ bool mixed(double v) {
-    const unsigned long long b = dbits(v);
-    return b != 0ull && b < kOneBits;   // 0 < v < 1 (sign bit set → huge, excluded)
+    const double v = (dbits(fa) == dbits(fm)) ? fa : (fa + fm) / 2.0;
+    const long long I = lin(g, x, y, z);
+    fb[I] = v;
+    const bool want = inner && mixed(v);
+    const unsigned int bal = __ballot_sync(__activemask(), want);
+    if (want) {
+        const int lane = int(threadIdx.x) & 31, leader = __ffs(bal) - 1;
+        unsigned int base = 0;
+        if (lane == leader) base = atomicAdd(count, unsigned(__popc(bal)));
+        base = __shfl_sync(bal, base, leader);
+        list[base + __popc(bal & ((1u << lane) - 1u))] = int(I);
+    }
 }
 
 // getPopinetHeightAdaptive, monotonic (src/surfaceTension.jl:78-101); axis a, direction sg
@@ -602,14 +617,18 @@ __device__ double curvature(const Grid& g, const double* fb, const int c[3], int
     return Hxx / sqrt(q1 * q1 * q1);
 }
 
+// surfTen! on the listed cells, one per lane: the interface cells fill whole warps and spread
+// over every multiprocessor instead of idling most lanes of the warps that hold them
 template <int D>
 __global__ void surften_kern(MomConsts k, int d, const double* __restrict__ f, const double* __restrict__ fb,
-                             double eta, double* __restrict__ r) {
+                             double eta, double* __restrict__ r, const int* __restrict__ list,
+                             const unsigned int* __restrict__ count) {
     const Grid& g = k.g;
-    ICELL_XYZ
-    const int c[3] = {x, y, z};
-    const long long I = lin(g, x, y, z);
-    if (!mixed(fb[I])) return;
+    const unsigned int n = *count;
+    for (unsigned int q = blockIdx.x * blockDim.x + threadIdx.x; q < n; q += gridDim.x * blockDim.x) {
+    const long long I = list[q];
+    int c[3];
+    coords3(g, I, c);
     Stencil S;
     S.f = fb;
     S.c = I;
@@ -622,6 +641,7 @@ __global__ void surften_kern(MomConsts k, int d, const double* __restrict__ f, c
     const int md = signbit(n[ia]) ? -(ia + 1) : (ia + 1);
     const double kap = curvature(g, fb, c, md);
     r[I + d * g.N] += eta * kap * -(f[I] - f[I - g.s[d]]);
+    }
 }
 
 // ------------------------------------------------------------------ update, L, projection
@@ -821,10 +841,12 @@ cudaError_t k_zero(double* a, long long n, cudaStream_t s) {
     { zero_kern<<<1216, 256, 0, s>>>(a, n); ia::note_launch(); }
     return cudaGetLastError();
 }
-cudaError_t k_surften(const MomConsts& k, int d, const double* f, double eta, double* fb, double* r, cudaStream_t s) {
-    { fbuffer_kern<<<ggrd(k.g), blk(), 0, s>>>(k, d, f, fb); ia::note_launch(); }
-    if (k.g.D == 2) { surften_kern<2><<<igrd(k.g), blk(), 0, s>>>(k, d, f, fb, eta, r); ia::note_launch(); }
-    else { surften_kern<3><<<igrd(k.g), blk(), 0, s>>>(k, d, f, fb, eta, r); ia::note_launch(); }
+cudaError_t k_surften(const MomConsts& k, int d, const double* f, double eta, double* fb, double* r, int* list,
+                      unsigned int* count, cudaStream_t s) {
+    cudaMemsetAsync(count, 0, sizeof(unsigned int), s);
+    { fbuffer_kern<<<ggrd(k.g), blk(), 0, s>>>(k, d, f, fb, list, count); ia::note_launch(); }
+    if (k.g.D == 2) { surften_kern<2><<<608, 64, 0, s>>>(k, d, f, fb, eta, r, list, count); ia::note_launch(); }
+    else { surften_kern<3><<<608, 64, 0, s>>>(k, d, f, fb, eta, r, list, count); ia::note_launch(); }
     return cudaGetLastError();
 }
 cudaError_t k_updateu(const MomConsts& k, double* u, double* rhou, const double* u0, const double* F, double dt,

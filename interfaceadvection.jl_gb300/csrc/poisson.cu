@@ -482,15 +482,25 @@ __global__ void prolong_k(Grid gf, Grid gc, const T* __restrict__ xc, T* __restr
 template <class T>
 __global__ void coarse_k(Grid g, const T* __restrict__ L, const T* __restrict__ iD, T* __restrict__ b,
                          T* __restrict__ xv, int nuc) {
+    // the sweeps run on a shared-memory copy of x when the level fits (it holds at most a few
+    // hundred cells), with 32-bit cell coordinates
+    constexpr int SMAX = 4096;
     __shared__ double red[1024];
-    const long long total = g.N;
+    __shared__ T xs[SMAX];
+    const int total = int(g.N);
+    const bool sm = total <= SMAX;
+    T* xw = sm ? xs : xv;
+    auto coords = [&](int q, int c[3]) {
+        c[0] = q % g.n[0];
+        const int r = q / g.n[0];
+        c[1] = r % g.n[1];
+        c[2] = r / g.n[1];
+    };
     double acc = 0.0;
-    long long cnt = 0;
-    for (long long q = threadIdx.x; q < total; q += blockDim.x) {
-        const int c[3] = {int(q % g.n[0]), int((q / g.n[0]) % g.n[1]), int(q / ((long long)g.n[0] * g.n[1]))};
-        if (!is_interior(g, c)) continue;
-        acc += double(b[q]);
-        ++cnt;
+    for (int q = threadIdx.x; q < total; q += blockDim.x) {
+        int c[3];
+        coords(q, c);
+        if (is_interior(g, c)) acc += double(b[q]);
     }
     red[threadIdx.x] = acc;
     __syncthreads();
@@ -502,21 +512,25 @@ __global__ void coarse_k(Grid g, const T* __restrict__ L, const T* __restrict__ 
     for (int e = 0; e < g.D; ++e) ninner *= (g.n[e] - 2);
     const T mean = T(red[0] / double(ninner));
     __syncthreads();
-    for (long long q = threadIdx.x; q < total; q += blockDim.x) {
-        const int c[3] = {int(q % g.n[0]), int((q / g.n[0]) % g.n[1]), int(q / ((long long)g.n[0] * g.n[1]))};
+    for (int q = threadIdx.x; q < total; q += blockDim.x) {
+        int c[3];
+        coords(q, c);
         if (is_interior(g, c)) b[q] -= mean;
-        xv[q] = T(0);
+        xw[q] = T(0);
     }
     __syncthreads();
     for (int it = 0; it < 2 * nuc; ++it) {
         const int color = (it & 1) ^ ((it >> 1) & 1);   // R B, B R, R B, ...
-        for (long long q = threadIdx.x; q < total; q += blockDim.x) {
-            const int c[3] = {int(q % g.n[0]), int((q / g.n[0]) % g.n[1]), int(q / ((long long)g.n[0] * g.n[1]))};
+        for (int q = threadIdx.x; q < total; q += blockDim.x) {
+            int c[3];
+            coords(q, c);
             if (!is_interior(g, c) || ((c[0] + c[1] + c[2]) & 1) != color) continue;
-            xv[q] = (b[q] - offdiag(g, L, xv, q, c)) * iD[q];
+            xw[q] = (b[q] - offdiag(g, L, xw, q, c)) * iD[q];
         }
         __syncthreads();
     }
+    if (sm)
+        for (int q = threadIdx.x; q < total; q += blockDim.x) xv[q] = xs[q];
 }
 
 template <class T>

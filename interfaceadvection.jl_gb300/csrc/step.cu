@@ -16,6 +16,8 @@ struct MomScratch {
     double* Phi = nullptr;     // momentum face fluxes of one sweep (vector)
     double* Phi6 = nullptr;    // viscous face / edge fluxes (D(D+1)/2 scalars)
     double* fb = nullptr;      // face fraction for surface tension
+    int* slist = nullptr;      // interior cells with a mixed face fraction
+    unsigned int* scount = nullptr;
     double* ft1 = nullptr;     // out-of-place VOF sweep buffers
     double* ft2 = nullptr;
     unsigned long long* cfl = nullptr;   // device max reductions (2)
@@ -53,6 +55,8 @@ static int ensure_scratch(ia_handle* h) {
     e = e ? e : cudaMalloc(&m->Phi, 8 * N * D);
     e = e ? e : cudaMalloc(&m->Phi6, 8 * N * npair);
     e = e ? e : cudaMalloc(&m->fb, 8 * N);
+    e = e ? e : cudaMalloc(&m->slist, 4 * N);
+    e = e ? e : cudaMalloc(&m->scount, sizeof(unsigned int));
     e = e ? e : cudaMalloc(&m->ft1, 8 * N);
     e = e ? e : cudaMalloc(&m->ft2, 8 * N);
     e = e ? e : cudaMalloc(&m->cfl, 16);
@@ -72,6 +76,8 @@ void extra_destroy(ia_handle* h) {
     cudaFree(m->Phi);
     cudaFree(m->Phi6);
     cudaFree(m->fb);
+    cudaFree(m->slist);
+    cudaFree(m->scount);
     cudaFree(m->ft1);
     cudaFree(m->ft2);
     cudaFree(m->cfl);
@@ -127,7 +133,8 @@ static int visc_surften(ia_handle* h, const double* f) {
     if (e != cudaSuccess) return IA_ERR_CUDA;
     if (h->cfg.eta != 0.0)
         for (int d = 0; d < g.D; ++d)
-            if (k_surften(k, d, f, h->cfg.eta, m->fb, h->fld.force, st) != cudaSuccess) return IA_ERR_CUDA;
+            if (k_surften(k, d, f, h->cfg.eta, m->fb, h->fld.force, m->slist, m->scount, st) != cudaSuccess)
+                return IA_ERR_CUDA;
     timing_end(h, tk);
     return IA_OK;
 }
