@@ -763,13 +763,28 @@ __global__ void matvec32_dot_k(Grid g, const float* __restrict__ L, const float*
     if (threadIdx.x == 0) partial[blockIdx.x] = a;
 }
 
-__global__ void dot2_32_k(Grid g, const float* __restrict__ sv, const float* __restrict__ q,
+// Whole-array FP32 vector kernels of the inner solve.  Only interior cells of these vectors are
+// ever written, so their ghost entries stay zero and sums and updates over all N entries equal
+// those over the interior; the arrays are streamed as 16-byte vectors (cudaMalloc alignment),
+// the N mod 4 tail by the first threads.
+__global__ void dot2_32_k(long long n, const float* __restrict__ sv, const float* __restrict__ q,
                           const float* __restrict__ r, double* __restrict__ partial) {
     float a1 = 0.f, a2 = 0.f;
-    ROWS_BEGIN(g)
-    a1 += sv[I] * q[I];
-    a2 += sv[I] * r[I];
-    ROWS_END
+    const long long n4 = n / 4, stride = (long long)gridDim.x * blockDim.x;
+    const long long t0 = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    const float4* s4 = reinterpret_cast<const float4*>(sv);
+    const float4* q4 = reinterpret_cast<const float4*>(q);
+    const float4* r4 = reinterpret_cast<const float4*>(r);
+    for (long long i = t0; i < n4; i += stride) {
+        const float4 a = s4[i], bq = q4[i], br = r4[i];
+        a1 += a.x * bq.x + a.y * bq.y + a.z * bq.z + a.w * bq.w;
+        a2 += a.x * br.x + a.y * br.y + a.z * br.z + a.w * br.w;
+    }
+    if (t0 < n - 4 * n4) {
+        const long long i = 4 * n4 + t0;
+        a1 += sv[i] * q[i];
+        a2 += sv[i] * r[i];
+    }
     double b1 = a1, b2 = a2;
     block_sum2(b1, b2);
     if (threadIdx.x == 0) {
@@ -780,23 +795,57 @@ __global__ void dot2_32_k(Grid g, const float* __restrict__ sv, const float* __r
 
 // p = s + β p; β = 0 restarts from s without reading the old direction (which a rejected
 // preconditioner output may have left non-finite)
-__global__ void xpby32_k(Grid g, const float* __restrict__ sv, float beta, float* __restrict__ pv) {
-    ROWS_BEGIN(g)
-    pv[I] = (beta == 0.f) ? sv[I] : sv[I] + beta * pv[I];
-    ROWS_END
+__global__ void xpby32_k(long long n, const float* __restrict__ sv, float beta, float* __restrict__ pv) {
+    const long long n4 = n / 4, stride = (long long)gridDim.x * blockDim.x;
+    const long long t0 = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    const float4* s4 = reinterpret_cast<const float4*>(sv);
+    float4* p4 = reinterpret_cast<float4*>(pv);
+    const bool restart = beta == 0.f;
+    for (long long i = t0; i < n4; i += stride) {
+        const float4 a = s4[i];
+        if (restart) {
+            p4[i] = a;
+        } else {
+            const float4 p = p4[i];
+            p4[i] = make_float4(a.x + beta * p.x, a.y + beta * p.y, a.z + beta * p.z, a.w + beta * p.w);
+        }
+    }
+    if (t0 < n - 4 * n4) {
+        const long long i = 4 * n4 + t0;
+        pv[i] = restart ? sv[i] : sv[i] + beta * pv[i];
+    }
 }
 
 // e += α p ; r -= α q ; L∞(r) as float bits
-__global__ void update32_k(Grid g, float alpha, const float* __restrict__ pv, const float* __restrict__ q,
+__global__ void update32_k(long long n, float alpha, const float* __restrict__ pv, const float* __restrict__ q,
                            float* __restrict__ e, float* __restrict__ r, unsigned int* linf) {
     unsigned long long m = 0ull;
-    ROWS_BEGIN(g)
-    e[I] += alpha * pv[I];
-    const float v = r[I] - alpha * q[I];
-    r[I] = v;
-    const unsigned long long b = __float_as_uint(v) & 0x7FFFFFFFu;
-    m = b > m ? b : m;
-    ROWS_END
+    const long long n4 = n / 4, stride = (long long)gridDim.x * blockDim.x;
+    const long long t0 = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    const float4* p4 = reinterpret_cast<const float4*>(pv);
+    const float4* q4 = reinterpret_cast<const float4*>(q);
+    float4* e4 = reinterpret_cast<float4*>(e);
+    float4* r4 = reinterpret_cast<float4*>(r);
+    auto mx = [&](float v) {
+        const unsigned long long b = __float_as_uint(v) & 0x7FFFFFFFu;
+        m = b > m ? b : m;
+    };
+    for (long long i = t0; i < n4; i += stride) {
+        const float4 p = p4[i], qq = q4[i];
+        float4 ee = e4[i], rr = r4[i];
+        ee.x += alpha * p.x; ee.y += alpha * p.y; ee.z += alpha * p.z; ee.w += alpha * p.w;
+        rr.x -= alpha * qq.x; rr.y -= alpha * qq.y; rr.z -= alpha * qq.z; rr.w -= alpha * qq.w;
+        e4[i] = ee;
+        r4[i] = rr;
+        mx(rr.x); mx(rr.y); mx(rr.z); mx(rr.w);
+    }
+    if (t0 < n - 4 * n4) {
+        const long long i = 4 * n4 + t0;
+        e[i] += alpha * pv[i];
+        const float v = r[i] - alpha * q[i];
+        r[i] = v;
+        mx(v);
+    }
     m = block_max(m);
     if (threadIdx.x == 0) atomicMax(linf, (unsigned int)m);
 }
@@ -1300,7 +1349,7 @@ static int poisson_solve_mixed(ia_handle* h, double* xv, const double* zz, const
             float* sv = nullptr;
             if (!precond(sv)) return IA_ERR_CUDA;
             tk = timing_begin(h, TK_KRYLOV);
-            { dot2_32_k<<<mg->kb, KTHREADS, 0, st>>>(g, sv, mg->q32, rr, mg->partial); ia::note_launch(); }
+            { dot2_32_k<<<mg->kb, KTHREADS, 0, st>>>(N, sv, mg->q32, rr, mg->partial); ia::note_launch(); }
             { finalize_k<<<1, 1024, 0, st>>>(mg->partial, mg->kb, 2, dots); ia::note_launch(); }
             timing_end(h, tk);
             cudaMemcpyAsync(mg->hsc + 2, dots, 16, cudaMemcpyDeviceToHost, st);
@@ -1308,7 +1357,7 @@ static int poisson_solve_mixed(ia_handle* h, double* xv, const double* zz, const
             const double sq = mg->hsc[2], sr = mg->hsc[3];
             const double beta = (it == 0) ? 0.0 : (-alpha_prev * sq) / rho_prev;
             tk = timing_begin(h, TK_KRYLOV);
-            { xpby32_k<<<mg->kb, KTHREADS, 0, st>>>(g, sv, float(beta), mg->p32); ia::note_launch(); }
+            { xpby32_k<<<mg->kb, KTHREADS, 0, st>>>(N, sv, float(beta), mg->p32); ia::note_launch(); }
             LAUNCH_D(g, matvec32_dot_k, mg->kb, KTHREADS, g, F.L32, mg->p32, mg->q32, mg->partial);
             { finalize_k<<<1, 1024, 0, st>>>(mg->partial, mg->kb, 1, dots); ia::note_launch(); }
             timing_end(h, tk);
@@ -1321,7 +1370,7 @@ static int poisson_solve_mixed(ia_handle* h, double* xv, const double* zz, const
             const double alpha = sr / pq;
             cudaMemsetAsync(dlinf32, 0, 4, st);
             tk = timing_begin(h, TK_KRYLOV);
-            { update32_k<<<mg->kb, KTHREADS, 0, st>>>(g, float(alpha), mg->p32, mg->q32, mg->e32, rr, dlinf32); ia::note_launch(); }
+            { update32_k<<<mg->kb, KTHREADS, 0, st>>>(N, float(alpha), mg->p32, mg->q32, mg->e32, rr, dlinf32); ia::note_launch(); }
             timing_end(h, tk);
             const double rin = read_linf32(h, dlinf32);
             rho_prev = sr;
