@@ -60,6 +60,8 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-secondary", action="store_true", help="skip the FP64-MG and VOF-only side runs")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--smoother", default="halfsweep", choices=["halfsweep", "blocked"],
+                    help="FP32 V-cycle smoother of the mixed solver")
     return ap.parse_args()
 
 
@@ -252,6 +254,7 @@ def run_bubble(args, world, local_rank):
     barrier = (lambda: torch.distributed.barrier()) if world > 1 else (lambda: None)
     L = _lib.load()
     sim = make_bubble(N, "mixed", dev)
+    ia.set_smoother(sim.handle, args.smoother)
     for _ in range(args.warmup):
         ia.sim_step(sim)
     n0 = L.ia_launch_count()

@@ -169,11 +169,15 @@ __device__ __forceinline__ void warp_append(unsigned int* list, unsigned int* co
 
 template <int D, bool FIRST>
 __global__ void __launch_bounds__(256) vof_bulk(SweepArgs a) {
-    const int x = blockIdx.x * blockDim.x + threadIdx.x;
-    const int y = blockIdx.y * blockDim.y + threadIdx.y;
-    const int z = blockIdx.z;
+    // x in [1, n-2] one cell per lane, so that a row of 32k interior cells fills k warps; the
+    // last block column's first warp takes the ghost cells x = 0 and n-1 of the block's 8 rows.
+    // Lanes without a cell stay in the warp (the list appends are warp-collective).
     const Grid& g = a.g;
-    const bool valid = x < g.n[0] && y < g.n[1];
+    const bool gcol = blockIdx.x + 1 == gridDim.x;
+    const int x = gcol ? ((threadIdx.x & 1) ? g.n[0] - 1 : 0) : 1 + int(blockIdx.x) * 32 + int(threadIdx.x);
+    const int y = gcol ? int(blockIdx.y) * 8 + int(threadIdx.x >> 1) : int(blockIdx.y) * 8 + int(threadIdx.y);
+    const int z = blockIdx.z;
+    const bool valid = (gcol ? (threadIdx.y == 0 && threadIdx.x < 16) : x <= g.n[0] - 2) && y < g.n[1];
     bool need_cell = false, need_face = false;
     long long O = 0;
     if (valid) {
@@ -281,7 +285,7 @@ __global__ void __launch_bounds__(256) vof_scatter(SweepArgs a) {
 template <int D, bool FIRST>
 void launch_bulk(const SweepArgs& a, cudaStream_t st) {
     dim3 blk(32, 8, 1);
-    dim3 grd((a.g.n[0] + 31) / 32, (a.g.n[1] + 7) / 8, a.g.n[2]);
+    dim3 grd((a.g.n[0] - 2 + 31) / 32 + 1, (a.g.n[1] + 7) / 8, a.g.n[2]);
     { vof_bulk<D, FIRST><<<grd, blk, 0, st>>>(a); ia::note_launch(); }
 }
 
