@@ -43,6 +43,44 @@ __device__ __forceinline__ bool face_bc(const Grid& g, int d, int c[3]) {
     return upper;
 }
 
+// The cells BC! changes: the planes c[e] in {0, 1, n_e - 1} of each dimension (ghost layers and
+// Dirichlet wall faces), numbered dimension by dimension, plane by plane, x fastest within a plane.
+// bc_plane_cells() counts them; bc_plane_cell() gives the coordinates of number t (false when t is
+// past the end).  Cells on an edge or corner appear once per plane they lie on.
+__host__ __device__ inline long long bc_plane_cells(const Grid& g) {
+    const long long n0 = g.n[0], n1 = g.n[1], n2 = g.n[2];
+    return 3 * n1 * n2 + 3 * n0 * n2 + (g.D == 3 ? 3 * n0 * n1 : 0);
+}
+__host__ __device__ inline int bc_plane_coord(int which, int n) { return which == 0 ? 0 : (which == 1 ? 1 : n - 1); }
+__host__ __device__ inline bool bc_plane_cell(const Grid& g, long long t, int c[3]) {
+    const long long n0 = g.n[0], n1 = g.n[1], n2 = g.n[2];
+    const long long a0 = n1 * n2, a1 = n0 * n2, a2 = n0 * n1;   // cells per plane of dimension 0, 1, 2
+    if (t < 3 * a0) {
+        const long long r = t % a0;
+        c[0] = bc_plane_coord(int(t / a0), g.n[0]);
+        c[1] = int(r % n1);
+        c[2] = int(r / n1);
+        return true;
+    }
+    t -= 3 * a0;
+    if (t < 3 * a1) {
+        const long long r = t % a1;
+        c[1] = bc_plane_coord(int(t / a1), g.n[1]);
+        c[0] = int(r % n0);
+        c[2] = int(r / n0);
+        return true;
+    }
+    t -= 3 * a1;
+    if (g.D == 3 && t < 3 * a2) {
+        const long long r = t % a2;
+        c[2] = bc_plane_coord(int(t / a2), g.n[2]);
+        c[0] = int(r % n0);
+        c[1] = int(r / n0);
+        return true;
+    }
+    return false;
+}
+
 __device__ __forceinline__ bool is_interior(const Grid& g, const int c[3]) {
     for (int e = 0; e < g.D; ++e)
         if (c[e] < 1 || c[e] > g.n[e] - 2) return false;

@@ -135,12 +135,17 @@ __device__ __forceinline__ void bcvel_cell(const Grid& g, double* a, const doubl
     }
 }
 
+// BC! changes only the planes c[e] in {0, 1, n_e - 1} of each dimension (the ghost layers and the
+// Dirichlet wall faces): one thread per cell of those planes, instead of a launch over every cell.
+// A cell on an edge or corner lies on several planes and is written by each with the same value:
+// a written value is A[i] or a copy from a source whose coordinates all lie in [1, n-2] with the
+// normal one >= 2 on a wall, a position no thread writes.
 __global__ void bcvel_kern(MomConsts k, double* a, double A0, double A1, double A2) {
     const Grid& g = k.g;
-    GCELL_XYZ
-    const int c0[3] = {x, y, z};
+    int c[3];
+    if (!bc_plane_cell(g, blockIdx.x * (long long)blockDim.x + threadIdx.x, c)) return;
     const double A[3] = {A0, A1, A2};
-    bcvel_cell(g, a, A, c0);
+    bcvel_cell(g, a, A, c);
 }
 
 // ------------------------------------------------------------------ limiters (src/flow.jl:5-15)
@@ -775,7 +780,7 @@ cudaError_t k_u2rhou(const MomConsts& k, double* rhou, const double* u, const do
     return cudaGetLastError();
 }
 cudaError_t k_bc_vel(const MomConsts& k, double* a, const double* A, cudaStream_t s) {
-    { bcvel_kern<<<ggrd(k.g), blk(), 0, s>>>(k, a, A[0], A[1], A[2]); ia::note_launch(); }
+    { bcvel_kern<<<unsigned((bc_plane_cells(k.g) + 255) / 256), 256, 0, s>>>(k, a, A[0], A[1], A[2]); ia::note_launch(); }
     return cudaGetLastError();
 }
 cudaError_t k_momflux(const MomConsts& k, int j, int limiter, const double* ustar, const double* rhouf_j,
