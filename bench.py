@@ -61,7 +61,7 @@ def parse():
     ap.add_argument("--no-secondary", action="store_true", help="skip the FP64-MG and VOF-only side runs")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--smoother", default="halfsweep", choices=["halfsweep", "blocked"],
-                    help="FP32 V-cycle smoother of the mixed solver")
+                    help="FP32 V-cycle smoother of the mixed solver (blocked: relaxation factor 1)")
     return ap.parse_args()
 
 
@@ -254,7 +254,8 @@ def run_bubble(args, world, local_rank):
     barrier = (lambda: torch.distributed.barrier()) if world > 1 else (lambda: None)
     L = _lib.load()
     sim = make_bubble(N, "mixed", dev)
-    ia.set_smoother(sim.handle, args.smoother)
+    # the blocked smoother applies at relaxation factor 1 only
+    ia.set_smoother(sim.handle, args.smoother, 1.0 if args.smoother == "blocked" else None)
     for _ in range(args.warmup):
         ia.sim_step(sim)
     n0 = L.ia_launch_count()

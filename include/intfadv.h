@@ -304,8 +304,13 @@ int ia_poisson_precond(ia_handle* h, int32_t precond, int32_t inner_max, double 
 int ia_poisson_mg_params(ia_handle* h, int32_t nu1, int32_t nu2, int32_t nuc);
 /* smoother of the FP32 V-cycle (no reference counterpart: the reference smooths in FP64 with
  * WaterLily's MultiLevelPoisson): IA_SMOOTHER_*.  The blocked smoother is used where it applies
- * (3D levels, nu1 and nu2 in {1, 2}) and the half-sweeps elsewhere */
+ * (3D levels, nu1 and nu2 in {1, 2}, relaxation factor 1) and the half-sweeps elsewhere */
 int ia_poisson_smoother(ia_handle* h, int32_t kind);
+/* relaxation factor omega in (0, 2) of the V-cycle's red-black half-sweeps, x += omega (x_GS - x)
+ * (no reference counterpart; default 1.15, which takes the rising-bubble solves from 12 to 10 FCG
+ * iterations per step; 1 is plain Gauss-Seidel); the coarsest-level sweeps stay at 1.  The blocked
+ * smoother runs only at omega = 1 (the half-sweeps are used otherwise) */
+int ia_poisson_mg_relax(ia_handle* h, double omega);
 /* counters since the handle's creation: [0] net applications, [1] V-cycles, [2] fallbacks
  * to the V-cycle, [3] inner FCG iterations, [4] outer corrections */
 int ia_poisson_stats(ia_handle* h, int64_t* out5);

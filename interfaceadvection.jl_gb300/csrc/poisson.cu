@@ -173,9 +173,11 @@ __global__ void restrict_L_k(Grid gc, Grid gf, const T* __restrict__ Lf, T* __re
 // interior cells (1 + 2tx, 2 + 2tx) of its row and updates the one of this colour, so no
 // lane idles; the diagonal comes from the face coefficients the update reads anyway
 // (same value and zero-diagonal rule as set_diag_k).
-template <class T, int D>
+// With PROL (over-relaxed first red half-sweep of a post-smoothing whose prolongation is fused
+// into the sweeps) the cell's previous value is x + the injected coarse correction.
+template <class T, int D, bool PROL = false>
 __global__ void rbgs_pair_k(Grid g, const T* __restrict__ L, const T* __restrict__ b, T* __restrict__ xv,
-                            int color) {
+                            int color, T omega, Grid gc = Grid(), const T* __restrict__ xc = nullptr) {
     const int y = 1 + blockIdx.y * blockDim.y + threadIdx.y;
     const int z = D == 3 ? 1 + int(blockIdx.z) : 0;
     if (y > g.n[1] - 2) return;
@@ -188,7 +190,14 @@ __global__ void rbgs_pair_k(Grid g, const T* __restrict__ L, const T* __restrict
     const T dd = diag7<D>(g, L, I);
     const T eps = sizeof(T) == 8 ? T(2.220446049250313e-16) : T(1.1920929e-7);
     const T iD = (dd * dd < T(2) * eps) ? T(0) : T(1) / dd;
-    xv[I] = (b[I] - off) * iD;
+    const T gs = (b[I] - off) * iD;
+    if (omega == T(1)) {
+        xv[I] = gs;
+    } else {   // over-relaxation: x + ω (x_GS - x)
+        T xo = xv[I];
+        if (PROL) xo += xc[lin(gc, (x + 1) / 2, (y + 1) / 2, D == 3 ? (z + 1) / 2 : 0)];
+        xv[I] = xo + omega * (gs - xo);
+    }
 }
 
 // ---- first half-sweep of a smoothing, fused with the pass before it.  A red update reads only
@@ -200,18 +209,19 @@ __global__ void rbgs_pair_k(Grid g, const T* __restrict__ L, const T* __restrict
 template <class T, bool PROL>
 __device__ __forceinline__ T first_nb(const Grid& g, const Grid& gc, const T* __restrict__ b,
                                       const T* __restrict__ iD, const T* __restrict__ xc, const T* xv, int J,
-                                      int cx, int cy, int cz) {
+                                      int cx, int cy, int cz, T omega) {
     // J, (cx, cy, cz): index and (periodically wrapped) coordinates of the neighbour
     const bool in = cx >= 1 && cx <= g.n[0] - 2 && cy >= 1 && cy <= g.n[1] - 2 &&
                     (g.D == 2 || (cz >= 1 && cz <= g.n[2] - 2));
     if (!in) return xv[J];
     if (PROL) return xv[J] + xc[lin(gc, (cx + 1) / 2, (cy + 1) / 2, g.D == 3 ? (cz + 1) / 2 : 0)];
-    return b[J] * iD[J];
+    return omega == T(1) ? b[J] * iD[J] : omega * (b[J] * iD[J]);
 }
 
 template <class T, int D, bool PROL>
 __global__ void rbgs_first_k(Grid g, Grid gc, const T* __restrict__ L, const T* __restrict__ b,
-                             const T* __restrict__ iD, const T* __restrict__ xc, T* __restrict__ xv, int write_red) {
+                             const T* __restrict__ iD, const T* __restrict__ xc, T* __restrict__ xv, int write_red,
+                             T omega) {
     const int y = 1 + blockIdx.y * blockDim.y + threadIdx.y;
     const int z = D == 3 ? 1 + int(blockIdx.z) : 0;
     if (y > g.n[1] - 2) return;
@@ -221,7 +231,7 @@ __global__ void rbgs_first_k(Grid g, Grid gc, const T* __restrict__ L, const T* 
     const int s1 = int(g.s[1]), s2 = int(g.s[2]);
     if (!PROL && write_red && xr <= g.n[0] - 2) {
         const int Ir = xr + y * s1 + z * s2;
-        xv[Ir] = b[Ir] * iD[Ir];
+        xv[Ir] = omega == T(1) ? b[Ir] * iD[Ir] : omega * (b[Ir] * iD[Ir]);
     }
     if (x > g.n[0] - 2) return;
     const int I = x + y * s1 + z * s2;
@@ -229,20 +239,28 @@ __global__ void rbgs_first_k(Grid g, Grid gc, const T* __restrict__ L, const T* 
     const int xl = (g.isper(0) && x == 1) ? g.n[0] - 2 : x - 1, xh = (g.isper(0) && x == g.n[0] - 2) ? 1 : x + 1;
     const int yl = (g.isper(1) && y == 1) ? g.n[1] - 2 : y - 1, yh = (g.isper(1) && y == g.n[1] - 2) ? 1 : y + 1;
     const T* L1 = L + g.N;
-    T a = L[I] * first_nb<T, PROL>(g, gc, b, iD, xc, xv, I + o.xl, xl, y, z) +
-          L[I + 1] * first_nb<T, PROL>(g, gc, b, iD, xc, xv, I + o.xh, xh, y, z);
-    a += L1[I] * first_nb<T, PROL>(g, gc, b, iD, xc, xv, I + o.yl, x, yl, z) +
-         L1[I + s1] * first_nb<T, PROL>(g, gc, b, iD, xc, xv, I + o.yh, x, yh, z);
+    T a = L[I] * first_nb<T, PROL>(g, gc, b, iD, xc, xv, I + o.xl, xl, y, z, omega) +
+          L[I + 1] * first_nb<T, PROL>(g, gc, b, iD, xc, xv, I + o.xh, xh, y, z, omega);
+    a += L1[I] * first_nb<T, PROL>(g, gc, b, iD, xc, xv, I + o.yl, x, yl, z, omega) +
+         L1[I + s1] * first_nb<T, PROL>(g, gc, b, iD, xc, xv, I + o.yh, x, yh, z, omega);
     if (D == 3) {
         const int zl = (g.isper(2) && z == 1) ? g.n[2] - 2 : z - 1, zh = (g.isper(2) && z == g.n[2] - 2) ? 1 : z + 1;
         const T* L2 = L1 + g.N;
-        a += L2[I] * first_nb<T, PROL>(g, gc, b, iD, xc, xv, I + o.zl, x, y, zl) +
-             L2[I + s2] * first_nb<T, PROL>(g, gc, b, iD, xc, xv, I + o.zh, x, y, zh);
+        a += L2[I] * first_nb<T, PROL>(g, gc, b, iD, xc, xv, I + o.zl, x, y, zl, omega) +
+             L2[I + s2] * first_nb<T, PROL>(g, gc, b, iD, xc, xv, I + o.zh, x, y, zh, omega);
     }
     const T dd = diag7<D>(g, L, I);
     const T eps = sizeof(T) == 8 ? T(2.220446049250313e-16) : T(1.1920929e-7);
     const T iDI = (dd * dd < T(2) * eps) ? T(0) : T(1) / dd;
-    xv[I] = (b[I] - a) * iDI;
+    const T gs = (b[I] - a) * iDI;
+    if (omega == T(1)) {
+        xv[I] = gs;
+    } else if (PROL) {   // over-relaxation from the prolongated value of this (black) cell
+        const T xo = xv[I] + xc[lin(gc, (x + 1) / 2, (y + 1) / 2, D == 3 ? (z + 1) / 2 : 0)];
+        xv[I] = xo + omega * (gs - xo);
+    } else {             // from x = 0
+        xv[I] = omega * gs;
+    }
 }
 
 // ---- temporally blocked red-black Gauss-Seidel (3D, FP32): S half-sweeps in one launch.
@@ -889,12 +907,11 @@ __global__ void add_correction_k(Grid g, const float* __restrict__ e, double* __
     ROWS_END
 }
 
-// periodic ghosts of a scalar (WaterLily perBC!)
+// periodic ghosts of a scalar (WaterLily perBC!), one thread per cell of the boundary planes
 __global__ void perbc_k(Grid g, double* a) {
-    const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y;
-    const int z = blockIdx.z;
-    if (x >= g.n[0] || y >= g.n[1]) return;
-    int c[3] = {x, y, z};
+    int c[3];
+    if (!bc_plane_cell(g, blockIdx.x * (long long)blockDim.x + threadIdx.x, c)) return;
+    const int x = c[0], y = c[1], z = c[2];
     bool any = false;
     for (int e = 0; e < g.D; ++e)
         if (g.isper(e) && (c[e] == 0 || c[e] == g.n[e] - 1)) {
@@ -925,7 +942,7 @@ static int tb_zchunk(const Grid& g, int S, int nsm) {
 // the blocked smoother runs the FP32 V-cycle of a 3D level with an even number of interior
 // cells in every dimension (every level but the coarsest), for nu1, nu2 in {1, 2}
 static bool tb_usable(const PoissonMG* mg, const Grid& g) {
-    if (mg->smoother != IA_SMOOTHER_BLOCKED || g.D != 3) return false;
+    if (mg->smoother != IA_SMOOTHER_BLOCKED || g.D != 3 || mg->omega != 1.0) return false;
     if (mg->nu1 < 1 || mg->nu1 > 2 || mg->nu2 < 1 || mg->nu2 > 2) return false;
     for (int e = 0; e < 3; ++e)
         if ((g.n[e] - 2) % 2 != 0) return false;
@@ -993,21 +1010,26 @@ static cudaError_t vcycle(ia_handle* h, PoissonMG* mg, int l, cudaStream_t st, i
     }
     auto half = [&](int color) {
         const int tk = (l == 0) ? timing_begin(h, TK_MG_FINE) : -1;
-        if (L.g.D == 3) { rbgs_pair_k<T, 3><<<pair_grid(L.g), blk(), 0, st>>>(L.g, Lc, b, x, color); ia::note_launch(); }
-        else { rbgs_pair_k<T, 2><<<pair_grid(L.g), blk(), 0, st>>>(L.g, Lc, b, x, color); ia::note_launch(); }
+        if (L.g.D == 3) { rbgs_pair_k<T, 3><<<pair_grid(L.g), blk(), 0, st>>>(L.g, Lc, b, x, color, T(mg->omega)); ia::note_launch(); }
+        else { rbgs_pair_k<T, 2><<<pair_grid(L.g), blk(), 0, st>>>(L.g, Lc, b, x, color, T(mg->omega)); ia::note_launch(); }
         timing_end(h, tk);
     };
     auto& C = mg->lev[l + 1];
+    // over-relaxed updates read the cell's own previous value: the red values of the first sweep
+    // are then stored, and the post-smoothing's first red half-sweep adds the coarse correction
+    // to the value it reads
+    const bool relax = mg->omega != 1.0;
+    const int write_red = (nu1 == 1 || relax) ? 1 : 0;
     // first black half-sweep: from x = 0 (pre) or from x + P(x_coarse) (post)
     auto first = [&](bool prol) {
         const int tk = (l == 0) ? timing_begin(h, TK_MG_FIRST) : -1;
         const T* xc = C.template x_<T>();
         if (L.g.D == 3) {
-            if (prol) rbgs_first_k<T, 3, true><<<pair_grid(L.g), blk(), 0, st>>>(L.g, C.g, Lc, b, iD, xc, x, 0);
-            else rbgs_first_k<T, 3, false><<<pair_grid(L.g), blk(), 0, st>>>(L.g, C.g, Lc, b, iD, xc, x, nu1 == 1);
+            if (prol) rbgs_first_k<T, 3, true><<<pair_grid(L.g), blk(), 0, st>>>(L.g, C.g, Lc, b, iD, xc, x, 0, T(mg->omega));
+            else rbgs_first_k<T, 3, false><<<pair_grid(L.g), blk(), 0, st>>>(L.g, C.g, Lc, b, iD, xc, x, write_red, T(mg->omega));
         } else {
-            if (prol) rbgs_first_k<T, 2, true><<<pair_grid(L.g), blk(), 0, st>>>(L.g, C.g, Lc, b, iD, xc, x, 0);
-            else rbgs_first_k<T, 2, false><<<pair_grid(L.g), blk(), 0, st>>>(L.g, C.g, Lc, b, iD, xc, x, nu1 == 1);
+            if (prol) rbgs_first_k<T, 2, true><<<pair_grid(L.g), blk(), 0, st>>>(L.g, C.g, Lc, b, iD, xc, x, 0, T(mg->omega));
+            else rbgs_first_k<T, 2, false><<<pair_grid(L.g), blk(), 0, st>>>(L.g, C.g, Lc, b, iD, xc, x, write_red, T(mg->omega));
         }
         ia::note_launch();
         timing_end(h, tk);
@@ -1026,7 +1048,16 @@ static cudaError_t vcycle(ia_handle* h, PoissonMG* mg, int l, cudaStream_t st, i
         return cudaGetLastError();
     }
     first(true);
-    half(0);
+    if (relax) {   // the red cells still hold x without the coarse correction
+        const int tk = (l == 0) ? timing_begin(h, TK_MG_FINE) : -1;
+        const T* xc = C.template x_<T>();
+        if (L.g.D == 3) rbgs_pair_k<T, 3, true><<<pair_grid(L.g), blk(), 0, st>>>(L.g, Lc, b, x, 0, T(mg->omega), C.g, xc);
+        else rbgs_pair_k<T, 2, true><<<pair_grid(L.g), blk(), 0, st>>>(L.g, Lc, b, x, 0, T(mg->omega), C.g, xc);
+        ia::note_launch();
+        timing_end(h, tk);
+    } else {
+        half(0);
+    }
     for (int k = 1; k < nu2; ++k) {
         half(1);
         half(0);
@@ -1040,7 +1071,8 @@ static cudaError_t vcycle_run(ia_handle* h, PoissonMG* mg, cudaStream_t st) {
     if (h->timing.on) return vcycle<T>(h, mg, 0, st, mg->nu1, mg->nu2, mg->nuc);
     const int k = sizeof(T) == 4 ? 0 : 1;
     int* nu = mg->vgraph_nu[k];
-    if (mg->vgraph[k] && (nu[0] != mg->nu1 || nu[1] != mg->nu2 || nu[2] != mg->nuc || nu[3] != mg->smoother)) {
+    if (mg->vgraph[k] && (nu[0] != mg->nu1 || nu[1] != mg->nu2 || nu[2] != mg->nuc || nu[3] != mg->smoother ||
+                          mg->vgraph_omega[k] != mg->omega)) {
         cudaGraphExecDestroy(mg->vgraph[k]);
         mg->vgraph[k] = nullptr;
     }
@@ -1069,6 +1101,7 @@ static cudaError_t vcycle_run(ia_handle* h, PoissonMG* mg, cudaStream_t st) {
         nu[1] = mg->nu2;
         nu[2] = mg->nuc;
         nu[3] = mg->smoother;
+        mg->vgraph_omega[k] = mg->omega;
     }
     note_launches(mg->vgraph_kernels[k]);
     return cudaGraphLaunch(mg->vgraph[k], st);
@@ -1392,7 +1425,7 @@ static int poisson_solve_mixed(ia_handle* h, double* xv, const double* zz, const
             mg->stats[2]++;
         }
     }
-    { perbc_k<<<gb, blk(), 0, st>>>(g, xv); ia::note_launch(); }
+    { perbc_k<<<unsigned((bc_plane_cells(g) + 255) / 256), 256, 0, st>>>(g, xv); ia::note_launch(); }
     if (cudaGetLastError() != cudaSuccess) return IA_ERR_CUDA;
     *iters = total;
     *resid = res;
@@ -1465,7 +1498,7 @@ int poisson_solve(ia_handle* h, double* xv, const double* zz, const double* L, d
         alpha_prev = alpha;
         ++it;
     }
-    { perbc_k<<<gb, blk(), 0, st>>>(g, xv); ia::note_launch(); }
+    { perbc_k<<<unsigned((bc_plane_cells(g) + 255) / 256), 256, 0, st>>>(g, xv); ia::note_launch(); }
     if (cudaGetLastError() != cudaSuccess) return IA_ERR_CUDA;
     *iters = it;
     *resid = res;

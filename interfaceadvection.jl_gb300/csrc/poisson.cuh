@@ -52,6 +52,7 @@ struct PoissonMG {
     double* hsc = nullptr;                                            // pinned host scalars
     int nu1 = 2, nu2 = 2, nuc = 16;
     int smoother = 0;                                                 // IA_SMOOTHER_* (FP32 V-cycle)
+    double omega = 1.15;                                              // smoother relaxation factor
     int nsm = 0;                                                      // multiprocessors of the device
     // each precision's finest-level V-cycle is captured once into a CUDA graph (its launch
     // sequence and arguments are fixed for the handle) and replayed; recaptured when the
@@ -59,6 +60,7 @@ struct PoissonMG {
     cudaGraphExec_t vgraph[2] = {nullptr, nullptr};   // FP32, FP64
     long long vgraph_kernels[2] = {0, 0};
     int vgraph_nu[2][4] = {{0, 0, 0, 0}, {0, 0, 0, 0}};
+    double vgraph_omega[2] = {1.0, 1.0};
     cudaStream_t capture = nullptr;
 };
 

@@ -316,6 +316,13 @@ int ia_poisson_mg_params(ia_handle* h, int32_t nu1, int32_t nu2, int32_t nuc) {
     return IA_OK;
 }
 
+int ia_poisson_mg_relax(ia_handle* h, double omega) {
+    if (!h || !(omega > 0.0) || !(omega < 2.0)) return IA_ERR_INVALID;
+    if (ensure_scratch(h) != IA_OK) return IA_ERR_CUDA;
+    h->mg->omega = omega;
+    return IA_OK;
+}
+
 int ia_poisson_smoother(ia_handle* h, int32_t kind) {
     if (!h || (kind != IA_SMOOTHER_HALFSWEEP && kind != IA_SMOOTHER_BLOCKED)) return IA_ERR_INVALID;
     if (ensure_scratch(h) != IA_OK) return IA_ERR_CUDA;

@@ -5,7 +5,7 @@
 // deterministic interior sum used for mass diagnostics.
 #include <cuda_runtime.h>
 
-#include "ia_core.cuh"
+#include "ia_bc.cuh"
 #include "ia_geom.cuh"
 #include "vof.cuh"
 
@@ -40,9 +40,12 @@ __global__ void apply_vof_k(Grid g, const double* __restrict__ sdf, double* f, d
     f[I] = (v < tol) ? 0.0 : ((v > 1.0 - tol) ? 1.0 : v);
 }
 
+// one thread per cell of the boundary planes (bc_plane_cell); the interior cells among them return
 __global__ void ghosts_k(Grid g, double* f) {
-    const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y, z = blockIdx.z;
-    if (x >= g.n[0] || y >= g.n[1] || interior(g, x, y, z)) return;
+    int cc[3];
+    if (!bc_plane_cell(g, blockIdx.x * (long long)blockDim.x + threadIdx.x, cc)) return;
+    const int x = cc[0], y = cc[1], z = cc[2];
+    if (interior(g, x, y, z)) return;
     const int sz = g.D == 3 ? bc_src(g, 2, z) : 0;
     f[lin(g, x, y, z)] = f[lin(g, bc_src(g, 0, x), bc_src(g, 1, y), sz)];
 }
@@ -71,8 +74,10 @@ __global__ void reconstruct_k(Grid g, int scheme, const double* __restrict__ f, 
 // BCVOF! ghosts: f from the full boundary map; α, n̂ copied only along
 // periodic dimensions (zero-gradient sides leave them untouched).
 __global__ void bcvof_ghosts_k(Grid g, double* f, double* alpha, double* nhat) {
-    const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y, z = blockIdx.z;
-    if (x >= g.n[0] || y >= g.n[1] || interior(g, x, y, z)) return;
+    int cc[3];
+    if (!bc_plane_cell(g, blockIdx.x * (long long)blockDim.x + threadIdx.x, cc)) return;
+    const int x = cc[0], y = cc[1], z = cc[2];
+    if (interior(g, x, y, z)) return;
     const long long O = lin(g, x, y, z);
     const int sz = g.D == 3 ? bc_src(g, 2, z) : 0;
     f[O] = f[lin(g, bc_src(g, 0, x), bc_src(g, 1, y), sz)];
@@ -158,7 +163,7 @@ inline dim3 grd3(const Grid& g) { return dim3((g.n[0] + 31) / 32, (g.n[1] + 7) /
 }  // namespace
 
 cudaError_t fill_ghosts_scalar(const Grid& g, double* f, cudaStream_t st) {
-    { ghosts_k<<<grd3(g), blk3(), 0, st>>>(g, f); ia::note_launch(); }
+    { ghosts_k<<<unsigned((bc_plane_cells(g) + 255) / 256), 256, 0, st>>>(g, f); ia::note_launch(); }
     return cudaGetLastError();
 }
 
@@ -175,7 +180,7 @@ cudaError_t reconstruct(const Grid& g, int scheme, double* f, double* alpha, dou
     else { reconstruct_k<3><<<grd3(g), blk3(), 0, st>>>(g, scheme, f, alpha, nhat); ia::note_launch(); }
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
-    { bcvof_ghosts_k<<<grd3(g), blk3(), 0, st>>>(g, f, alpha, nhat); ia::note_launch(); }
+    { bcvof_ghosts_k<<<unsigned((bc_plane_cells(g) + 255) / 256), 256, 0, st>>>(g, f, alpha, nhat); ia::note_launch(); }
     return cudaGetLastError();
 }
 

@@ -94,6 +94,7 @@ _SIGS = {
     "ia_poisson_stats": (C.c_int, [C.c_void_p, C.c_void_p]),
     "ia_poisson_mg_params": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.c_int32]),
     "ia_poisson_smoother": (C.c_int, [C.c_void_p, C.c_int32]),
+    "ia_poisson_mg_relax": (C.c_int, [C.c_void_p, C.c_double]),
     "ia_poisson_residual": (C.c_int, [C.c_void_p] * 5 + [C.POINTER(C.c_double)]),
     "ia_metrics": (C.c_int, [C.c_void_p] * 8),
     "ia_levelset_init": (C.c_int, [C.c_void_p] * 4),

@@ -101,10 +101,13 @@ def set_learned(handle, precond="hybrid", weights=None, inner_max=30, inner_rtol
                            int(inner_max), float(inner_rtol)), "ia_poisson_precond")
 
 
-def set_smoother(handle, kind: str = "halfsweep") -> None:
+def set_smoother(handle, kind: str = "halfsweep", omega: float | None = None) -> None:
     """Smoother of the FP32 V-cycle: "halfsweep" (one launch per red-black half-sweep, the default)
-    or "blocked" (all half-sweeps of a smoothing in one z-wavefront launch); same arithmetic."""
+    or "blocked" (all half-sweeps of a smoothing in one z-wavefront launch, relaxation factor 1 only);
+    same arithmetic.  omega sets the half-sweeps' over-relaxation x += ω (x_GS - x) (default 1.15)."""
     _lib.check(handle.call("ia_poisson_smoother", _lib.SMOOTHERS[kind]), "ia_poisson_smoother")
+    if omega is not None:
+        _lib.check(handle.call("ia_poisson_mg_relax", float(omega)), "ia_poisson_mg_relax")
 
 
 def poisson_stats(handle) -> dict:

@@ -206,11 +206,13 @@ def test_broken_weights_fall_back_to_vcycle(system):
 
 def test_untrained_hybrid_matches_vcycle_iterations_when_net_is_zero(system):
     # zero weights: the net outputs zero, ω = 0 and the hybrid is exactly the V-cycle preconditioner
+    # of the same solver settings
     L, z = system
     zero = np.zeros(learned.param_count(), dtype=np.float32)
-    _, it_h, res_h, st = solve("learned", L, z, precond="hybrid", weights=zero)
-    _, it_m, res_m, _ = solve("mixed", L, z)
-    assert it_h == it_m and res_h <= 1e-8 and st["fallbacks"] == 0
+    x_h, it_h, res_h, st = solve("learned", L, z, precond="hybrid", weights=zero)
+    x_v, it_v, res_v, _ = solve("learned", L, z, precond="vcycle", weights=zero)
+    assert it_h == it_v and res_h <= 1e-8 and st["fallbacks"] == 0
+    assert torch.equal(x_h, x_v)
 
 
 def _cos(a, b):
