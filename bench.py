@@ -45,7 +45,7 @@ TRAFFIC_VOF_BULK_PER_CELL = 31.1   # vof_bulk, ncu capture at 192³ (profiles/vo
 B_BULK_PER_CELL = 33       # vof_bulk: read f, u_d, u0_d (24) + c̄ (1); write ρuf_d (8)
 TK = {"vof_bulk": 0, "vof_cells": 1, "ustar": 2, "forcing": 3, "mg_vcycle": 4, "mg_transfer": 6, "krylov": 7,
       "vof_faces": 9, "momflux": 10, "momupdate": 11, "update_project": 12, "mg_fine_rbgs": 13, "nn_precond": 14,
-      "mg_fine_first": 15}
+      "mg_fine_first": 15, "other": 8}
 
 
 def parse():

@@ -650,6 +650,8 @@ __global__ void surften_kern(MomConsts k, int d, const double* __restrict__ f, c
 }
 
 // ------------------------------------------------------------------ update, L, projection
+// A0: a = 0 (the corrector, w = 1), where a·ρu⁰ only adds a zero: ρu⁰ is then not formed
+template <bool A0>
 __global__ void updateu_kern(MomConsts k, double* __restrict__ u, double* __restrict__ rhou,
                              const double* __restrict__ u0, const double* __restrict__ F, double dt,
                              const double* __restrict__ fref, const double* __restrict__ fupd, double w, double a,
@@ -659,8 +661,13 @@ __global__ void updateu_kern(MomConsts k, double* __restrict__ u, double* __rest
     const long long I = lin(g, x, y, z);
     for (int i = 0; i < g.D; ++i) {
         const long long q = I + i * g.N;
-        const double rho0 = mul_rho(k, u0[q], fref[I], fref[I - g.s[i]]);   // u2ρu!(n̂, u⁰, c.f)
-        const double rn = (a * rho0 + rhou[q] + F[q] * dt) * w;
+        double rn;
+        if (A0) {
+            rn = (rhou[q] + F[q] * dt) * w;
+        } else {
+            const double rho0 = mul_rho(k, u0[q], fref[I], fref[I - g.s[i]]);   // u2ρu!(n̂, u⁰, c.f)
+            rn = (a * rho0 + rhou[q] + F[q] * dt) * w;
+        }
         double v = div_rho(k, rn, fupd[I], fupd[I - g.s[i]]);
         if (k.has_g) v = (dt * w) * k.gvec[i] + v;
         u[q] = v;
@@ -857,7 +864,8 @@ cudaError_t k_surften(const MomConsts& k, int d, const double* f, double eta, do
 cudaError_t k_updateu(const MomConsts& k, double* u, double* rhou, const double* u0, const double* F, double dt,
                       const double* fref, const double* fupd, double w, bool write_rhou, cudaStream_t s) {
     const double a = 1.0 / w - 1.0;
-    { updateu_kern<<<igrd(k.g), blk(), 0, s>>>(k, u, rhou, u0, F, dt, fref, fupd, w, a, write_rhou); ia::note_launch(); }
+    if (a == 0.0) { updateu_kern<true><<<igrd(k.g), blk(), 0, s>>>(k, u, rhou, u0, F, dt, fref, fupd, w, a, write_rhou); ia::note_launch(); }
+    else { updateu_kern<false><<<igrd(k.g), blk(), 0, s>>>(k, u, rhou, u0, F, dt, fref, fupd, w, a, write_rhou); ia::note_launch(); }
     return cudaGetLastError();
 }
 cudaError_t k_updatel(const MomConsts& k, double* mu0, const double* f, cudaStream_t s) {

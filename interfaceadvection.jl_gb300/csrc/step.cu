@@ -209,9 +209,11 @@ int ia_mom_step(ia_handle* h, double dt, int64_t n_dt, double t_now, ia_status* 
     ia_status S;
     std::memset(&S, 0, sizeof(S));
     // ---- predictor: u(n) → u(n+½) with u(n)
+    int tk = timing_begin(h, TK_UPDATE);
     cudaMemcpyAsync(F.u0, F.u, 8 * NV, cudaMemcpyDeviceToDevice, st);
     cudaMemcpyAsync(F.f0, F.f, 8 * N, cudaMemcpyDeviceToDevice, st);
     if (k_u2rhou(k, F.rhou, F.u0, F.f0, st) != cudaSuccess) return IA_ERR_CUDA;
+    timing_end(h, tk);
     int rc = status_reset(h);
     if (rc == IA_OK) rc = advect_fq(h, F.f0, F.u0, F.u, F.u, dt, dirs, 0);
     if (rc != IA_OK) return rc;
@@ -220,10 +222,14 @@ int ia_mom_step(ia_handle* h, double dt, int64_t n_dt, double t_now, ia_status* 
         if (status) *status = S;
         return rc;
     }
+    tk = timing_begin(h, TK_UPDATE);
     if (k_average(F.f0, F.f, N, st) != cudaSuccess) return IA_ERR_CUDA;          // f⁰ = (f⁰ + f)/2
+    timing_end(h, tk);
     if ((rc = visc_surften(h, F.f0)) != IA_OK) return rc;
+    tk = timing_begin(h, TK_UPDATE);
     if (k_updateu(k, F.u, F.rhou, F.u0, F.force, dt, F.f, F.f0, 0.5, false, st) != cudaSuccess) return IA_ERR_CUDA;
     if (k_bc_vel(k, F.u, h->cfg.uBC, st) != cudaSuccess) return IA_ERR_CUDA;
+    timing_end(h, tk);
     int it0 = 0;
     double r0 = 0.0;
     rc = project(h, F.f0, 0.5 * dt, &it0, &r0);
@@ -232,8 +238,10 @@ int ia_mom_step(ia_handle* h, double dt, int64_t n_dt, double t_now, ia_status* 
     S.poisson_iters[0] = it0;
     S.poisson_resid[0] = r0;
     // ---- corrector: u(n) → u(n+1) with u(n+½)
+    tk = timing_begin(h, TK_UPDATE);
     cudaMemcpyAsync(F.f0, F.f, 8 * N, cudaMemcpyDeviceToDevice, st);
     if (k_u2rhou(k, F.rhou, F.u0, F.f, st) != cudaSuccess) return IA_ERR_CUDA;
+    timing_end(h, tk);
     rc = status_reset(h);
     if (rc == IA_OK) rc = advect_fq(h, F.f, F.u, F.u, F.u0, dt, dirs, 8);
     if (rc != IA_OK) return rc;
@@ -244,9 +252,11 @@ int ia_mom_step(ia_handle* h, double dt, int64_t n_dt, double t_now, ia_status* 
     }
     if ((rc = visc_surften(h, F.f)) != IA_OK) return rc;
     // a = 0 for w = 1, so ρu⁰ only enters as 0·ρu⁰; u⁰ takes u(n+½) first (src/flow.jl:100)
+    tk = timing_begin(h, TK_UPDATE);
     cudaMemcpyAsync(F.u0, F.u, 8 * NV, cudaMemcpyDeviceToDevice, st);
     if (k_updateu(k, F.u, F.rhou, F.u0, F.force, dt, F.f, F.f, 1.0, true, st) != cudaSuccess) return IA_ERR_CUDA;
     if (k_bc_vel(k, F.u, h->cfg.uBC, st) != cudaSuccess) return IA_ERR_CUDA;
+    timing_end(h, tk);
     int it1 = 0;
     double r1 = 0.0;
     rc = project(h, F.f, dt, &it1, &r1);
@@ -255,7 +265,10 @@ int ia_mom_step(ia_handle* h, double dt, int64_t n_dt, double t_now, ia_status* 
     S.poisson_iters[1] = it1;
     S.poisson_resid[1] = r1;
     double cfl = 0.0;
-    if ((rc = mpcfl(h, &cfl)) != IA_OK) return rc;
+    tk = timing_begin(h, TK_OTHER);
+    rc = mpcfl(h, &cfl);
+    timing_end(h, tk);
+    if (rc != IA_OK) return rc;
     S.dt_next = cfl < 1.2 * dt ? cfl : 1.2 * dt;                                 // push!(Δt, min(MPCFL, 1.2δt))
     int code = IA_OK;
     if (S.flags & (IA_FLAG_OVERFILL | IA_FLAG_UNDERFILL)) code = IA_WARN_FILL;
