@@ -678,24 +678,6 @@ __global__ void true_resid_k(Grid g, const double* __restrict__ L, const double*
     if (threadIdx.x == 0) atomicMax(linf, m);
 }
 
-// finest-level set-up of the mixed solver in one pass: FP32 face coefficients of every cell and
-// ghost (to_f32_k), and on interior cells the FP64 diagonal (set_diag64_k) and the FP32 inverse
-// diagonal of the converted coefficients (set_diag_k<float>)
-__global__ void setup_mixed_k(Grid g, const double* __restrict__ L, double* __restrict__ diag64,
-                              float* __restrict__ L32, float* __restrict__ iD32) {
-    const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y;
-    const int z = blockIdx.z;
-    if (x >= g.n[0] || y >= g.n[1]) return;
-    const long long I = lin(g, x, y, z);
-    for (int i = 0; i < g.D; ++i) L32[I + i * g.N] = float(L[I + i * g.N]);
-    const int c[3] = {x, y, z};
-    if (!is_interior(g, c)) return;
-    diag64[I] = diag_of(g, L, I);
-    float dd = 0.f;
-    for (int i = 0; i < g.D; ++i) dd -= float(L[I + i * g.N]) + float(L[I + g.s[i] + i * g.N]);
-    iD32[I] = (dd * dd < 2.f * 1.1920929e-7f) ? 0.f : 1.f / dd;
-}
-
 // q = A p and partial dot p·q
 template <int D>
 __global__ void matvec_dot_k(Grid g, const double* __restrict__ L, const double* __restrict__ diag,
@@ -1234,8 +1216,8 @@ static cudaError_t mg_setup(ia_handle* h, const double* L0) {
     const bool mixed = h->cfg.poisson_mode != IA_POISSON_FP64;
     MGLevel& F = mg->lev[0];
     const long long nv = F.g.N * F.g.D;
+    { set_diag64_k<<<mg->kb, KTHREADS, 0, st>>>(F.g, L0, mg->diag64); ia::note_launch(); }
     if (!mixed) {
-        { set_diag64_k<<<mg->kb, KTHREADS, 0, st>>>(F.g, L0, mg->diag64); ia::note_launch(); }
         cudaMemcpyAsync(F.L, L0, 8 * nv, cudaMemcpyDeviceToDevice, st);
         { set_diag_k<double><<<grd(F.g), blk(), 0, st>>>(F.g, F.L, F.iD); ia::note_launch(); }
         for (int l = 1; l < mg->nlev; ++l) {
@@ -1244,7 +1226,10 @@ static cudaError_t mg_setup(ia_handle* h, const double* L0) {
             { set_diag_k<double><<<grd(mg->lev[l].g), blk(), 0, st>>>(mg->lev[l].g, mg->lev[l].L, mg->lev[l].iD); ia::note_launch(); }
         }
     } else {
-        { setup_mixed_k<<<grd(F.g), blk(), 0, st>>>(F.g, L0, mg->diag64, F.L32, F.iD32); ia::note_launch(); }
+        // the FP64 -> FP32 conversion runs in a memory-bound pass of its own: conversions issue on
+        // the FP64 pipe, which the FP64 diagonal pass already saturates
+        { to_f32_k<<<1216, 256, 0, st>>>(nv, L0, F.L32); ia::note_launch(); }
+        { set_diag_k<float><<<grd(F.g), blk(), 0, st>>>(F.g, F.L32, F.iD32); ia::note_launch(); }
         for (int l = 1; l < mg->nlev; ++l) {
             { restrict_L_k<float><<<grd(mg->lev[l].g), blk(), 0, st>>>(mg->lev[l].g, mg->lev[l - 1].g,
                                                                       mg->lev[l - 1].L32, mg->lev[l].L32); ia::note_launch(); }
