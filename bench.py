@@ -283,21 +283,31 @@ def run_bubble(args, world, local_rank):
         # state kept on the host: each step uploads u and f from pinned memory, runs the step through the
         # public API and downloads u, f, p
         fl, it = sim.flow, sim.intf
-        hu = torch.empty(fl.u.shape, dtype=torch.float64, pin_memory=True).copy_(fl.u)
-        hf = torch.empty(it.f.shape, dtype=torch.float64, pin_memory=True).copy_(it.f)
-        hp = torch.empty(fl.p.shape, dtype=torch.float64, pin_memory=True)
+        # pinned host state in the fields' own (column-major) layout, so that each copy is one DMA
+        pinned = lambda t: torch.empty_strided(t.shape, t.stride(), dtype=t.dtype, pin_memory=True)
+        hu = pinned(fl.u).copy_(fl.u)
+        hf = pinned(it.f).copy_(it.f)
+        hp = pinned(fl.p)
         e_steps = max(2, min(args.steps, 4))
         torch.cuda.synchronize()
         barrier()
         t0 = time.perf_counter()
+        # the link copies ~200 GB/s one way and ~340 GB/s both ways at once: the downloads of f and p
+        # run on a second stream, beside the next step's upload of u.  Every copy still follows what
+        # it depends on: u is uploaded after its download (same stream), f after its download and the
+        # next step's kernels after the download of p (the f upload waits for the second stream)
+        main, side = torch.cuda.current_stream(), torch.cuda.Stream()
         for _ in range(e_steps):
             fl.u.copy_(hu, non_blocking=True)
+            main.wait_stream(side)
             it.f.copy_(hf, non_blocking=True)
             ia.sim_step(sim)
             hu.copy_(fl.u, non_blocking=True)
-            hf.copy_(it.f, non_blocking=True)
-            hp.copy_(fl.p, non_blocking=True)
-            torch.cuda.synchronize()
+            side.wait_stream(main)
+            with torch.cuda.stream(side):
+                hf.copy_(it.f, non_blocking=True)
+                hp.copy_(fl.p, non_blocking=True)
+        torch.cuda.synchronize()
         barrier()
         el = time.perf_counter() - t0
         nb = fl.u.numel() * 8 + it.f.numel() * 8
