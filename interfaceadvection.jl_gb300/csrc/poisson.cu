@@ -235,20 +235,43 @@ __global__ void rbgs_first_k(Grid g, Grid gc, const T* __restrict__ L, const T* 
     }
     if (x > g.n[0] - 2) return;
     const int I = x + y * s1 + z * s2;
-    const Nb o = nb_of<D>(g, x, y, z);
-    const int xl = (g.isper(0) && x == 1) ? g.n[0] - 2 : x - 1, xh = (g.isper(0) && x == g.n[0] - 2) ? 1 : x + 1;
-    const int yl = (g.isper(1) && y == 1) ? g.n[1] - 2 : y - 1, yh = (g.isper(1) && y == g.n[1] - 2) ? 1 : y + 1;
     const T* L1 = L + g.N;
-    T a = L[I] * first_nb<T, PROL>(g, gc, b, iD, xc, xv, I + o.xl, xl, y, z, omega) +
-          L[I + 1] * first_nb<T, PROL>(g, gc, b, iD, xc, xv, I + o.xh, xh, y, z, omega);
-    a += L1[I] * first_nb<T, PROL>(g, gc, b, iD, xc, xv, I + o.yl, x, yl, z, omega) +
-         L1[I + s1] * first_nb<T, PROL>(g, gc, b, iD, xc, xv, I + o.yh, x, yh, z, omega);
-    if (D == 3) {
-        const int zl = (g.isper(2) && z == 1) ? g.n[2] - 2 : z - 1, zh = (g.isper(2) && z == g.n[2] - 2) ? 1 : z + 1;
-        const T* L2 = L1 + g.N;
-        a += L2[I] * first_nb<T, PROL>(g, gc, b, iD, xc, xv, I + o.zl, x, y, zl, omega) +
-             L2[I + s2] * first_nb<T, PROL>(g, gc, b, iD, xc, xv, I + o.zh, x, y, zh, omega);
+    const T* L2 = L1 + g.N;
+    // the six neighbour values, then one shared accumulation (the same sums in the same order
+    // whichever way the values were found)
+    T v[6] = {T(0), T(0), T(0), T(0), T(0), T(0)};
+    if (x >= 2 && x <= g.n[0] - 3 && y >= 2 && y <= g.n[1] - 3 && (D == 2 || (z >= 2 && z <= g.n[2] - 3))) {
+        // every neighbour interior, no wrap: the coarse parent of the neighbour below (above) along
+        // e is the cell's own parent, or the one below (above) when the coordinate is odd (even)
+        const int J[6] = {I - 1, I + 1, I - s1, I + s1, I - s2, I + s2};
+        if (PROL) {
+            const int g1 = int(gc.s[1]), g2 = int(gc.s[2]);
+            const int P = (x + 1) / 2 + ((y + 1) / 2) * g1 + (D == 3 ? ((z + 1) / 2) * g2 : 0);
+            const int Pn[6] = {P - ((x & 1) ? 1 : 0), P + ((x & 1) ? 0 : 1), P - ((y & 1) ? g1 : 0),
+                               P + ((y & 1) ? 0 : g1), P - ((z & 1) ? g2 : 0), P + ((z & 1) ? 0 : g2)};
+#pragma unroll
+            for (int q = 0; q < 2 * D; ++q) v[q] = xv[J[q]] + xc[Pn[q]];
+        } else {
+#pragma unroll
+            for (int q = 0; q < 2 * D; ++q) v[q] = omega == T(1) ? b[J[q]] * iD[J[q]] : omega * (b[J[q]] * iD[J[q]]);
+        }
+    } else {
+        const Nb o = nb_of<D>(g, x, y, z);
+        const int xl = (g.isper(0) && x == 1) ? g.n[0] - 2 : x - 1, xh = (g.isper(0) && x == g.n[0] - 2) ? 1 : x + 1;
+        const int yl = (g.isper(1) && y == 1) ? g.n[1] - 2 : y - 1, yh = (g.isper(1) && y == g.n[1] - 2) ? 1 : y + 1;
+        v[0] = first_nb<T, PROL>(g, gc, b, iD, xc, xv, I + o.xl, xl, y, z, omega);
+        v[1] = first_nb<T, PROL>(g, gc, b, iD, xc, xv, I + o.xh, xh, y, z, omega);
+        v[2] = first_nb<T, PROL>(g, gc, b, iD, xc, xv, I + o.yl, x, yl, z, omega);
+        v[3] = first_nb<T, PROL>(g, gc, b, iD, xc, xv, I + o.yh, x, yh, z, omega);
+        if (D == 3) {
+            const int zl = (g.isper(2) && z == 1) ? g.n[2] - 2 : z - 1, zh = (g.isper(2) && z == g.n[2] - 2) ? 1 : z + 1;
+            v[4] = first_nb<T, PROL>(g, gc, b, iD, xc, xv, I + o.zl, x, y, zl, omega);
+            v[5] = first_nb<T, PROL>(g, gc, b, iD, xc, xv, I + o.zh, x, y, zh, omega);
+        }
     }
+    T a = L[I] * v[0] + L[I + 1] * v[1];
+    a += L1[I] * v[2] + L1[I + s1] * v[3];
+    if (D == 3) a += L2[I] * v[4] + L2[I + s2] * v[5];
     const T dd = diag7<D>(g, L, I);
     const T eps = sizeof(T) == 8 ? T(2.220446049250313e-16) : T(1.1920929e-7);
     const T iDI = (dd * dd < T(2) * eps) ? T(0) : T(1) / dd;
