@@ -116,9 +116,7 @@ __global__ void ustar_kern(MomConsts k, const double* __restrict__ rhou, const d
 __global__ void u2rhou_kern(MomConsts k, double* __restrict__ rhou, const double* __restrict__ u,
                             const double* __restrict__ f) {
     const Grid& g = k.g;
-    GCELL_XYZ
-    const int c[3] = {x, y, z};
-    if (!is_interior(g, c)) return;
+    ICELL_XYZ
     const long long I = lin(g, x, y, z);
     for (int i = 0; i < g.D; ++i) rhou[I + i * g.N] = mul_rho(k, u[I + i * g.N], f[I], f[I - g.s[i]]);
 }
@@ -679,6 +677,11 @@ __global__ void updatel_kern(MomConsts k, double* __restrict__ mu0, const double
     const Grid& g = k.g;
     GCELL_XYZ
     const long long O = lin(g, x, y, z);
+    if (x >= 2 && x <= g.n[0] - 2 && y >= 2 && y <= g.n[1] - 2 && (g.D == 2 || (z >= 2 && z <= g.n[2] - 2))) {
+        const double fo = f[O];
+        for (int i = 0; i < g.D; ++i) mu0[O + i * g.N] = div_rho(k, 1.0, fo, f[O - g.s[i]]);
+        return;
+    }
     for (int i = 0; i < g.D; ++i) {
         int c[3] = {x, y, z};
         if (vel_bc(g, i, c)) { mu0[O + i * g.N] = 0.0; continue; }
@@ -783,7 +786,7 @@ cudaError_t k_ustar(const MomConsts& k, const double* rhou, const double* f, dou
     return cudaGetLastError();
 }
 cudaError_t k_u2rhou(const MomConsts& k, double* rhou, const double* u, const double* f, cudaStream_t s) {
-    { u2rhou_kern<<<ggrd(k.g), blk(), 0, s>>>(k, rhou, u, f); ia::note_launch(); }
+    { u2rhou_kern<<<igrd(k.g), blk(), 0, s>>>(k, rhou, u, f); ia::note_launch(); }
     return cudaGetLastError();
 }
 cudaError_t k_bc_vel(const MomConsts& k, double* a, const double* A, cudaStream_t s) {
