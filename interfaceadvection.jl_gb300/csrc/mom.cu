@@ -525,30 +525,34 @@ __device__ __forceinline__ bool mixed(double v) {
     return b != 0ull && b < kOneBits;   // 0 < v < 1 (sign bit set → huge, excluded)
 }
 
-// fᶠ along d, and the list of interior cells where it is mixed (the only cells surften_kern
-// changes), appended one warp at a time
-__global__ void fbuffer_kern(MomConsts k, int d, const double* __restrict__ f, double* __restrict__ fb,
+// fᶠ along every d in one pass over f, and per d the list of interior cells where fᶠ is mixed
+// (the only cells surften_kern changes), appended one warp at a time
+__global__ void fbuffer_kern(MomConsts k, const double* __restrict__ f, double* __restrict__ fb,
                              int* __restrict__ list, unsigned int* __restrict__ count) {
     const Grid& g = k.g;
     GCELL_XYZ
-    int c[3] = {x, y, z};
-    const bool inner = is_interior(g, c);
-    // BCf!(d, ·): the high ghost along a zero-gradient d is not written by the
-    // reference (it keeps older buffer contents); it is taken as a zero-gradient copy here.
-    if (face_bc(g, d, c)) c[d] = g.n[d] - 2;
-    const long long P = lin3(g, c);
-    const double fa = f[P], fm = f[P - g.s[d]];
-    const double v = (dbits(fa) == dbits(fm)) ? fa : (fa + fm) / 2.0;
+    const int c0[3] = {x, y, z};
+    const bool inner = is_interior(g, c0);
     const long long I = lin(g, x, y, z);
-    fb[I] = v;
-    const bool want = inner && mixed(v);
-    const unsigned int bal = __ballot_sync(__activemask(), want);
-    if (want) {
-        const int lane = int(threadIdx.x) & 31, leader = __ffs(bal) - 1;
-        unsigned int base = 0;
-        if (lane == leader) base = atomicAdd(count, unsigned(__popc(bal)));
-        base = __shfl_sync(bal, base, leader);
-        list[base + __popc(bal & ((1u << lane) - 1u))] = int(I);
+    const int lane = int(threadIdx.x) & 31;
+    for (int d = 0; d < g.D; ++d) {
+        int c[3] = {x, y, z};
+        // BCf!(d, ·): the high ghost along a zero-gradient d is not written by the
+        // reference (it keeps older buffer contents); it is taken as a zero-gradient copy here.
+        if (face_bc(g, d, c)) c[d] = g.n[d] - 2;
+        const long long P = lin3(g, c);
+        const double fa = f[P], fm = f[P - g.s[d]];
+        const double v = (dbits(fa) == dbits(fm)) ? fa : (fa + fm) / 2.0;
+        fb[d * g.N + I] = v;
+        const bool want = inner && mixed(v);
+        const unsigned int bal = __ballot_sync(__activemask(), want);
+        if (want) {
+            const int leader = __ffs(bal) - 1;
+            unsigned int base = 0;
+            if (lane == leader) base = atomicAdd(count + d, unsigned(__popc(bal)));
+            base = __shfl_sync(bal, base, leader);
+            list[d * g.N + base + __popc(bal & ((1u << lane) - 1u))] = int(I);
+        }
     }
 }
 
@@ -856,12 +860,17 @@ cudaError_t k_zero(double* a, long long n, cudaStream_t s) {
     { zero_kern<<<1216, 256, 0, s>>>(a, n); ia::note_launch(); }
     return cudaGetLastError();
 }
-cudaError_t k_surften(const MomConsts& k, int d, const double* f, double eta, double* fb, double* r, int* list,
+cudaError_t k_surften(const MomConsts& k, const double* f, double eta, double* fb, double* r, int* list,
                       unsigned int* count, cudaStream_t s) {
-    cudaMemsetAsync(count, 0, sizeof(unsigned int), s);
-    { fbuffer_kern<<<ggrd(k.g), blk(), 0, s>>>(k, d, f, fb, list, count); ia::note_launch(); }
-    if (k.g.D == 2) { surften_kern<2><<<608, 64, 0, s>>>(k, d, f, fb, eta, r, list, count); ia::note_launch(); }
-    else { surften_kern<3><<<608, 64, 0, s>>>(k, d, f, fb, eta, r, list, count); ia::note_launch(); }
+    const Grid& g = k.g;
+    cudaMemsetAsync(count, 0, sizeof(unsigned int) * g.D, s);
+    { fbuffer_kern<<<ggrd(g), blk(), 0, s>>>(k, f, fb, list, count); ia::note_launch(); }
+    for (int d = 0; d < g.D; ++d) {
+        double* fbd = fb + d * g.N;
+        const int* ld = list + d * g.N;
+        if (g.D == 2) { surften_kern<2><<<608, 64, 0, s>>>(k, d, f, fbd, eta, r, ld, count + d); ia::note_launch(); }
+        else { surften_kern<3><<<608, 64, 0, s>>>(k, d, f, fbd, eta, r, ld, count + d); ia::note_launch(); }
+    }
     return cudaGetLastError();
 }
 cudaError_t k_updateu(const MomConsts& k, double* u, double* rhou, const double* u0, const double* F, double dt,

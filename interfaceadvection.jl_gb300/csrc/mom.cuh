@@ -32,7 +32,8 @@ cudaError_t k_visc(const MomConsts& k, const double* u, const double* f, double 
                    double* r, cudaStream_t s);
 cudaError_t k_zero(double* a, long long n, cudaStream_t s);
 // surfTen! (src/surfaceTension.jl:8-20), one direction d
-cudaError_t k_surften(const MomConsts& k, int d, const double* f, double eta, double* fb, double* r, int* list,
+// surfTen! along every d: fb holds D face-fraction fields, list D cell lists of N entries, count D
+cudaError_t k_surften(const MomConsts& k, const double* f, double eta, double* fb, double* r, int* list,
                       unsigned int* count, cudaStream_t s);
 // updateU! (src/flow.jl:244-252) on interior cells; writes ρu when write_rhou
 cudaError_t k_updateu(const MomConsts& k, double* u, double* rhou, const double* u0, const double* F, double dt,

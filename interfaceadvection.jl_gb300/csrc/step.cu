@@ -15,9 +15,9 @@ struct MomScratch {
     double* ustar = nullptr;   // uStar: velocity of the momentum being advected (vector)
     double* Phi = nullptr;     // momentum face fluxes of one sweep (vector)
     double* Phi6 = nullptr;    // viscous face / edge fluxes (D(D+1)/2 scalars)
-    double* fb = nullptr;      // face fraction for surface tension
-    int* slist = nullptr;      // interior cells with a mixed face fraction
-    unsigned int* scount = nullptr;
+    double* fb = nullptr;      // face fractions for surface tension (D fields)
+    int* slist = nullptr;      // per d, the interior cells with a mixed face fraction (D lists of N)
+    unsigned int* scount = nullptr;   // D list lengths
     double* ft1 = nullptr;     // out-of-place VOF sweep buffers
     double* ft2 = nullptr;
     unsigned long long* cfl = nullptr;   // device max reductions (2)
@@ -54,9 +54,9 @@ static int ensure_scratch(ia_handle* h) {
     e = e ? e : cudaMalloc(&m->ustar, 8 * N * D);
     e = e ? e : cudaMalloc(&m->Phi, 8 * N * D);
     e = e ? e : cudaMalloc(&m->Phi6, 8 * N * npair);
-    e = e ? e : cudaMalloc(&m->fb, 8 * N);
-    e = e ? e : cudaMalloc(&m->slist, 4 * N);
-    e = e ? e : cudaMalloc(&m->scount, sizeof(unsigned int));
+    e = e ? e : cudaMalloc(&m->fb, 8 * N * D);
+    e = e ? e : cudaMalloc(&m->slist, 4 * N * D);
+    e = e ? e : cudaMalloc(&m->scount, sizeof(unsigned int) * D);
     e = e ? e : cudaMalloc(&m->ft1, 8 * N);
     e = e ? e : cudaMalloc(&m->ft2, 8 * N);
     e = e ? e : cudaMalloc(&m->cfl, 16);
@@ -131,10 +131,8 @@ static int visc_surften(ia_handle* h, const double* f) {
     if (h->cfg.mu != 0.0) e = k_visc(k, h->fld.u, f, h->cfg.lmu, h->cfg.mu, m->Phi6, h->fld.force, st);
     else e = k_zero(h->fld.force, g.N * g.D, st);
     if (e != cudaSuccess) return IA_ERR_CUDA;
-    if (h->cfg.eta != 0.0)
-        for (int d = 0; d < g.D; ++d)
-            if (k_surften(k, d, f, h->cfg.eta, m->fb, h->fld.force, m->slist, m->scount, st) != cudaSuccess)
-                return IA_ERR_CUDA;
+    if (h->cfg.eta != 0.0 && k_surften(k, f, h->cfg.eta, m->fb, h->fld.force, m->slist, m->scount, st) != cudaSuccess)
+        return IA_ERR_CUDA;
     timing_end(h, tk);
     return IA_OK;
 }
