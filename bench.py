@@ -40,7 +40,7 @@ PTOL = 1e-8
 B_RBGS_PER_CELL_F32 = 18   # one FP32 red-black half-sweep: L (12) + x read/write (4) + b (2) per cell
 # DRAM bytes per cell of that launch from an ncu capture of the same kernel at 160x320x160
 # (profiles/kernel_counters_bubble160.md), scaled by the cells of the launch
-TRAFFIC_RBGS_PER_CELL_F32 = 22.6
+TRAFFIC_RBGS_PER_CELL_F32 = 22.7
 TRAFFIC_VOF_BULK_PER_CELL = 31.1   # vof_bulk, ncu capture at 192³ (profiles/vof_bulk_sphere192.md)
 B_BULK_PER_CELL = 33       # vof_bulk: read f, u_d, u0_d (24) + c̄ (1); write ρuf_d (8)
 TK = {"vof_bulk": 0, "vof_cells": 1, "ustar": 2, "forcing": 3, "mg_vcycle": 4, "mg_transfer": 6, "krylov": 7,
@@ -275,7 +275,7 @@ def run_bubble(args, world, local_rank):
         ach = b / (fine["avg_launch_ms"] / 1e3) / 1e9
         roof = {"bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s", "frac": ach / peak,
                 "traffic": TRAFFIC_RBGS_PER_CELL_F32 * cells,
-                "traffic_note": "ncu dram bytes of the finest-level launch at 160x320x160 (22.6 B/cell), scaled",
+                "traffic_note": "ncu dram bytes of the finest-level launch at 160x320x160 (22.7 B/cell), scaled",
                 "kernel": "rbgs_pair_k<float> (finest-level red-black Gauss-Seidel half-sweep, mixed V-cycle)",
                 "peak_kind": peak_kind, "bytes_per_launch": b, "avg_launch_ms": fine["avg_launch_ms"]}
     e2e = None
