@@ -56,6 +56,7 @@ def test_config_validation_is_host_side(lib):
     assert lib.ia_advect_vof(None, None, None, None, 0.1, 1, None) == _lib.IA_ERR_INVALID
     assert lib.ia_poisson_smoother(None, _lib.SMOOTHERS["blocked"]) == _lib.IA_ERR_INVALID
     assert lib.ia_poisson_mg_params(None, 2, 2, 16) == _lib.IA_ERR_INVALID
+    assert lib.ia_poisson_mg_relax(None, 1.15) == _lib.IA_ERR_INVALID
 
 
 def test_split_order_matches_reference():
