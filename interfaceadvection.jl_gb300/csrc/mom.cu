@@ -279,7 +279,8 @@ __device__ __forceinline__ double phiq_inner(const FluxCtx& F, double Psi, doubl
 }
 
 template <int LIM>
-__global__ void momflux_kern(FluxCtx F, double* __restrict__ Phi) {
+// 40 registers (six 256-thread blocks per SM) without spills: more warps to cover the FP64 latency
+__global__ void __launch_bounds__(256, 6) momflux_kern(FluxCtx F, double* __restrict__ Phi) {
     const Grid& g = F.k.g;
     SPLIT_XYZ
     const int j = F.j;
