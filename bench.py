@@ -1,8 +1,8 @@
 #!/usr/bin/env python
 """Throughput of the per-step hot path of InterfaceAdvection.jl on GB300.
 
-Headline workload (BASELINE config "mixed-precision Poisson", the rising
-bubble the metric is quoted on): a 3D rising bubble at 256 cells per unit
+Headline workload (the mixed-precision Poisson rising bubble the metric is
+quoted on): a 3D rising bubble at 256 cells per unit
 length in a 1x2x1 domain (256x512x256 interior cells), periodic in x/z, walls
 in y, one air bubble of radius 0.125 at (0.5,0.5,0.5) in water, density ratio
 1000, viscosity ratio 100, Eötvös 10, Morton 1e-3 (gravity 1e-3 in grid units
@@ -17,6 +17,7 @@ Metric: Mcell-steps/s = interior cells × steps / s.  All per-step inputs are
 larger than L2 (fields of 274 MB each), so no flush is needed between steps.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--size 256] [--impl reference]
+                  [--smoother halfsweep|blocked]
 """
 from __future__ import annotations
 
