@@ -465,7 +465,9 @@ __device__ __forceinline__ int pair_index(int D, int i, int j) {
 }
 
 template <int D>
-__global__ void viscflux_kern(ViscCtx V, double* __restrict__ Phi6) {
+// five 256-thread blocks per SM (48 registers; the few spills stay in L1): more warps to cover the
+// FP64 latency
+__global__ void __launch_bounds__(256, 5) viscflux_kern(ViscCtx V, double* __restrict__ Phi6) {
     const Grid& g = V.k.g;
     SPLIT_XYZ
     const int c[3] = {x, y, z};
