@@ -1,23 +1,25 @@
 #!/usr/bin/env python
 """Throughput of the per-step hot path of InterfaceAdvection.jl on GB300.
 
-Headline workload (the mixed-precision Poisson rising bubble the metric is
-quoted on): a 3D rising bubble at 256 cells per unit
-length in a 1x2x1 domain (256x512x256 interior cells), periodic in x/z, walls
-in y, one air bubble of radius 0.125 at (0.5,0.5,0.5) in water, density ratio
-1000, viscosity ratio 100, Eötvös 10, Morton 1e-3 (gravity 1e-3 in grid units
-sets the time scale).  One step = sim_step! = MPFMomStep! through the C-ABI
-(RK2 predictor/corrector: CMOM momentum + VOF sweeps, viscosity, surface
-tension, two projections, MPCFL), Poisson to L∞ residual 1e-8:
-  * value    — mixed precision: FP32 V-cycles inside FP64 defect-correction FCG;
-  * fp64_mg  — the same step with FP64 V-cycles (plain FP64 multigrid path).
-Secondary line (`vof_only`): the VOF-only sphere in the LeVeque deformation field at 256³.
+Headline workload (the mixed-precision rising bubble the metric is quoted on): a 3D rising bubble at
+256 cells per unit length in a 1x2x1 domain (256x512x256 interior cells), periodic in x/z, walls in y,
+one air bubble of radius 0.125 at (0.5,0.5,0.5) in water, density ratio 1000, viscosity ratio 100,
+Eötvös 10, Morton 1e-3 (gravity 1e-3 in grid units sets the time scale).  One step = sim_step! =
+MPFMomStep! through the C-ABI (RK2 predictor/corrector: CMOM momentum + VOF sweeps, viscosity, surface
+tension, two projections, MPCFL), Poisson to an L∞ residual of 1e-8 of the dt-scaled system:
+  * value          — mixed precision: FP32 V-cycles inside FP64 defect-correction FCG, momentum
+                     arithmetic on FP32 pairs (float-float), VOF/PLIC and fields FP64;
+  * fp64_mg        — the plain FP64 path: FP64 V-cycles, FP64 momentum arithmetic;
+  * fp64_mg_ff     — FP64 V-cycles with the float-float momentum (separates the two gains);
+  * learned_hybrid — the mixed path with the inner FCG preconditioned by V-cycle + conv net.
+Further measurements in the same line: the headline's mass drift and a steps-matched FP64-oracle
+check on a small case, the VOF-only sphere over its full period (C2), a late-time window of the rising
+bubble (C3, steps 480-500 from rest), the 512³ bubble swarm (C5), and the oracle on the host cores.
 
-Metric: Mcell-steps/s = interior cells × steps / s.  All per-step inputs are
-larger than L2 (fields of 274 MB each), so no flush is needed between steps.
+Metric: Mcell-steps/s = interior cells × steps / s.  All per-step inputs are larger than L2 (fields of
+274 MB each), so no flush is needed between steps.
 
-  python bench.py [--gpus N] [--steps K] [--warmup W] [--size 256] [--impl reference]
-                  [--smoother halfsweep|blocked]
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--size 256] [--impl reference] [--quick]
 """
 from __future__ import annotations
 
@@ -38,31 +40,34 @@ for _p in (ROOT, PKG):
 
 METRIC = "Mcell-steps/s"
 PTOL = 1e-8
-B_RBGS_PER_CELL_F32 = 18   # one FP32 red-black half-sweep: L (12) + x read/write (4) + b (2) per cell
-# DRAM bytes per cell of that launch from an ncu capture of the same kernel at 160x320x160
-# (profiles/kernel_counters_bubble160.md), scaled by the cells of the launch
-TRAFFIC_RBGS_PER_CELL_F32 = 22.7
-TRAFFIC_VOF_BULK_PER_CELL = 31.1   # vof_bulk, ncu capture at 192³ (profiles/vof_bulk_sphere192.md)
-B_BULK_PER_CELL = 33       # vof_bulk: read f, u_d, u0_d (24) + c̄ (1); write ρuf_d (8)
 TK = {"vof_bulk": 0, "vof_cells": 1, "ustar": 2, "forcing": 3, "mg_vcycle": 4, "mg_transfer": 6, "krylov": 7,
       "vof_faces": 9, "momflux": 10, "momupdate": 11, "update_project": 12, "mg_fine_rbgs": 13, "nn_precond": 14,
       "mg_fine_first": 15, "other": 8}
+
+# Roofline candidates: timing family, algorithmic bytes per interior cell of one launch (each field a
+# fused launch must read once and write once), the DRAM bytes per cell ncu measured for one launch of
+# that kernel, and the kernel name.  The DRAM figures come from single-launch captures at 160x320x160
+# (momentum kernels, smoother) and 192³ (vof_bulk), scaled to the cells of a launch here.
+ROOF = {
+    "momflux": dict(bytes=64, traffic=None, kernel="momflux (CMOM face fluxes of one sweep: read uStar 3, "
+                                                   "ρuf_j, f_old; write Φ 3)"),
+    "momupdate": dict(bytes=113, traffic=None, kernel="momupdate (ρu += δt(Φ(I)-Φ(I+δj)+uOld ϕ(ρ̄∂ⱼuⱼ)))"),
+    "mg_fine_rbgs": dict(bytes=18, traffic=22.7, kernel="rbgs_pair_k<float> (finest-level red-black half-sweep)"),
+}
 
 
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=10)
-    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--size", type=int, default=256, help="cells per unit length")
-    ap.add_argument("--workload", default="bubble", choices=["bubble", "vof"])
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--cpu-seconds", type=float, default=20.0, help="bound of the CPU baseline sample")
+    ap.add_argument("--quick", action="store_true", help="headline only (no side runs, CPU baseline, e2e)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--no-secondary", action="store_true", help="skip the FP64-MG and VOF-only side runs")
+    ap.add_argument("--no-secondary", action="store_true", help="skip the side runs")
     ap.add_argument("--no-e2e", action="store_true")
-    ap.add_argument("--smoother", default="halfsweep", choices=["halfsweep", "blocked"],
-                    help="FP32 V-cycle smoother of the mixed solver (blocked: relaxation factor 1)")
+    ap.add_argument("--ref-steps", type=int, default=2, help="oracle steps timed by the reference arm")
     return ap.parse_args()
 
 
@@ -125,53 +130,76 @@ def measured_peak_hbm():
 
 
 # ------------------------------------------------------------------------------------- workloads
-def bubble_params(N):
-    """Rising bubble in grid units: Eo = ρ g D²/σ = 10, Mo = g μ⁴/(ρ σ³) = 1e-3."""
-    G, D, Eo, Mo = 1e-3, 0.25 * N, 10.0, 1e-3
-    sigma = G * D * D / Eo
-    mu = (Mo * sigma ** 3 / G) ** 0.25
-    return dict(dims=(N, 2 * N, N), centre=(N / 2, N / 2, N / 2), radius=0.125 * N, G=G, sigma=sigma, mu=mu,
-                lrho=1e-3, lmu=1e-2, perdir=(0, 2))
-
-
-def make_bubble(N, poisson, device):
+def make_bubble(N, poisson, device, arith="default"):
     import torch
 
     import intfadv as ia
-    p = bubble_params(N)
+    from intfadv import workloads
+    p = workloads.bubble_params(N)
     c, r = p["centre"], p["radius"]
     sdf = lambda x: r - torch.sqrt((x[0] - c[0]) ** 2 + (x[1] - c[1]) ** 2 + (x[2] - c[2]) ** 2)
     return ia.TwoPhaseSimulation(p["dims"], (0.0, 0.0, 0.0), float(N), perdir=p["perdir"], λρ=p["lrho"],
                                  λμ=p["lmu"], ν=p["mu"], η=p["sigma"], g=(0.0, -p["G"], 0.0), InterfaceSDF=sdf,
-                                 poisson=poisson, poisson_tol=PTOL, poisson_itmx=400, device=device)
+                                 poisson=poisson, poisson_tol=PTOL, poisson_itmx=400, device=device,
+                                 momentum_arith=arith)
+
+
+def make_swarm(N, poisson, device, arith="default"):
+    import intfadv as ia
+    from intfadv import learned, workloads
+    bubbles = workloads.swarm_layout(N=N)
+    D = 2 * max(r for _, r in bubbles)
+    p = workloads.bubble_params(N, Eo=5.0, D=D)
+    return ia.TwoPhaseSimulation((N, N, N), (0.0, 0.0, 0.0), float(N), perdir=(0, 2), λρ=p["lrho"], λμ=p["lmu"],
+                                 ν=p["mu"], η=p["sigma"], g=(0.0, -p["G"], 0.0),
+                                 InterfaceSDF=learned.bubbles_sdf(bubbles), poisson=poisson, poisson_tol=PTOL,
+                                 poisson_itmx=400, device=device, momentum_arith=arith)
 
 
 # ------------------------------------------------------------------------------------- CPU side
-def cpu_bubble_baseline(N, seconds):
-    """The oracle (C++ OpenMP restatement; Jacobi-PCG Poisson) on the same bubble at reduced size."""
+def _omp_threads(n):
+    """Set the OpenMP thread count of the oracle (libgomp is shared by the process)."""
+    try:
+        C.CDLL("libgomp.so.1").omp_set_num_threads(int(n))
+    except OSError:
+        pass
+
+
+def cpu_bubble(N, steps, threads=None):
+    """The oracle (C++ OpenMP restatement; multigrid-preconditioned CG in the role of WaterLily's
+    MultiLevelPoisson) on the rising bubble at N cells per unit length: one MPFMomStep! per step,
+    Poisson to the same L∞ tolerance."""
     import numpy as np
 
+    from intfadv import workloads
     from oracle.sim import OracleSim
-    p = bubble_params(N)
+    cores = threads or (os.cpu_count() or 1)
+    _omp_threads(cores)
+    p = workloads.bubble_params(N)
     c, r = p["centre"], p["radius"]
     sdf = lambda x: r - np.sqrt((x[0] - c[0]) ** 2 + (x[1] - c[1]) ** 2 + (x[2] - c[2]) ** 2)
+    t0 = time.perf_counter()
     orc = OracleSim(p["dims"], (0.0, 0.0, 0.0), sdf=sdf, perdir=p["perdir"], lrho=p["lrho"], lmu=p["lmu"],
-                    ν=p["mu"], g=(0.0, -p["G"], 0.0), eta=p["sigma"], ptol=PTOL, pitmx=20000)
-    cells = p["dims"][0] * p["dims"][1] * p["dims"][2]
-    steps, t0 = 0, time.perf_counter()
-    while True:
+                    ν=p["mu"], g=(0.0, -p["G"], 0.0), eta=p["sigma"], ptol=PTOL, pitmx=2000, psolver="mg")
+    t_init = time.perf_counter() - t0
+    times, iters = [], []
+    for _ in range(steps):
+        t0 = time.perf_counter()
         orc.step()
-        steps += 1
-        el = time.perf_counter() - t0
-        if el >= seconds or steps >= 50:
-            break
-    cores = int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1))
+        times.append(time.perf_counter() - t0)
+        iters.append(int(orc.s.piters))
+    _omp_threads(os.cpu_count() or 1)
+    cells = p["dims"][0] * p["dims"][1] * p["dims"][2]
+    el = sum(times)
+    dims = "x".join(str(d) for d in p["dims"])
     return {"value": cells * steps / el / 1e6, "unit": METRIC, "cores": cores, "kind": "port",
-            "sample": f"{steps} MPFMomStep! of the rising bubble at {p['dims'][0]}x{p['dims'][1]}x{p['dims'][2]} "
-                      f"in {el:.1f} s (oracle, OpenMP, Jacobi-PCG to L-inf 1e-8)"}
+            "sample": f"{steps} MPFMomStep! of the rising bubble at {dims} in {el:.1f} s after {t_init:.1f} s of "
+                      f"set-up (oracle: C++ OpenMP, {cores} threads; multigrid-preconditioned CG to L-inf {PTOL}, "
+                      f"last solve {iters[-1]} iterations)",
+            "step_s": times, "grid": list(p["dims"])}
 
 
-def cpu_vof_baseline(N, seconds):
+def cpu_vof(N, steps):
     import numpy as np
 
     from intfadv import fields, workloads
@@ -198,18 +226,45 @@ def cpu_vof_baseline(N, seconds):
     dt = 1.0 / (4 * N)
     u1 = np.asfortranarray(U * workloads.deformation_time_factor(0.0))
     u2 = O.zeros(U.shape)
-    steps, t0 = 0, time.perf_counter()
-    while True:
-        np.multiply(U, workloads.deformation_time_factor((steps + 1) * dt), out=u2)
-        O.advect_vof(f, u1, u2, dt, O.dir_order(steps + 1, 3))
+    t0 = time.perf_counter()
+    for s in range(steps):
+        np.multiply(U, workloads.deformation_time_factor((s + 1) * dt), out=u2)
+        O.advect_vof(f, u1, u2, dt, O.dir_order(s + 1, 3))
         u1, u2 = u2, u1
-        steps += 1
-        el = time.perf_counter() - t0
-        if el >= seconds or steps >= 200:
-            break
-    cores = int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1))
-    return {"value": N ** 3 * steps / el / 1e6, "unit": METRIC, "cores": cores, "kind": "port",
-            "sample": f"{steps} step(s) of the {N}^3 deformation advect! in {el:.1f} s (oracle, OpenMP)"}
+    el = time.perf_counter() - t0
+    return {"value": N ** 3 * steps / el / 1e6, "unit": METRIC, "cores": os.cpu_count() or 1, "kind": "port",
+            "sample": f"{steps} advect! steps of the {N}^3 deformation sphere in {el:.1f} s (oracle, OpenMP)"}
+
+
+def oracle_check(device, N=24, steps=5):
+    """A steps-matched FP64-oracle comparison on a small rising bubble (the headline's physics at
+    N cells per unit length, N x 2N x N, the headline's solver and arithmetic); both sides solve the
+    pressure to L-inf 1e-12 so that the comparison measures the step, not the solver tolerance."""
+    import numpy as np
+    import torch
+
+    import intfadv as ia
+    from intfadv import workloads
+    from oracle.sim import OracleSim
+    p = workloads.bubble_params(N)
+    c, r = p["centre"], p["radius"]
+    sdf_t = lambda x: r - torch.sqrt((x[0] - c[0]) ** 2 + (x[1] - c[1]) ** 2 + (x[2] - c[2]) ** 2)
+    sdf_n = lambda x: r - np.sqrt((x[0] - c[0]) ** 2 + (x[1] - c[1]) ** 2 + (x[2] - c[2]) ** 2)
+    kw = dict(perdir=p["perdir"], ν=p["mu"], g=(0.0, -p["G"], 0.0))
+    sim = ia.TwoPhaseSimulation(p["dims"], (0.0, 0.0, 0.0), float(N), λρ=p["lrho"], λμ=p["lmu"], η=p["sigma"],
+                                InterfaceSDF=sdf_t, poisson="mixed", poisson_tol=1e-12, poisson_itmx=500,
+                                device=device, **kw)
+    orc = OracleSim(p["dims"], (0.0, 0.0, 0.0), sdf=sdf_n, lrho=p["lrho"], lmu=p["lmu"], eta=p["sigma"], ptol=1e-12,
+                    pitmx=5000, psolver="mg", **kw)
+    for _ in range(steps):
+        ia.sim_step(sim)
+        orc.step()
+    torch.cuda.synchronize()
+    ef = float(np.abs(sim.intf.f.cpu().numpy() - orc.f).max())
+    eu = float(np.abs(sim.flow.u.cpu().numpy() - orc.u).max()) / float(np.abs(orc.u).max())
+    return {"case": f"rising bubble {N}x{2 * N}x{N} (the headline's physics), {steps} steps, mixed solver with "
+                    f"float-float momentum vs the FP64 oracle, both to L-inf 1e-12",
+            "max_abs_err_f": ef, "max_rel_err_u": eu}
 
 
 # ------------------------------------------------------------------------------------- GPU side
@@ -244,6 +299,34 @@ def kernel_times(sim, steps):
                 "avg_launch_ms": (T[i] / Lc[i]) if Lc[i] else None} for k, i in TK.items()}
 
 
+def probe_peaks():
+    from intfadv import _lib
+    L = _lib.load()
+    a, b = C.c_double(), C.c_double()
+    if L.ia_probe_fma_rates(C.byref(a), C.byref(b)) != 0:
+        return None
+    return {"fp64_fma_per_s": a.value, "fp32_fma_per_s": b.value,
+            "how": "8 independent FMA chains per thread, 8 blocks of 256 threads per SM, CUDA events"}
+
+
+def rooflines(kt, cells, peak, peak_kind):
+    """Roofline of each candidate kernel from its live per-launch CUDA-event time; the dominant one
+    (largest time per step) is the line's `roofline`."""
+    out = {}
+    for fam, spec in ROOF.items():
+        k = kt.get(fam)
+        if not k or not k["avg_launch_ms"]:
+            continue
+        b = spec["bytes"] * cells
+        ach = b / (k["avg_launch_ms"] / 1e3) / 1e9
+        out[fam] = {"bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s", "frac": ach / peak,
+                    "traffic": (spec["traffic"] * cells) if spec["traffic"] else None, "kernel": spec["kernel"],
+                    "peak_kind": peak_kind, "bytes_per_launch": b, "avg_launch_ms": k["avg_launch_ms"],
+                    "ms_per_step": k["ms_per_step"]}
+    dom = max(out, key=lambda f: out[f]["ms_per_step"]) if out else None
+    return dom, out
+
+
 def run_bubble(args, world, local_rank):
     import torch
 
@@ -255,13 +338,13 @@ def run_bubble(args, world, local_rank):
     barrier = (lambda: torch.distributed.barrier()) if world > 1 else (lambda: None)
     L = _lib.load()
     sim = make_bubble(N, "mixed", dev)
-    # the blocked smoother applies at relaxation factor 1 only
-    ia.set_smoother(sim.handle, args.smoother, 1.0 if args.smoother == "blocked" else None)
+    m0 = sim.intf.mass()
     for _ in range(args.warmup):
         ia.sim_step(sim)
     n0 = L.ia_launch_count()
     ms, its, res, clk = timed_steps(sim, args.steps, barrier, True, local_rank)
     launches = L.ia_launch_count() - n0
+    m1 = sim.intf.mass()
     if world > 1:
         t = torch.tensor([ms], device=dev)
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
@@ -269,16 +352,12 @@ def run_bubble(args, world, local_rank):
     value = world * cells * args.steps / (ms / 1e3) / 1e6
     kt = kernel_times(sim, max(2, min(args.steps, 3)))
     peak, peak_kind = measured_peak_hbm()
-    fine = kt["mg_fine_rbgs"]
-    roof = None
-    if fine["avg_launch_ms"]:
-        b = B_RBGS_PER_CELL_F32 * cells
-        ach = b / (fine["avg_launch_ms"] / 1e3) / 1e9
-        roof = {"bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s", "frac": ach / peak,
-                "traffic": TRAFFIC_RBGS_PER_CELL_F32 * cells,
-                "traffic_note": "ncu dram bytes of the finest-level launch at 160x320x160 (22.7 B/cell), scaled",
-                "kernel": "rbgs_pair_k<float> (finest-level red-black Gauss-Seidel half-sweep, mixed V-cycle)",
-                "peak_kind": peak_kind, "bytes_per_launch": b, "avg_launch_ms": fine["avg_launch_ms"]}
+    dom, roofs = rooflines(kt, cells, peak, peak_kind)
+    out = {"value": value, "ms_per_step": ms / args.steps, "clocks": clk, "launches": launches,
+           "roofline": roofs.get(dom), "rooflines": roofs, "kernels": kt,
+           "poisson_iters_per_step": statistics.mean(its), "max_resid": max(res), "dt": sim.flow.Δt[-1],
+           "mass_drift": {"value": abs(m1 - m0) / m0, "steps": args.warmup + args.steps + 0,
+                          "note": "|Σf - Σf₀|/Σf₀ over the warm-up and timed steps from the initial state"}}
     e2e = None
     if not args.no_e2e:
         # state kept on the host: each step uploads u and f from pinned memory, runs the step through the
@@ -315,47 +394,100 @@ def run_bubble(args, world, local_rank):
         e2e = {"value": world * cells * e_steps / el / 1e6, "unit": METRIC, "h2d_bytes_per_step": nb,
                "d2h_bytes_per_step": nb + fl.p.numel() * 8 + C.sizeof(_lib.Status),
                "note": "state on the host: u, f uploaded and u, f, p downloaded every step around sim_step"}
-    out = {"value": value, "ms_per_step": ms / args.steps, "clocks": clk, "launches": launches, "roofline": roof,
-           "kernels": kt, "poisson_iters_per_step": statistics.mean(its), "max_resid": max(res), "e2e": e2e,
-           "dt": sim.flow.Δt[-1]}
+    out["e2e"] = e2e
     del sim
     torch.cuda.empty_cache()
-    if not args.no_secondary:
-        ref = make_bubble(N, "fp64", dev)
+    if args.no_secondary:
+        return out
+    k = max(2, min(args.steps, 5))
+    for key, arith in (("fp64_mg", "fp64"), ("fp64_mg_ff", "ff")):
+        ref = make_bubble(N, "fp64", dev, arith)
         for _ in range(max(1, args.warmup - 1)):
             ia.sim_step(ref)
-        k = max(2, min(args.steps, 5))
         ms2, its2, res2, _ = timed_steps(ref, k, barrier, False, local_rank)
-        out["fp64_mg"] = {"value": world * cells * k / (ms2 / 1e3) / 1e6, "ms_per_step": ms2 / k,
-                          "poisson_iters_per_step": statistics.mean(its2), "max_resid": max(res2),
-                          "mg_vcycle_ms_per_step": kernel_times(ref, 2)["mg_vcycle"]["ms_per_step"]}
-        out["speedup_vs_fp64_mg"] = value / out["fp64_mg"]["value"]
+        out[key] = {"value": world * cells * k / (ms2 / 1e3) / 1e6, "ms_per_step": ms2 / k,
+                    "poisson_iters_per_step": statistics.mean(its2), "max_resid": max(res2),
+                    "momentum_arith": arith, "mg_vcycle_ms_per_step": kernel_times(ref, 2)["mg_vcycle"]["ms_per_step"]}
         del ref
         torch.cuda.empty_cache()
-        from intfadv import learned
-        if os.path.exists(learned.WEIGHTS):
-            # learned preconditioner: the same step with the inner FCG preconditioned by V-cycle + net
-            lrn = make_bubble(N, "learned", dev)
-            for _ in range(max(1, args.warmup - 1)):
-                ia.sim_step(lrn)
-            k = max(2, min(args.steps, 5))
-            st0 = ia.poisson_stats(lrn.handle)
-            ms3, its3, res3, _ = timed_steps(lrn, k, barrier, False, local_rank)
-            st1 = ia.poisson_stats(lrn.handle)
-            kt3 = kernel_times(lrn, 2)
-            out["learned_hybrid"] = {
-                "value": world * cells * k / (ms3 / 1e3) / 1e6, "ms_per_step": ms3 / k,
-                "poisson_iters_per_step": statistics.mean(its3), "max_resid": max(res3),
-                "fallbacks": st1["fallbacks"] - st0["fallbacks"],
-                "net_ms_per_step": kt3["nn_precond"]["ms_per_step"],
-                "mg_vcycle_ms_per_step": kt3["mg_vcycle"]["ms_per_step"],
-                "weights": learned.load_params()[1]}
-            del lrn
-            torch.cuda.empty_cache()
+    out["speedup_vs_fp64_mg"] = value / out["fp64_mg"]["value"]
+    from intfadv import learned
+    if os.path.exists(learned.WEIGHTS):
+        # learned preconditioner: the same step with the inner FCG preconditioned by V-cycle + net
+        lrn = make_bubble(N, "learned", dev)
+        for _ in range(max(1, args.warmup - 1)):
+            ia.sim_step(lrn)
+        st0 = ia.poisson_stats(lrn.handle)
+        ms3, its3, res3, _ = timed_steps(lrn, k, barrier, False, local_rank)
+        st1 = ia.poisson_stats(lrn.handle)
+        kt3 = kernel_times(lrn, 2)
+        out["learned_hybrid"] = {
+            "value": world * cells * k / (ms3 / 1e3) / 1e6, "ms_per_step": ms3 / k,
+            "poisson_iters_per_step": statistics.mean(its3), "max_resid": max(res3),
+            "fallbacks": st1["fallbacks"] - st0["fallbacks"],
+            "net_ms_per_step": kt3["nn_precond"]["ms_per_step"],
+            "mg_vcycle_ms_per_step": kt3["mg_vcycle"]["ms_per_step"],
+            "weights": learned.load_params()[1]}
+        del lrn
+        torch.cuda.empty_cache()
     return out
 
 
-def run_vof(args, world, local_rank, steps=200):
+def run_bubble_late(args, local_rank, total=500, window=20):
+    """C3 as configured: 500 steps from rest; the last `window` steps timed (deformed bubble)."""
+    import torch
+
+    import intfadv as ia
+    dev = torch.device("cuda", local_rank)
+    N = args.size
+    cells = N * 2 * N * N
+    sim = make_bubble(N, "mixed", dev)
+    m0 = sim.intf.mass()
+    t0 = time.perf_counter()
+    for _ in range(total - window):
+        ia.sim_step(sim)
+    ms, its, res, _ = timed_steps(sim, window, lambda: None, False, local_rank)
+    el = time.perf_counter() - t0
+    out = {"workload": f"rising bubble {N}x{2 * N}x{N}, steps {total - window + 1}-{total} of a run from rest",
+           "value": cells * window / (ms / 1e3) / 1e6, "ms_per_step": ms / window,
+           "poisson_iters_per_step": statistics.mean(its), "max_resid": max(res),
+           "mass_drift": abs(sim.intf.mass() - m0) / m0, "all_steps_wall_s": el, "t": sum(sim.flow.Δt[:-1])}
+    del sim
+    torch.cuda.empty_cache()
+    return out
+
+
+def run_swarm(args, local_rank, N=512, steps=100, fp64_steps=10):
+    """C5: 512³ unit cube, 64 bubbles r ∈ U[0.02, 0.05] (seed 5), Eö 5: the mixed path over the
+    configured 100 steps (all timed), and the plain FP64 path over its first steps."""
+    import torch
+
+    import intfadv as ia
+    dev = torch.device("cuda", local_rank)
+    cells = N ** 3
+    out = {"workload": f"bubble swarm {N}^3, 64 bubbles r in U[0.02,0.05] (seed 5), Eo=5, density ratio 1000, "
+                       f"viscosity ratio 100, periodic x/z, walls y"}
+    for key, poisson, arith, k in (("mixed", "mixed", "default", steps), ("fp64_mg", "fp64", "fp64", fp64_steps)):
+        sim = make_swarm(N, poisson, dev, arith)
+        m0 = sim.intf.mass()
+        ms, its, res, _ = timed_steps(sim, k, lambda: None, False, local_rank)
+        out[key] = {"value": cells * k / (ms / 1e3) / 1e6, "ms_per_step": ms / k, "steps": k,
+                    "poisson_iters_per_step": statistics.mean(its), "max_resid": max(res),
+                    "mass_drift": abs(sim.intf.mass() - m0) / m0}
+        if key == "mixed":
+            kt = kernel_times(sim, 2)
+            peak, peak_kind = measured_peak_hbm()
+            dom, roofs = rooflines(kt, cells, peak, peak_kind)
+            out["roofline"] = roofs.get(dom)
+        del sim
+        torch.cuda.empty_cache()
+    out["speedup_vs_fp64_mg"] = out["mixed"]["value"] / out["fp64_mg"]["value"]
+    return out
+
+
+def run_vof(args, world, local_rank):
+    """C2: the sphere in the LeVeque deformation field over its full period T=3 at CFL 0.5 (12 N steps),
+    all timed; L1 shape error Σ|f - f₀|Δx³ against the initial sphere and the mass drift."""
     import torch
 
     import intfadv as ia
@@ -363,24 +495,24 @@ def run_vof(args, world, local_rank, steps=200):
     dev = torch.device("cuda", local_rank)
     N = args.size
     intf = ia.cVOF((N, N, N), InterfaceSDF=workloads.sphere_sdf((0.35, 0.35, 0.35), 0.15, N), device=dev)
+    f0 = intf.f.clone()
     U = workloads.deformation_field(N, device=dev)
     dt = 1.0 / (4 * N)
+    steps = 12 * N                              # T = 3 at Δt = 1/(4N)
     u1 = U * workloads.deformation_time_factor(0.0)
     u2 = torch.empty_like(U)
     m0 = intf.mass()
     s = [0]
+    codes = set()
 
     def one():
         nonlocal u1, u2
         s[0] += 1
         torch.mul(U, workloads.deformation_time_factor(s[0] * dt), out=u2)
         st = ia.advect_vof_raw(intf, intf.f, u1, u2, dt, s[0])
-        if st.code not in (0, 100):
-            raise RuntimeError(f"advect status {st.code}")
+        codes.add(st.code)
         u1, u2 = u2, u1
 
-    for _ in range(5):
-        one()
     torch.cuda.synchronize()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     e0.record()
@@ -389,6 +521,9 @@ def run_vof(args, world, local_rank, steps=200):
     e1.record()
     torch.cuda.synchronize()
     ms = e0.elapsed_time(e1)
+    inner = (slice(1, -1),) * 3
+    l1 = float((intf.f[inner] - f0[inner]).abs().sum()) / N ** 3
+    drift = abs(intf.mass() - m0) / m0
     T, Lc = (C.c_double * 16)(), (C.c_int64 * 16)()
     intf.handle.call("ia_timing", 1, None, None, 0)
     for _ in range(10):
@@ -396,14 +531,14 @@ def run_vof(args, world, local_rank, steps=200):
     intf.handle.call("ia_timing", 0, T, Lc, 16)
     bulk_ms = T[0] / max(1, Lc[0])
     peak, peak_kind = measured_peak_hbm()
-    ach = B_BULK_PER_CELL * N ** 3 / (bulk_ms / 1e3) / 1e9
-    return {"workload": f"VOF-only sphere r=0.15, LeVeque deformation, {N}^3, CFL 0.5",
-            "value": world * N ** 3 * steps / (ms / 1e3) / 1e6, "ms_per_step": ms / steps,
-            "mass_drift": abs(intf.mass() - m0) / m0,
+    ach = 33 * N ** 3 / (bulk_ms / 1e3) / 1e9
+    return {"workload": f"VOF-only sphere r=0.15 at (0.35,0.35,0.35), LeVeque deformation, {N}^3, CFL 0.5, "
+                        f"full period T=3 ({steps} advect! steps, all timed)",
+            "value": world * N ** 3 * steps / (ms / 1e3) / 1e6, "ms_per_step": ms / steps, "steps": steps,
+            "l1_shape_error": l1, "mass_drift": drift, "status_codes": sorted(codes),
             "roofline": {"bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s", "frac": ach / peak,
-                         "traffic": TRAFFIC_VOF_BULK_PER_CELL * N ** 3,
-                         "traffic_note": "ncu dram bytes of one launch at 192^3 (31.1 B/cell), scaled",
-                         "kernel": "vof_bulk", "peak_kind": peak_kind, "avg_launch_ms": bulk_ms}}
+                         "traffic": 31.1 * N ** 3, "kernel": "vof_bulk (read f, u_d, u⁰_d, c̄; write ρuf_d: 33 B)",
+                         "peak_kind": peak_kind, "avg_launch_ms": bulk_ms}}
 
 
 def main():
@@ -413,55 +548,51 @@ def main():
         import torch
         torch.distributed.init_process_group("nccl" if args.impl == "ours" else "gloo")
     N = args.size
-    p = bubble_params(N)
-    cfg = {"workload": f"3D rising bubble {p['dims'][0]}x{p['dims'][1]}x{p['dims'][2]} (1x2x1, periodic x/z, "
-                       f"walls y), r=0.125 at (0.5,0.5,0.5), density ratio 1000, viscosity ratio 100, Eo=10, "
-                       f"Mo=1e-3; MPFMomStep! with Poisson to L-inf residual {PTOL}",
-           "grid": list(p["dims"]), "poisson": "FP32 V-cycles + FP64 defect-correction FCG (mixed)",
+    dims = (N, 2 * N, N)
+    cfg = {"workload": f"3D rising bubble {dims[0]}x{dims[1]}x{dims[2]} (1x2x1, periodic x/z, walls y), r=0.125 at "
+                       f"(0.5,0.5,0.5), density ratio 1000, viscosity ratio 100, Eo=10, Mo=1e-3; MPFMomStep! with "
+                       f"Poisson to L-inf residual {PTOL}",
+           "grid": list(dims), "poisson": "FP32 V-cycles + FP64 defect-correction FCG (mixed)",
+           "momentum_arith": "float-float (FP32 pairs); VOF, PLIC, fields and defect correction FP64",
            "l2_flush": "inputs larger than L2 (each field 274 MB)", "parallelism": f"replicas x{world}"}
-    if args.workload == "vof":
-        cfg = {"workload": f"VOF-only sphere r=0.15, LeVeque deformation, {N}^3, CFL 0.5", "grid": [N, N, N],
-               "parallelism": f"replicas x{world}"}
     if args.impl == "reference":
         if rank != 0:
             return
-        if args.workload == "vof":
-            base = cpu_vof_baseline(N, args.cpu_seconds)
-        else:
-            base = cpu_bubble_baseline(max(16, N // 4), args.cpu_seconds)
+        base = cpu_bubble(N, args.ref_steps)
         line = {"impl": "reference", "metric": METRIC, "value": base["value"], "unit": METRIC, "n_gpus": world,
-                "steps": args.steps, "warmup": args.warmup, "ms_per_step": None, "higher_is_better": True,
-                "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic", "config": cfg,
-                "cpu_baseline": base,
+                "steps": args.ref_steps, "warmup": 0, "ms_per_step": 1e3 * statistics.mean(base["step_s"]),
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+                "data": "synthetic", "config": cfg, "cpu_baseline": base,
                 "e2e": {"value": base["value"], "unit": METRIC, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
-                "note": "the reference is Julia (no toolchain here); this arm times the C++ OpenMP restatement"}
+                "note": f"the reference is Julia (no toolchain here); this arm times the C++ OpenMP restatement of "
+                        f"its step (multigrid-preconditioned CG in the role of MultiLevelPoisson) on the same "
+                        f"{dims[0]}x{dims[1]}x{dims[2]} grid, {args.ref_steps} steps whatever --steps says"}
         print(json.dumps(line), flush=True)
         return
     import torch
     torch.cuda.set_device(local_rank)
-    if args.workload == "vof":
-        res = run_vof(args, world, local_rank)
-        if rank == 0:
-            cpu = None if args.no_cpu_baseline else cpu_vof_baseline(N, args.cpu_seconds)
-            print(json.dumps({"metric": METRIC, "value": res["value"], "unit": METRIC, "n_gpus": world,
-                              "steps": 200, "warmup": 5, "ms_per_step": res["ms_per_step"], "higher_is_better": True,
-                              "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-                              "config": cfg, "roofline": res["roofline"], "cpu_baseline": cpu}), flush=True)
-        return
     res = run_bubble(args, world, local_rank)
     if rank == 0:
-        vof = None if args.no_secondary else run_vof(args, 1, local_rank)
-        cpu = None if args.no_cpu_baseline else cpu_bubble_baseline(max(16, N // 4), args.cpu_seconds)
+        quick = args.quick or args.no_secondary
+        extra = {}
+        if not quick:
+            extra["oracle_check"] = oracle_check(torch.device("cuda", local_rank))
+            extra["vof_only"] = run_vof(args, 1, local_rank)
+            extra["rising_bubble_late"] = run_bubble_late(args, local_rank)
+            extra["swarm"] = run_swarm(args, local_rank)
+            extra["measured_fma_peaks"] = probe_peaks()
+        cpu = None if (quick or args.no_cpu_baseline) else cpu_bubble(N, 1)
+        cpu1 = None if (quick or args.no_cpu_baseline) else cpu_bubble(max(16, N // 4), 2, threads=1)
         line = {"metric": METRIC, "value": res["value"], "unit": METRIC, "n_gpus": world, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": res["ms_per_step"], "higher_is_better": True,
-                "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic", "config": cfg,
-                "clocks": res["clocks"], "e2e": res["e2e"], "gpu_launches": res["launches"],
-                "roofline": res["roofline"], "cpu_baseline": cpu,
-                "fp64_mg": res.get("fp64_mg"), "speedup_vs_fp64_mg": res.get("speedup_vs_fp64_mg"),
-                "learned_hybrid": res.get("learned_hybrid"),
+                "scaling": "weak", "vs_baseline": None, "dtype": "f64 fields; f32-pair momentum; f32 V-cycles",
+                "data": "synthetic", "config": cfg, "clocks": res["clocks"], "e2e": res["e2e"],
+                "gpu_launches": res["launches"], "roofline": res["roofline"], "rooflines": res["rooflines"],
+                "cpu_baseline": cpu, "cpu_baseline_1core": cpu1,
+                "mass_drift": res["mass_drift"], "fp64_mg": res.get("fp64_mg"), "fp64_mg_ff": res.get("fp64_mg_ff"),
+                "speedup_vs_fp64_mg": res.get("speedup_vs_fp64_mg"), "learned_hybrid": res.get("learned_hybrid"),
                 "poisson_iters_per_step": res["poisson_iters_per_step"], "max_poisson_resid": res["max_resid"],
-                "kernels_ms_per_step": {k: v["ms_per_step"] for k, v in res["kernels"].items()},
-                "vof_only": vof}
+                "kernels_ms_per_step": {k: v["ms_per_step"] for k, v in res["kernels"].items()}, **extra}
         print(json.dumps(line), flush=True)
     if world > 1:
         import torch

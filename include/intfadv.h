@@ -81,6 +81,11 @@ extern "C" {
 #define IA_SMOOTHER_BLOCKED   1   /* all half-sweeps of a smoothing in one z-wavefront launch
                                      (3D); same arithmetic                                 */
 
+/* Arithmetic of the momentum kernels (ia_momentum_arith) */
+#define IA_ARITH_DEFAULT  (-1)  /* float-float in the MIXED / LEARNED modes, FP64 in the FP64 mode      */
+#define IA_ARITH_FP64       0   /* FP64, as the reference computes (Float64 fields)                     */
+#define IA_ARITH_FF         1   /* FP32 pairs (48-bit significands) built from error-free transformations */
+
 typedef struct ia_handle ia_handle;
 
 /* Construction parameters: TwoPhaseSimulation / cVOF keywords
@@ -160,8 +165,12 @@ int ia_advect_vof(ia_handle* h, double* f, const double* u1, const double* u2,
  * grids above IA_NOALLOC_MAX_CELLS ghost-inclusive cells return
  * IA_ERR_TOO_LARGE; every call reuses the array (status and counters are
  * cleared at the start of each call), so calls whose GPU work overlaps race and
- * must be serialised by the caller; the first call on a device looks up the
- * array's address and should come before any stream capture on that device. */
+ * must be serialised by the caller.  The array is per device: `stream` must
+ * belong to the current device (IA_ERR_INVALID otherwise), and the first call
+ * on a device looks up the array's address there.  Like ia_advect_vof, the
+ * call reads its status back and synchronises `stream` before returning, so it
+ * must not be called inside a stream capture.  exitBC is rejected with
+ * IA_ERR_UNSUPPORTED, as by ia_create. */
 #define IA_NOALLOC_MAX_CELLS 1048576
 int ia_advect_vof_noalloc(const ia_config* cfg, void* stream, double* f, const double* u1,
                           const double* u2, double dt, int64_t n_dt, int8_t* cbar, double* rhouf,
@@ -220,9 +229,27 @@ int ia_project(ia_handle* h, const double* f, double dtp, int32_t* iters, double
 int ia_advect_momentum(ia_handle* h, double* f, const double* u1, const double* u2,
                        const double* uOld, double dt, int64_t n_dt, ia_status* status);
 
+/* Arithmetic of the momentum chain of ia_mom_step / ia_advect_momentum / ia_visc_surften (uStar,
+ * the CMOM face fluxes, the momentum update, the viscous fluxes, updateU!): IA_ARITH_FP64,
+ * IA_ARITH_FF or IA_ARITH_DEFAULT.  No reference counterpart: the reference computes in the field
+ * type T.  The float-float path keeps every FP64 field and the FP64 VOF, PLIC, Poisson defect
+ * correction and rare mixed-cell branches; only the momentum arithmetic runs on FP32 pairs
+ * (relative precision about 2^-46 per operation), because GB300 issues FP64 at 1/64 of the FP32 rate. */
+int ia_momentum_arith(ia_handle* h, int32_t kind);
+
 /* viscSurfTenρu!(r, u, ...) — src/flow.jl:113-117 into the bound force field,
  * with the fraction f (the reference's f⁰ midpoint or f). */
 int ia_visc_surften(ia_handle* h, const double* f);
+
+/* surfTen!(forcing, f, α, n̂, fbuffer, η) — src/surfaceTension.jl:8-20: for every direction d
+ * the face fraction ϕ(d,·,f) with BCf!(d, ·), the WY normal and the Popinet height-function
+ * curvature on the cells whose face fraction is mixed, forcing[I,d] += η κ (−∂(d,I,f)).
+ * `forcing` is a device vector field (accumulated into), `f` the fraction.  The reference reuses
+ * fbuffer (the cVOF's fᶠ) for every d, and BCf!(d, ·) never writes its high ghost along a wall
+ * dimension d, so that position holds the buffer's previous content; `fbuffer` supplies that content
+ * for d = 1 (its high x-ghost plane is read, nothing is written to it; NULL = zeros, which is what
+ * fᶠ holds there after a VOF sweep between walls of zero normal velocity).  η = 0 is η::Nothing (no-op). */
+int ia_surften(ia_handle* h, double* forcing, const double* f, const double* fbuffer, double eta);
 
 /* Σ f over interior cells (FP64, deterministic tree order): the mass the
  * reference checks with sum(f[inside(f)]), test/maintests.jl:209,215. */
@@ -258,6 +285,10 @@ int ia_metrics(ia_handle* h, const double* u, const double* f, const double* ome
  * then, if enable >= 0, resets the totals and switches recording on (1) or
  * off (0). */
 int ia_timing(ia_handle* h, int32_t enable, double* ms_out, int64_t* launches_out, int32_t n);
+
+/* Measured FMA throughput of the current device, FP64 and FP32, in fused multiply-adds per second
+ * per device (instrumentation for the roofline figures; no reference counterpart). */
+int ia_probe_fma_rates(double* fp64_fma_per_s, double* fp32_fma_per_s);
 
 /* Number of CUDA kernels this library has launched in the process so far
  * (instrumentation, no reference counterpart; used for launch accounting). */

@@ -48,13 +48,17 @@ int status_collect(ia_handle* h, const double* u1, const double* u2, ia_status* 
     cudaError_t e = cudaMemcpyAsync(h->hst, h->dst, sizeof(DevStatus), cudaMemcpyDeviceToHost, h->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
     if (e != cudaSuccess) return IA_ERR_CUDA;
-    const DevStatus& s = *h->hst;
     ia_status st;
     if (merge && out) st = *out;
     else std::memset(&st, 0, sizeof(st));
+    const int code = translate_fill_status(h->g, *h->hst, u1, u2, st);
+    if (out) *out = st;
+    return code;
+}
+
+int translate_fill_status(const Grid& g, const DevStatus& s, const double* u1, const double* u2, ia_status& st) {
     st.flags |= s.flags & (IA_FLAG_NAN | IA_FLAG_OVERFILL | IA_FLAG_UNDERFILL);
     auto div_at = [&](long long I, double& dsum) -> int {
-        const Grid& g = h->g;
         double acc[2] = {0.0, 0.0};
         const double* us[2] = {u1, u2};
         for (int k = 0; k < 2; ++k)
@@ -87,7 +91,6 @@ int status_collect(ia_handle* h, const double* u1, const double* u2, ia_status* 
     else if (st.flags & (IA_FLAG_OVERFILL | IA_FLAG_UNDERFILL)) code = IA_WARN_FILL;
     else if (st.flags & IA_FLAG_POISSON) code = IA_WARN_NOT_CONVERGED;
     st.code = code;
-    if (out) *out = st;
     return code;
 }
 

@@ -43,6 +43,7 @@ struct ia_handle {
     double* partial = nullptr;         // reduction partials
     double* dscalar = nullptr;         // device scalars
     int8_t* cbar_own = nullptr;        // c̄ when the caller binds none
+    int mom_arith = -1;                // IA_ARITH_* of the momentum kernels (-1: by Poisson mode)
     Timing timing;
     MomScratch* mom = nullptr;
     PoissonMG* mg = nullptr;
@@ -53,6 +54,10 @@ namespace ia {
 int cuda_fail(cudaError_t e);
 int status_reset(ia_handle* h);
 int status_collect(ia_handle* h, const double* u1, const double* u2, ia_status* out, bool merge);
+// Host-side translation of one read-back device status into `st` (flags OR-ed in, fill extremes,
+// the divergence check of both velocity fields at a flagged cell) and the reportFillError return
+// code (src/advection.jl:145-189).  Shared by every entry point that reports a fill status.
+int translate_fill_status(const Grid& g, const DevStatus& s, const double* u1, const double* u2, ia_status& st);
 // one VOF sweep along d, fin -> fout (fin == fout: in place)
 int vof_sweep(ia_handle* h, const double* fin, double* fout, const double* u1, const double* u2, double dt, int d,
               bool first, int8_t* cbar, double* rhouf, double tol_rep, int counter);

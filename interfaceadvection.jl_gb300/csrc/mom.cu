@@ -13,88 +13,11 @@
 
 #include "ia_geom.cuh"
 #include "mom.cuh"
+#include "mom_common.cuh"
 
 namespace ia {
 
 namespace {
-
-inline dim3 blk() { return dim3(32, 8, 1); }
-
-// Interior-cell launch: lane 0 of the first block sits on cell 1, so a row of 32k interior
-// cells fills k warps exactly and no warp spends FP64 issue slots on a ghost-cell lane.
-inline dim3 igrd(const Grid& g) {
-    return dim3((g.n[0] - 2 + 31) / 32, (g.n[1] - 2 + 7) / 8, g.D == 3 ? g.n[2] - 2 : 1);
-}
-#define ICELL_XYZ                                                                     \
-    const int x = 1 + blockIdx.x * blockDim.x + threadIdx.x;                          \
-    const int y = 1 + blockIdx.y * blockDim.y + threadIdx.y;                          \
-    const int z = g.D == 3 ? 1 + int(blockIdx.z) : 0;                                 \
-    if (x > g.n[0] - 2 || y > g.n[1] - 2) return;
-
-// Whole-grid launch: the x-range [1, n-2] one cell per lane, then one more block column whose
-// first warp takes the ghost cells x = 0 and x = n-1 of the block's 8 rows, so that a row of
-// 32k interior cells fills k warps and no warp of FP64 work runs with two lanes.
-inline dim3 ggrd(const Grid& g) { return dim3((g.n[0] - 2 + 31) / 32 + 1, (g.n[1] + 7) / 8, g.n[2]); }
-#define GCELL_XYZ                                                                     \
-    int x, y;                                                                         \
-    const int z = blockIdx.z;                                                         \
-    if (blockIdx.x + 1 < gridDim.x) {                                                 \
-        x = 1 + int(blockIdx.x) * 32 + int(threadIdx.x);                              \
-        y = int(blockIdx.y) * 8 + int(threadIdx.y);                                   \
-        if (x > g.n[0] - 2) return;                                                   \
-    } else {                                                                          \
-        if (threadIdx.y != 0 || threadIdx.x >= 16) return;                            \
-        x = (threadIdx.x & 1) ? g.n[0] - 1 : 0;                                       \
-        y = int(blockIdx.y) * 8 + (int(threadIdx.x) >> 1);                            \
-    }                                                                                 \
-    if (y >= g.n[1]) return;
-
-// Face-flux launch (momentum flux, viscous flux): the x-range [3, n-3], whose faces and
-// edges need no boundary rule, one cell per lane; then one more block column whose first
-// warp takes the x-boundary cells {1, 2, n-2, n-1} of the block's 8 rows.  A warp then runs
-// either the bulk path or the boundary path for all its lanes: FP64 issues per warp
-// instruction, whatever the number of active lanes, so a warp that mixes the two pays for both.
-inline dim3 split_grid(const Grid& g) {
-    const int wi = g.n[0] > 5 ? (g.n[0] - 5 + 31) / 32 : 0;
-    return dim3(wi + 1, (g.n[1] + 7) / 8, g.n[2]);
-}
-#define SPLIT_XYZ                                                                     \
-    int x, y;                                                                         \
-    const int z = blockIdx.z;                                                         \
-    if (blockIdx.x + 1 < gridDim.x) {                                                 \
-        x = 3 + int(blockIdx.x) * 32 + int(threadIdx.x);                              \
-        y = int(blockIdx.y) * 8 + int(threadIdx.y);                                   \
-        if (x > g.n[0] - 3) return;                                                   \
-    } else {                                                                          \
-        if (threadIdx.y != 0) return;                                                 \
-        const int kb = int(threadIdx.x) & 3;                                          \
-        x = kb < 2 ? 1 + kb : g.n[0] - 4 + kb;                                        \
-        if (kb >= 2 && x <= 2) return;                                                \
-        y = int(blockIdx.y) * 8 + (int(threadIdx.x) >> 2);                            \
-    }                                                                                 \
-    if (y >= g.n[1]) return;
-
-// x / getρ and x · getρ for a face between cells with fractions fa, fb (src/VOFutil.jl:176,
-// 198-201).  The mixed-face forms stay out of line: inlined, they are if-converted and their
-// predicated-off FP64 instructions would take FP64 issue slots on every bulk face.
-__device__ __noinline__ double div_rho_mixed(double lrho, double one_m, double v, double fa, double fb) {
-    return v / (lrho + one_m * ((fa + fb) / 2.0));
-}
-__device__ __noinline__ double mul_rho_mixed(double lrho, double one_m, double v, double fa, double fb) {
-    return v * (lrho + one_m * ((fa + fb) / 2.0));
-}
-__device__ __forceinline__ double div_rho(const MomConsts& k, double v, double fa, double fb) {
-    const unsigned long long a = dbits(fa), b = dbits(fb);
-    if (a == b && a == 0ull) return v * k.inv_lrho;
-    if (a == b && a == kOneBits) return v * k.inv_rho1;
-    return div_rho_mixed(k.lrho, k.one_m, v, fa, fb);
-}
-__device__ __forceinline__ double mul_rho(const MomConsts& k, double v, double fa, double fb) {
-    const unsigned long long a = dbits(fa), b = dbits(fb);
-    if (a == b && a == 0ull) return v * k.lrho;
-    if (a == b && a == kOneBits) return v * k.rho1;
-    return mul_rho_mixed(k.lrho, k.one_m, v, fa, fb);
-}
 
 // ------------------------------------------------------------------ velocity from momentum
 __global__ void ustar_kern(MomConsts k, const double* __restrict__ rhou, const double* __restrict__ f,
@@ -182,57 +105,12 @@ __device__ __forceinline__ double limiter(int which, double u, double c, double 
 }
 
 // ------------------------------------------------------------------ CMOM face flux
-struct FluxCtx {
-    MomConsts k;
-    int j, lim;
-    const double* us;
-    const double* rj;     // ρuf[:, j] before the 1/δt scaling
-    const double* fold;
-    double dt, inv_dt, half_inv_dt;
-    // pure-phase faces: m_old < m_out  <=>  |Ψ| > thr (thr = m_old/δt), l₂ = |Ψ|·kl (kl = δt/m_old)
-    double thr_l, thr_1, kl_l, kl_1;
-};
-
-// ρuf[X, j] (raw, before 1/δt) or, on a BC! face, the boundary velocity (returns true)
-__device__ __forceinline__ bool rraw(const FluxCtx& F, int c[3], double& v) {
-    const Grid& g = F.k.g;
-    if (vel_bc(g, F.j, c)) {
-        v = F.k.uBC[F.j];
-        return true;
-    }
-    v = F.rj[lin3(g, c)];
-    return false;
-}
 // Ψ = ϕ(i, CI(I,j), ρuf/δt) = (ρuf[a]/δt + ρuf[b]/δt)/2, one product when neither is a BC face
 __device__ __forceinline__ double face_psi(const FluxCtx& F, int ca[3], int cb[3]) {
     double va, vb;
     const bool ba = rraw(F, ca, va), bb = rraw(F, cb, vb);
     if (!ba && !bb) return (va + vb) * F.half_inv_dt;
     return ((ba ? va : va * F.inv_dt) + (bb ? vb : vb * F.inv_dt)) / 2.0;
-}
-
-// m_old = λρ + (1-λρ) dρ[X, i] with dρ = BCv!(f2face!(f_old)): kind 1 light, 2 dark (constants),
-// 0 mixed (value in m).  The upper normal face of a zero-gradient dimension is never written by
-// the reference and keeps the 1 it is initialised with (src/cVOF.jl:74).
-__device__ __forceinline__ int m_old_kind(const FluxCtx& F, int i, int c[3], double& m) {
-    const Grid& g = F.k.g;
-    if (face_bc(g, i, c)) return 2;
-    const long long P = lin3(g, c);
-    const double fa = F.fold[P], fb = F.fold[P - g.s[i]];
-    const unsigned long long a = dbits(fa), b = dbits(fb);
-    if (a == b && a == 0ull) return 1;
-    if (a == b && a == kOneBits) return 2;
-    m = F.k.lrho + F.k.one_m * ((fa + fb) / 2.0);
-    return 0;
-}
-
-// l₂ = m_out / m_old on a face whose old fractions fa, fb are not both 0 or both 1, or -1 when
-// m_old < m_out (the flux is then Ψ v_I).  Out of line so that bulk faces do not issue it.
-__device__ __noinline__ double l2_mixed(const FluxCtx& F, double fa, double fb, double aP) {
-    const double mOld = F.k.lrho + F.k.one_m * ((fa + fb) / 2.0);
-    const double mOut = aP * F.dt;
-    if (dlt(mOld, mOut)) return -1.0;
-    return mOut / mOld;
 }
 
 // ϕq (src/flow.jl:37-57) on the upwind triple (uu, cc, dd); cic = coords of the face.
@@ -353,8 +231,6 @@ __device__ __forceinline__ double dila_q(const MomConsts& k, double rq_l, double
 // and marches MU_ZC planes up z; each plane's ρ̄∂ⱼuⱼ/2 values (plus the x-1 / y-1 halo) go to
 // shared memory and the previous plane's stay in a register, so every value is computed once
 // (4 FP64 ops) instead of once per use (4 uses per cell).
-constexpr int MU_ZC = 16;
-
 template <int D>
 __global__ void __launch_bounds__(256) momupdate_kern(MomConsts k, int j, const double* __restrict__ Phi,
                                                       const double* __restrict__ uOld,
@@ -403,67 +279,6 @@ __global__ void __launch_bounds__(256) momupdate_kern(MomConsts k, int j, const 
 }
 
 // ------------------------------------------------------------------ viscosity
-struct ViscCtx {
-    MomConsts k;
-    const double* u;
-    const double* f;
-    double lmu, mu, mu_face0, mu_face1;   // μ at full-light / full-dark faces
-    double ratio;                         // λμ/λρ
-};
-
-// fFace = BCv!(f2face!(f)); the reference's fFace buffer aliases n̂, whose upper
-// normal face still holds uStar's Dirichlet value u_BC[d] from the last momentum sweep.
-__device__ __forceinline__ double fface(const ViscCtx& V, int d, int c[3]) {
-    const Grid& g = V.k.g;
-    if (face_bc(g, d, c)) return V.k.uBC[d];
-    const long long P = lin3(g, c);
-    const double fa = V.f[P], fb = V.f[P - g.s[d]];
-    if (dbits(fa) == dbits(fb)) return fa;
-    return (fa + fb) / 2.0;
-}
-
-// getμ(i,j,I,fFace,λμ,μ,λρ) (src/VOFutil.jl:186-191).  Kept out of line: inlined, its
-// mixed-face arithmetic is if-converted and the predicated-off FP64 instructions still take
-// FP64 issue slots in every bulk cell.
-__device__ __noinline__ double get_mu(const ViscCtx& V, int i, int j, const int cI[3]) {
-    int a[3] = {cI[0], cI[1], cI[2]}, b[3] = {cI[0], cI[1], cI[2]}, c[3] = {cI[0], cI[1], cI[2]},
-        d[3] = {cI[0], cI[1], cI[2]};
-    a[j] -= 1;
-    c[i] -= 1;
-    const double f1 = fface(V, i, a), f2 = fface(V, i, b), f3 = fface(V, j, c), f4 = fface(V, j, d);
-    const unsigned long long b1 = dbits(f1);
-    if (b1 == dbits(f2) && b1 == dbits(f3) && b1 == dbits(f4)) {
-        if (b1 == 0ull) return V.mu_face0;
-        if (b1 == kOneBits) return V.mu_face1;
-    }
-    const double s = (f1 + f2 + f3 + f4) / 4.0;
-    const double fr = V.k.lrho < 1.0 ? dmin(dmin(f1, f2), dmin(f3, f4)) : dmax(dmax(f1, f2), dmax(f3, f4));
-    const double fac = dlt(0.5, s) ? 1.0 : V.ratio;
-    return V.mu * dmin(V.lmu + (1.0 - V.lmu) * s, fac * (V.k.lrho + V.k.one_m * fr));
-}
-
-// getμ for an edge/face whose cells all lie at least two cells inside the grid (no ghost or
-// boundary-face rule applies): the fractions of the 3 (i == j) or 4 cells decide a pure phase
-// with integer compares; anything else goes to the general helper.
-__device__ __forceinline__ double get_mu_inner(const ViscCtx& V, int i, int j, const int c[3], long long K) {
-    const Grid& g = V.k.g;
-    const double* f = V.f;
-    const unsigned long long a = dbits(f[K]), b = dbits(f[K - g.s[i]]);
-    const unsigned long long e = dbits(i == j ? f[K - 2 * g.s[i]] : f[K - g.s[j]]);
-    const unsigned long long d = i == j ? a : dbits(f[K - g.s[i] - g.s[j]]);
-    if (a == b && a == e && a == d) {
-        if (a == 0ull) return V.mu_face0;
-        if (a == kOneBits) return V.mu_face1;
-    }
-    return get_mu(V, i, j, c);
-}
-
-__device__ __forceinline__ int pair_index(int D, int i, int j) {
-    if (i == j) return i;
-    const int a = i < j ? i : j, b = i < j ? j : i;
-    return D + (a == 0 ? (b - 1) : 2);   // (0,1)->D, (0,2)->D+1, (1,2)->D+2
-}
-
 template <int D>
 // five 256-thread blocks per SM (48 registers; the few spills stay in L1): more warps to cover the
 // FP64 latency
@@ -528,10 +343,31 @@ __device__ __forceinline__ bool mixed(double v) {
     return b != 0ull && b < kOneBits;   // 0 < v < 1 (sign bit set → huge, excluded)
 }
 
-// fᶠ along every d in one pass over f, and per d the list of interior cells where fᶠ is mixed
+// The reference's surface-tension buffer for direction d at coordinate c0, after surfTen!'s
+// `@inside fbuffer[I] = ϕ(d,I,f)` and BCf!(d, fbuffer) (src/surfaceTension.jl:10-11,
+// src/VOFutil.jl:76-89).  fbuffer is the cVOF's fᶠ, reused for every d, and BCf!(d, ·) never writes
+// the high ghost along a non-periodic d: that position keeps the buffer's previous content.  For
+// d > 0 it is the previous direction's value there (whose own ghost rules send the d coordinate to
+// n-2; every other coordinate is already mapped); for d = 0 it is the last VOF sweep's flux fᶠ, read
+// from prev0 (NULL: zero, which is that flux on the plane whenever the wall's normal velocity is 0).
+__device__ __forceinline__ double fbuffer_at(const Grid& g, const double* __restrict__ f, int d, const int c0[3],
+                                             const double* __restrict__ prev0) {
+    int c[3] = {c0[0], c0[1], c0[2]};
+    int dd = d;
+    if (face_bc(g, d, c)) {
+        if (d == 0) return prev0 ? prev0[lin3(g, c)] : 0.0;
+        dd = d - 1;
+        face_bc(g, dd, c);
+    }
+    const long long P = lin3(g, c);
+    const double fa = f[P], fm = f[P - g.s[dd]];
+    return (dbits(fa) == dbits(fm)) ? fa : (fa + fm) / 2.0;
+}
+
+// fbuffer along every d in one pass over f, and per d the list of interior cells where it is mixed
 // (the only cells surften_kern changes), appended one warp at a time
-__global__ void fbuffer_kern(MomConsts k, const double* __restrict__ f, double* __restrict__ fb,
-                             int* __restrict__ list, unsigned int* __restrict__ count) {
+__global__ void fbuffer_kern(MomConsts k, const double* __restrict__ f, const double* __restrict__ prev0,
+                             double* __restrict__ fb, int* __restrict__ list, unsigned int* __restrict__ count) {
     const Grid& g = k.g;
     GCELL_XYZ
     const int c0[3] = {x, y, z};
@@ -539,13 +375,7 @@ __global__ void fbuffer_kern(MomConsts k, const double* __restrict__ f, double* 
     const long long I = lin(g, x, y, z);
     const int lane = int(threadIdx.x) & 31;
     for (int d = 0; d < g.D; ++d) {
-        int c[3] = {x, y, z};
-        // BCf!(d, ·): the high ghost along a zero-gradient d is not written by the
-        // reference (it keeps older buffer contents); it is taken as a zero-gradient copy here.
-        if (face_bc(g, d, c)) c[d] = g.n[d] - 2;
-        const long long P = lin3(g, c);
-        const double fa = f[P], fm = f[P - g.s[d]];
-        const double v = (dbits(fa) == dbits(fm)) ? fa : (fa + fm) / 2.0;
+        const double v = fbuffer_at(g, f, d, c0, prev0);
         fb[d * g.N + I] = v;
         const bool want = inner && mixed(v);
         const unsigned int bal = __ballot_sync(__activemask(), want);
@@ -863,11 +693,11 @@ cudaError_t k_zero(double* a, long long n, cudaStream_t s) {
     { zero_kern<<<1216, 256, 0, s>>>(a, n); ia::note_launch(); }
     return cudaGetLastError();
 }
-cudaError_t k_surften(const MomConsts& k, const double* f, double eta, double* fb, double* r, int* list,
-                      unsigned int* count, cudaStream_t s) {
+cudaError_t k_surften(const MomConsts& k, const double* f, const double* prev0, double eta, double* fb, double* r,
+                      int* list, unsigned int* count, cudaStream_t s) {
     const Grid& g = k.g;
     cudaMemsetAsync(count, 0, sizeof(unsigned int) * g.D, s);
-    { fbuffer_kern<<<ggrd(g), blk(), 0, s>>>(k, f, fb, list, count); ia::note_launch(); }
+    { fbuffer_kern<<<ggrd(g), blk(), 0, s>>>(k, f, prev0, fb, list, count); ia::note_launch(); }
     for (int d = 0; d < g.D; ++d) {
         double* fbd = fb + d * g.N;
         const int* ld = list + d * g.N;

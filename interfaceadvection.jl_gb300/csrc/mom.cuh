@@ -31,10 +31,11 @@ cudaError_t k_momupdate(const MomConsts& k, int j, const double* Phi, const doub
 cudaError_t k_visc(const MomConsts& k, const double* u, const double* f, double lmu, double mu, double* Phi6,
                    double* r, cudaStream_t s);
 cudaError_t k_zero(double* a, long long n, cudaStream_t s);
-// surfTen! (src/surfaceTension.jl:8-20), one direction d
-// surfTen! along every d: fb holds D face-fraction fields, list D cell lists of N entries, count D
-cudaError_t k_surften(const MomConsts& k, const double* f, double eta, double* fb, double* r, int* list,
-                      unsigned int* count, cudaStream_t s);
+// surfTen! (src/surfaceTension.jl:8-20) along every d: fb holds D face-fraction fields, list D cell
+// lists of N entries, count D; prev0 (may be NULL = zeros) is the content of the reference's fbuffer
+// before the call, of which only the high x-ghost plane is read
+cudaError_t k_surften(const MomConsts& k, const double* f, const double* prev0, double eta, double* fb, double* r,
+                      int* list, unsigned int* count, cudaStream_t s);
 // updateU! (src/flow.jl:244-252) on interior cells; writes ρu when write_rhou
 cudaError_t k_updateu(const MomConsts& k, double* u, double* rhou, const double* u0, const double* F, double dt,
                       const double* fref, const double* fupd, double w, bool write_rhou, cudaStream_t s);
@@ -48,5 +49,17 @@ cudaError_t k_correct(const MomConsts& k, double* u, const double* L, double* x,
 cudaError_t k_cfl(const MomConsts& k, const double* u, unsigned long long* out2, cudaStream_t s);
 // a = (a + b) / 2 over n entries
 cudaError_t k_average(double* a, const double* b, long long n, cudaStream_t s);
+
+// Float-float (FP32-pair) counterparts of the momentum chain (mom_ff.cu): uStar, the face fluxes and
+// the viscous fluxes are pairs (float2); ρu, u and the forcing r stay FP64 fields.
+cudaError_t k_ustar_ff(const MomConsts& k, const double* rhou, const double* f, float2* ustar, cudaStream_t s);
+cudaError_t k_momflux_ff(const MomConsts& k, int j, int limiter, const float2* ustar, const double* rhouf_j,
+                         const double* fold, double dt, float2* Phi, cudaStream_t s);
+cudaError_t k_momupdate_ff(const MomConsts& k, int j, const float2* Phi, const double* uOld, const double* u1,
+                           const double* u2, const int8_t* cbar, double dt, double* rhou, cudaStream_t s);
+cudaError_t k_visc_ff(const MomConsts& k, const double* u, const double* f, double lmu, double mu, float2* Phi6,
+                      double* r, cudaStream_t s);
+cudaError_t k_updateu_ff(const MomConsts& k, double* u, double* rhou, const double* u0, const double* F, double dt,
+                         const double* fref, const double* fupd, double w, bool write_rhou, cudaStream_t s);
 
 }  // namespace ia

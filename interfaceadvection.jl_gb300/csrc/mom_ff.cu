@@ -1,0 +1,505 @@
+// Float-float momentum kernels: the CMOM momentum sweep (src/flow.jl:20-57, 212-241), the viscous
+// forcing (src/flow.jl:119-153) and the velocity update (src/flow.jl:244-252) of mom.cu with their
+// arithmetic on FP32 pairs (ff.cuh) instead of FP64.
+//
+// The FP64 kernels of mom.cu spend 11 to 33 FP64 operations per cell; GB300 issues FP64 at 1/64 of
+// the FP32 rate, so they run at ~80 % FP64-pipe activity and 12-37 % of HBM bandwidth.  Here the
+// same formulas, in the same order, run on FP32 pairs (48-bit significands, relative precision
+// ~2^-46): every FP64 field value is split into a pair with integer operations when loaded, results
+// that leave the momentum chain (ρu, u, the forcing r) are joined back to FP64 with one FP64
+// addition each, and the intermediates passed between these kernels (uStar, the face fluxes Φ, the
+// viscous fluxes) are stored as pairs (float2, the size of a double).  Full/empty tests, the
+// boundary rules and the rare mixed-cell branches (mixed-face densities, viscosities, the SynDRoM
+// mass ratio on a mixed donor face) are those of mom.cu: the branch decisions use the same integer
+// tests and the rare branches run the same FP64 code.
+//
+// Differences to the FP64 kernels are rounding-level (a few units of 2^-46 of the operands of each
+// operation); they are checked against the FP64 oracle in the step parity tests at 1e-10.
+#include <cuda_runtime.h>
+
+#include <cstring>
+
+#include "ff.cuh"
+#include "ia_geom.cuh"
+#include "mom.cuh"
+#include "mom_common.cuh"
+
+namespace ia {
+
+namespace {
+
+// float-float copies of the step constants (MomConsts), the momentum-flux constants (FluxCtx) and the
+// pure-phase face viscosities (ViscCtx)
+struct MomFF {
+    ff lrho, rho1, inv_lrho, inv_rho1;
+    ff uBC[3], gvec[3];
+};
+struct FluxFF {
+    ff half_inv_dt, inv_dt, thr_l, thr_1, kl_l, kl_1, sixth;
+};
+struct ViscFF {
+    unsigned long long mu0bits, mu1bits;   // the FP64 pure-phase values get_mu returns
+    ff mu_face0, mu_face1;
+};
+
+MomFF mom_ff_consts(const MomConsts& k) {
+    MomFF q;
+    q.lrho = ff_split(k.lrho);
+    q.rho1 = ff_split(k.rho1);
+    q.inv_lrho = ff_split(k.inv_lrho);
+    q.inv_rho1 = ff_split(k.inv_rho1);
+    for (int d = 0; d < 3; ++d) {
+        q.uBC[d] = ff_split(k.uBC[d]);
+        q.gvec[d] = ff_split(k.gvec[d]);
+    }
+    return q;
+}
+
+__device__ __forceinline__ ff ldff(const float2* p) {
+    const float2 v = *p;
+    return {v.x, v.y};
+}
+__device__ __forceinline__ void stff(float2* p, ff v) { *p = make_float2(v.hi, v.lo); }
+
+// x / getρ and x · getρ on a face with cell fractions fa, fb (src/VOFutil.jl:176, 198-211)
+__device__ __forceinline__ ff div_rho_ff(const MomConsts& k, const MomFF& q, ff v, double fa, double fb) {
+    const unsigned long long a = dbits(fa), b = dbits(fb);
+    if (a == b && a == 0ull) return ff_mul(v, q.inv_lrho);
+    if (a == b && a == kOneBits) return ff_mul(v, q.inv_rho1);
+    return ff_split(div_rho_mixed(k.lrho, k.one_m, ff_join(v), fa, fb));
+}
+__device__ __forceinline__ ff mul_rho_ff(const MomConsts& k, const MomFF& q, ff v, double fa, double fb) {
+    const unsigned long long a = dbits(fa), b = dbits(fb);
+    if (a == b && a == 0ull) return ff_mul(v, q.lrho);
+    if (a == b && a == kOneBits) return ff_mul(v, q.rho1);
+    return ff_split(mul_rho_mixed(k.lrho, k.one_m, ff_join(v), fa, fb));
+}
+
+// ------------------------------------------------------------------ uStar = BC!(ρu / ρ(f))
+__global__ void ustar_ff_kern(MomConsts k, MomFF q, const double* __restrict__ rhou, const double* __restrict__ f,
+                              float2* __restrict__ us) {
+    const Grid& g = k.g;
+    GCELL_XYZ
+    const long long O = lin(g, x, y, z);
+    for (int i = 0; i < g.D; ++i) {
+        int c[3] = {x, y, z};
+        ff v;
+        if (vel_bc(g, i, c)) {
+            v = q.uBC[i];
+        } else {
+            const long long P = lin3(g, c);
+            v = div_rho_ff(k, q, ff_split(rhou[P + i * g.N]), f[P], f[P - g.s[i]]);
+        }
+        stff(us + O + i * g.N, v);
+    }
+}
+
+// ------------------------------------------------------------------ limiters (src/flow.jl:5-15)
+__device__ __forceinline__ ff ff_signed(bool pos, ff v) { return pos ? v : -v; }
+
+template <int LIM>
+__device__ __forceinline__ ff limiter_ff(const FluxFF& Q, ff u, ff c, ff d) {
+    if (LIM == IA_LIMITER_UPWIND) return c;
+    if (LIM == IA_LIMITER_MINMOD)
+        return ff_median3(ff_scale2(ff_sub(ff_mulf(c, 3.0f), u), 0.5f), c, ff_scale2(ff_add(c, d), 0.5f));
+    if (LIM == IA_LIMITER_VANALBADA1) {
+        const ff al = ff_sub(c, u), be = ff_sub(d, c);
+        const ff fac = (ff_zero(al) && ff_zero(be)) ? ff_from(0.0f)
+                                                    : ff_div(ff_add(al, be), ff_add(ff_mul(al, al), ff_mul(be, be)));
+        return ff_add(c, ff_scale2(ff_mul(ff_max(ff_mul(al, be), ff_from(0.0f)), fac), 0.5f));
+    }
+    if (LIM == IA_LIMITER_SWEBY || LIM == IA_LIMITER_SUPERBEE || LIM == IA_LIMITER_TVDCEN ||
+        LIM == IA_LIMITER_TVDDOWN) {
+        if (!ff_lt(ff_min(u, d), c) || !ff_lt(c, ff_max(u, d))) return c;
+        const bool s = ff_pos(ff_sub(d, u));               // c strictly between u and d: d - u != 0
+        const ff cu = ff_signed(s, ff_sub(c, u)), dc = ff_signed(s, ff_sub(d, c));
+        ff r;
+        if (LIM == IA_LIMITER_TVDCEN) {
+            r = ff_min(cu, ff_scale2(dc, 0.5f));
+        } else if (LIM == IA_LIMITER_TVDDOWN) {
+            r = ff_min(cu, dc);
+        } else {
+            const float gam = LIM == IA_LIMITER_SWEBY ? 1.5f : 2.0f;
+            r = ff_scale2(ff_max(ff_max(ff_from(0.0f), ff_min(ff_mulf(cu, gam), dc)), ff_min(cu, ff_mulf(dc, gam))),
+                          0.5f);
+        }
+        return ff_add(c, ff_signed(s, r));
+    }
+    // Koren: median(fma(-2, u, fma(7, c, d)) / 6, c, median(2c - u, c, d))
+    const ff t = ff_mul(ff_sub(ff_add(ff_mulf(c, 7.0f), d), ff_scale2(u, 2.0f)), Q.sixth);
+    return ff_median3(t, c, ff_median3(ff_sub(ff_scale2(c, 2.0f), u), c, d));
+}
+
+// SynDRoM blend Ψ (v_d + l₂ (v_I - v_d)) once l₂ is known (src/flow.jl:37-57)
+__device__ __forceinline__ ff blend(ff Psi, ff l2, ff cc, ff vd) {
+    return ff_mul(Psi, ff_add(ff_mul(l2, ff_sub(cc, vd)), vd));
+}
+
+// l₂ = m_out / m_old on a face whose old density m is mixed, or -1 when m_old < m_out
+__device__ __noinline__ double l2_from_m(double mOld, double aP, double dt) {
+    const double mOut = aP * dt;
+    if (dlt(mOld, mOut)) return -1.0;
+    return mOut / mOld;
+}
+
+template <int LIM>
+__device__ ff phiq_inner_ff(const FluxCtx& F, const FluxFF& Q, ff Psi, ff uu, ff cc, ff dd, double fa, double fb) {
+    const ff vd = limiter_ff<LIM>(Q, uu, cc, dd);
+    const ff aP = ff_abs(Psi);
+    const unsigned long long a = dbits(fa), b = dbits(fb);
+    ff l2;
+    if (a == b && (a == 0ull || a == kOneBits)) {
+        const bool light = a == 0ull;
+        if (ff_lt(light ? Q.thr_l : Q.thr_1, aP)) return ff_mul(Psi, cc);
+        l2 = ff_mul(aP, light ? Q.kl_l : Q.kl_1);
+    } else {
+        const double l = l2_mixed(F, fa, fb, ff_join(aP));
+        if (l < 0.0) return ff_mul(Psi, cc);
+        l2 = ff_split(l);
+    }
+    return blend(Psi, l2, cc, vd);
+}
+
+template <int LIM>
+__device__ ff phiq_ff(const FluxCtx& F, const FluxFF& Q, int i, const int cic[3], ff Psi, ff uu, ff cc, ff dd) {
+    int c[3] = {cic[0], cic[1], cic[2]};
+    if (ff_pos(Psi)) c[F.j] -= 1;                        // IiCell = Ψ>0 ? Ii-δj : Ii
+    const ff vd = limiter_ff<LIM>(Q, uu, cc, dd);
+    const ff aP = ff_abs(Psi);
+    double mOld = 0.0;
+    const int kind = m_old_kind(F, i, c, mOld);
+    ff l2;
+    if (kind == 1) {
+        if (ff_lt(Q.thr_l, aP)) return ff_mul(Psi, cc);
+        l2 = ff_mul(aP, Q.kl_l);
+    } else if (kind == 2) {
+        if (ff_lt(Q.thr_1, aP)) return ff_mul(Psi, cc);
+        l2 = ff_mul(aP, Q.kl_1);
+    } else {
+        const double l = l2_from_m(mOld, ff_join(aP), F.dt);
+        if (l < 0.0) return ff_mul(Psi, cc);
+        l2 = ff_split(l);
+    }
+    return blend(Psi, l2, cc, vd);
+}
+
+// Ψ = ϕ(i, CI(I,j), ρuf/δt) on a face near a boundary (a BC! face holds u_BC, not ρuf)
+__device__ __forceinline__ ff face_psi_ff(const FluxCtx& F, const FluxFF& Q, int ca[3], int cb[3]) {
+    double va, vb;
+    const bool ba = rraw(F, ca, va), bb = rraw(F, cb, vb);
+    const ff a = ff_split(va), b = ff_split(vb);
+    if (!ba && !bb) return ff_mul(ff_add(a, b), Q.half_inv_dt);
+    return ff_scale2(ff_add(ba ? a : ff_mul(a, Q.inv_dt), bb ? b : ff_mul(b, Q.inv_dt)), 0.5f);
+}
+
+template <int LIM>
+__global__ void __launch_bounds__(256, 4) momflux_ff_kern(FluxCtx F, FluxFF Q, const float2* __restrict__ us,
+                                                          float2* __restrict__ Phi) {
+    const Grid& g = F.k.g;
+    SPLIT_XYZ
+    const int j = F.j;
+    int c[3] = {x, y, z};
+    bool inner = true;
+    for (int e = 0; e < g.D; ++e) {
+        const int hi = (e == j) ? g.n[e] - 1 : g.n[e] - 2;
+        if (c[e] < 1 || c[e] > hi) return;
+        if (c[e] < 3 || c[e] > g.n[e] - 3) inner = false;
+    }
+    const long long K = lin(g, x, y, z);
+    if (inner) {
+        // no ghost, wall, periodic-image or boundary-face rule reaches this face's stencil
+        const long long sj = g.s[j];
+        const ff rK = ff_split(F.rj[K]);
+        for (int i = 0; i < g.D; ++i) {
+            const long long si = g.s[i];
+            const ff Psi = ff_mul(ff_add(rK, ff_split(F.rj[K - si])), Q.half_inv_dt);
+            const float2* u = us + i * g.N;
+            const bool pos = ff_pos(Psi);
+            const ff uu = ldff(u + (pos ? K - 2 * sj : K + sj));
+            const ff cc = ldff(u + (pos ? K - sj : K));
+            const ff dd = ldff(u + (pos ? K : K - sj));
+            const long long P = pos ? K - sj : K;
+            stff(Phi + K + i * g.N, phiq_inner_ff<LIM>(F, Q, Psi, uu, cc, dd, F.fold[P], F.fold[P - si]));
+        }
+        return;
+    }
+    const bool per = g.isper(j);
+    if (per && c[j] == g.n[j] - 1) c[j] = 1;              // periodic upper face = lower face
+    const long long Kk = lin3(g, c);
+    const int kj = c[j];
+    const long long sj = g.s[j];
+    const bool lower = kj == 1, upper = !per && kj == g.n[j] - 1;
+    for (int i = 0; i < g.D; ++i) {
+        int ca[3] = {c[0], c[1], c[2]}, cb[3] = {c[0], c[1], c[2]};
+        cb[i] -= 1;
+        const ff Psi = face_psi_ff(F, Q, ca, cb);                      // ϕ(i, CI(I,j), ρuf)
+        const float2* u = us + i * g.N;
+        const bool pos = ff_pos(Psi);
+        ff uu, cc, dd;
+        if (lower && !per) {               // ϕuL: linear extrapolation below the wall
+            if (pos) { cc = ldff(u + Kk - sj); dd = ldff(u + Kk); uu = ff_sub(ff_scale2(cc, 2.0f), dd); }
+            else { uu = ldff(u + Kk + sj); cc = ldff(u + Kk); dd = ldff(u + Kk - sj); }
+        } else if (lower) {                // ϕuP: periodic image of I-2δj
+            if (pos) { uu = ldff(u + Kk + (long long)(g.n[j] - 3 - kj) * sj); cc = ldff(u + Kk - sj); dd = ldff(u + Kk); }
+            else { uu = ldff(u + Kk + sj); cc = ldff(u + Kk); dd = ldff(u + Kk - sj); }
+        } else if (upper) {                // ϕuR
+            if (ff_neg(Psi)) { cc = ldff(u + Kk); dd = ldff(u + Kk - sj); uu = ff_sub(ff_scale2(cc, 2.0f), dd); }
+            else { uu = ldff(u + Kk - 2 * sj); cc = ldff(u + Kk - sj); dd = ldff(u + Kk); }
+        } else {                           // ϕu
+            if (pos) { uu = ldff(u + Kk - 2 * sj); cc = ldff(u + Kk - sj); dd = ldff(u + Kk); }
+            else { uu = ldff(u + Kk + sj); cc = ldff(u + Kk); dd = ldff(u + Kk - sj); }
+        }
+        stff(Phi + K + i * g.N, phiq_ff<LIM>(F, Q, i, c, Psi, uu, cc, dd));
+    }
+}
+
+// ------------------------------------------------------------------ ρu += δt (Φ(I) - Φ(I+δj) + uOld ϕ(i,I,ρ̄∂ⱼuⱼ))
+// ρ̄∂ⱼuⱼ/2 at a (ghost-mapped) cell: getρ(I,c̄,λρ)(∂(d,I,u)+∂(d,I,u⁰))/4
+__device__ __forceinline__ ff dila_q_ff(const Grid& g, ff rq_l, ff rq_1, int d, int c[3], const double* u1,
+                                        const double* u2, const int8_t* cbar) {
+    for (int e = 0; e < g.D; ++e) c[e] = bc_src(g, e, c[e]);
+    const long long P = lin3(g, c);
+    const long long sd = g.s[d];
+    const ff du = ff_add(ff_sub(ff_split(u1[P + sd]), ff_split(u1[P])), ff_sub(ff_split(u2[P + sd]), ff_split(u2[P])));
+    return ff_mul(cbar[P] ? rq_1 : rq_l, du);
+}
+
+// same z-march over 32 x 8 columns as momupdate_kern (mom.cu): each plane's ρ̄∂ⱼuⱼ/2 (plus the
+// x-1 / y-1 halo) is computed once into shared memory
+template <int D>
+__global__ void __launch_bounds__(256) momupdate_ff_kern(MomConsts k, MomFF q, int j, const float2* __restrict__ Phi,
+                                                         const double* __restrict__ uOld,
+                                                         const double* __restrict__ u1d, const double* __restrict__ u2d,
+                                                         const int8_t* __restrict__ cbar, ff dt,
+                                                         double* __restrict__ rhou) {
+    const Grid& g = k.g;
+    __shared__ float2 tile[9][33];
+    const int tx = threadIdx.x, ty = threadIdx.y;
+    const int x0 = 1 + blockIdx.x * 32, y0 = 1 + blockIdx.y * 8;
+    const int x = x0 + tx, y = y0 + ty;
+    const bool active = x <= g.n[0] - 2 && y <= g.n[1] - 2;
+    const ff rq_l = ff_scale2(q.lrho, 0.25f), rq_1 = ff_scale2(q.rho1, 0.25f);
+    const int zs = D == 3 ? 1 + int(blockIdx.z) * MU_ZC : 0;
+    const int ze = D == 3 ? min(zs + MU_ZC, g.n[2] - 1) : 1;
+    ff dprev = ff_from(0.0f);
+    if (D == 3 && active) {
+        int cm[3] = {x, y, zs - 1};
+        dprev = dila_q_ff(g, rq_l, rq_1, j, cm, u1d, u2d, cbar);
+    }
+    for (int z = zs; z < ze; ++z) {
+        for (int l = ty * 32 + tx; l < 9 * 33; l += 256) {
+            const int xx = x0 - 1 + l % 33, yy = y0 - 1 + l / 33;
+            ff v = ff_from(0.0f);
+            if (xx <= g.n[0] - 2 && yy <= g.n[1] - 2) {
+                int cc[3] = {xx, yy, z};
+                v = dila_q_ff(g, rq_l, rq_1, j, cc, u1d, u2d, cbar);
+            }
+            tile[l / 33][l % 33] = make_float2(v.hi, v.lo);
+        }
+        __syncthreads();
+        if (active) {
+            const long long I = lin(g, x, y, z);
+            const float2 tI = tile[ty + 1][tx + 1], tx0 = tile[ty + 1][tx], ty0 = tile[ty][tx + 1];
+            const ff dI = {tI.x, tI.y};
+            const ff dm[3] = {{tx0.x, tx0.y}, {ty0.x, ty0.y}, dprev};
+            const long long sj = g.s[j];
+#pragma unroll
+            for (int i = 0; i < D; ++i) {
+                const ff flux = ff_sub(ldff(Phi + I + i * g.N), ldff(Phi + I + sj + i * g.N));
+                const ff r = ff_add(ff_mul(ff_split(uOld[I + i * g.N]), ff_add(dI, dm[i])), flux);
+                rhou[I + i * g.N] = ff_join(ff_add(ff_mul(dt, r), ff_split(rhou[I + i * g.N])));
+            }
+            dprev = dI;
+        }
+        __syncthreads();
+    }
+}
+
+// ------------------------------------------------------------------ viscosity
+// the pure-phase values are recognised by their bit patterns (no FP64 comparison)
+__device__ __forceinline__ ff mu_ff(const ViscFF& W, double mu) {
+    const unsigned long long b = dbits(mu);
+    if (b == W.mu0bits) return W.mu_face0;
+    if (b == W.mu1bits) return W.mu_face1;
+    return ff_split(mu);
+}
+
+template <int D>
+__global__ void __launch_bounds__(256, 4) viscflux_ff_kern(ViscCtx V, ViscFF W, float2* __restrict__ Phi6) {
+    const Grid& g = V.k.g;
+    SPLIT_XYZ
+    const int c[3] = {x, y, z};
+    const long long K = lin(g, x, y, z);
+    bool inner = true;
+#pragma unroll
+    for (int e = 0; e < D; ++e)
+        if (c[e] < 3 || c[e] > g.n[e] - 3) inner = false;
+    if (inner) {
+        ff uK[D];
+#pragma unroll
+        for (int i = 0; i < D; ++i) uK[i] = ff_split(V.u[K + i * g.N]);
+#pragma unroll
+        for (int i = 0; i < D; ++i)
+#pragma unroll
+            for (int j = i; j < D; ++j) {
+                const ff mu = mu_ff(W, get_mu_inner(V, i, j, c, K));
+                const ff sji = ff_sub(uK[i], ff_split(V.u[K - g.s[j] + i * g.N]));
+                const ff sij = ff_sub(uK[j], ff_split(V.u[K - g.s[i] + j * g.N]));
+                stff(Phi6 + pair_index(D, i, j) * g.N + K, -ff_mul(mu, ff_add(sji, sij)));
+            }
+        return;
+    }
+    for (int i = 0; i < D; ++i)
+        for (int j = i; j < D; ++j) {
+            bool ok = true;
+            for (int e = 0; e < D; ++e) {
+                const int hi = (e == i || e == j) ? g.n[e] - 1 : g.n[e] - 2;
+                if (c[e] < 1 || c[e] > hi) ok = false;
+            }
+            if (!ok) continue;
+            const ff mu = mu_ff(W, get_mu(V, i, j, c));
+            const ff sji = ff_sub(ff_split(V.u[K + i * g.N]), ff_split(V.u[K - g.s[j] + i * g.N]));
+            const ff sij = ff_sub(ff_split(V.u[K + j * g.N]), ff_split(V.u[K - g.s[i] + j * g.N]));
+            stff(Phi6 + pair_index(D, i, j) * g.N + K, -ff_mul(mu, ff_add(sji, sij)));
+        }
+}
+
+template <int D>
+__global__ void viscacc_ff_kern(Grid g, const float2* __restrict__ Phi6, double* __restrict__ r) {
+    ICELL_XYZ
+    const long long I = lin(g, x, y, z);
+#pragma unroll
+    for (int i = 0; i < D; ++i) {
+        ff acc = ff_from(0.0f);
+#pragma unroll
+        for (int j = 0; j < D; ++j) {
+            const float2* P = Phi6 + pair_index(D, i, j) * g.N;
+            acc = ff_sub(ff_add(acc, ldff(P + I)), ldff(P + I + g.s[j]));
+        }
+        r[I + i * g.N] = ff_join(acc);
+    }
+}
+
+// ------------------------------------------------------------------ updateU! (src/flow.jl:244-252)
+template <bool A0>
+__global__ void updateu_ff_kern(MomConsts k, MomFF q, double* __restrict__ u, double* __restrict__ rhou,
+                                const double* __restrict__ u0, const double* __restrict__ F, ff dt, ff w, ff a,
+                                ff dtw, const double* __restrict__ fref, const double* __restrict__ fupd,
+                                bool write_rhou) {
+    const Grid& g = k.g;
+    ICELL_XYZ
+    const long long I = lin(g, x, y, z);
+    for (int i = 0; i < g.D; ++i) {
+        const long long qI = I + i * g.N;
+        ff rn = ff_add(ff_split(rhou[qI]), ff_mul(ff_split(F[qI]), dt));
+        if (!A0) {
+            const ff rho0 = mul_rho_ff(k, q, ff_split(u0[qI]), fref[I], fref[I - g.s[i]]);   // u2ρu!(n̂, u⁰, c.f)
+            rn = ff_add(ff_mul(a, rho0), rn);
+        }
+        rn = ff_mul(rn, w);
+        ff v = div_rho_ff(k, q, rn, fupd[I], fupd[I - g.s[i]]);
+        if (k.has_g) v = ff_add(ff_mul(dtw, q.gvec[i]), v);
+        u[qI] = ff_join(v);
+        if (write_rhou) rhou[qI] = ff_join(rn);
+    }
+}
+
+}  // namespace
+
+cudaError_t k_ustar_ff(const MomConsts& k, const double* rhou, const double* f, float2* ustar, cudaStream_t s) {
+    { ustar_ff_kern<<<ggrd(k.g), blk(), 0, s>>>(k, mom_ff_consts(k), rhou, f, ustar); ia::note_launch(); }
+    return cudaGetLastError();
+}
+
+cudaError_t k_momflux_ff(const MomConsts& k, int j, int limiter, const float2* ustar, const double* rhouf_j,
+                         const double* fold, double dt, float2* Phi, cudaStream_t s) {
+    FluxCtx F;
+    F.k = k;
+    F.j = j;
+    F.lim = limiter;
+    F.us = nullptr;
+    F.rj = rhouf_j;
+    F.fold = fold;
+    F.dt = dt;
+    F.inv_dt = 1.0 / dt;
+    F.half_inv_dt = 0.5 / dt;
+    F.thr_l = k.lrho / dt;
+    F.thr_1 = k.rho1 / dt;
+    F.kl_l = dt * k.inv_lrho;
+    F.kl_1 = dt * k.inv_rho1;
+    FluxFF Q;
+    Q.half_inv_dt = ff_split(F.half_inv_dt);
+    Q.inv_dt = ff_split(F.inv_dt);
+    Q.thr_l = ff_split(F.thr_l);
+    Q.thr_1 = ff_split(F.thr_1);
+    Q.kl_l = ff_split(F.kl_l);
+    Q.kl_1 = ff_split(F.kl_1);
+    Q.sixth = ff_split(1.0 / 6.0);
+    const dim3 gr = split_grid(k.g);
+    switch (limiter) {
+        case IA_LIMITER_UPWIND: { momflux_ff_kern<IA_LIMITER_UPWIND><<<gr, blk(), 0, s>>>(F, Q, ustar, Phi); ia::note_launch(); } break;
+        case IA_LIMITER_MINMOD: { momflux_ff_kern<IA_LIMITER_MINMOD><<<gr, blk(), 0, s>>>(F, Q, ustar, Phi); ia::note_launch(); } break;
+        case IA_LIMITER_VANALBADA1: { momflux_ff_kern<IA_LIMITER_VANALBADA1><<<gr, blk(), 0, s>>>(F, Q, ustar, Phi); ia::note_launch(); } break;
+        case IA_LIMITER_SWEBY: { momflux_ff_kern<IA_LIMITER_SWEBY><<<gr, blk(), 0, s>>>(F, Q, ustar, Phi); ia::note_launch(); } break;
+        case IA_LIMITER_SUPERBEE: { momflux_ff_kern<IA_LIMITER_SUPERBEE><<<gr, blk(), 0, s>>>(F, Q, ustar, Phi); ia::note_launch(); } break;
+        case IA_LIMITER_TVDCEN: { momflux_ff_kern<IA_LIMITER_TVDCEN><<<gr, blk(), 0, s>>>(F, Q, ustar, Phi); ia::note_launch(); } break;
+        case IA_LIMITER_TVDDOWN: { momflux_ff_kern<IA_LIMITER_TVDDOWN><<<gr, blk(), 0, s>>>(F, Q, ustar, Phi); ia::note_launch(); } break;
+        default: { momflux_ff_kern<IA_LIMITER_KOREN><<<gr, blk(), 0, s>>>(F, Q, ustar, Phi); ia::note_launch(); } break;
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t k_momupdate_ff(const MomConsts& k, int j, const float2* Phi, const double* uOld, const double* u1,
+                           const double* u2, const int8_t* cbar, double dt, double* rhou, cudaStream_t s) {
+    const Grid& g = k.g;
+    const dim3 tg((g.n[0] - 2 + 31) / 32, (g.n[1] - 2 + 7) / 8, g.D == 3 ? (g.n[2] - 2 + MU_ZC - 1) / MU_ZC : 1);
+    const MomFF q = mom_ff_consts(k);
+    const ff dtf = ff_split(dt);
+    if (g.D == 3) { momupdate_ff_kern<3><<<tg, blk(), 0, s>>>(k, q, j, Phi, uOld, u1 + j * g.N, u2 + j * g.N, cbar, dtf, rhou); ia::note_launch(); }
+    else { momupdate_ff_kern<2><<<tg, blk(), 0, s>>>(k, q, j, Phi, uOld, u1 + j * g.N, u2 + j * g.N, cbar, dtf, rhou); ia::note_launch(); }
+    return cudaGetLastError();
+}
+
+cudaError_t k_visc_ff(const MomConsts& k, const double* u, const double* f, double lmu, double mu, float2* Phi6,
+                      double* r, cudaStream_t s) {
+    ViscCtx V;
+    V.k = k;
+    V.u = u;
+    V.f = f;
+    V.lmu = lmu;
+    V.mu = mu;
+    V.ratio = lmu / k.lrho;
+    auto lin_prop = [](double sv, double l) { return l + (1.0 - l) * sv; };
+    auto mu_at = [&](double sv) {
+        const double fac = (sv > 0.5) ? 1.0 : lmu / k.lrho;
+        const double a = lin_prop(sv, lmu), b = fac * lin_prop(sv, k.lrho);
+        return mu * (b < a ? b : a);
+    };
+    V.mu_face0 = mu_at(0.0);
+    V.mu_face1 = mu_at(1.0);
+    ViscFF W;
+    std::memcpy(&W.mu0bits, &V.mu_face0, 8);
+    std::memcpy(&W.mu1bits, &V.mu_face1, 8);
+    W.mu_face0 = ff_split(V.mu_face0);
+    W.mu_face1 = ff_split(V.mu_face1);
+    if (k.g.D == 3) {
+        { viscflux_ff_kern<3><<<split_grid(k.g), blk(), 0, s>>>(V, W, Phi6); ia::note_launch(); }
+        { viscacc_ff_kern<3><<<igrd(k.g), blk(), 0, s>>>(k.g, Phi6, r); ia::note_launch(); }
+    } else {
+        { viscflux_ff_kern<2><<<split_grid(k.g), blk(), 0, s>>>(V, W, Phi6); ia::note_launch(); }
+        { viscacc_ff_kern<2><<<igrd(k.g), blk(), 0, s>>>(k.g, Phi6, r); ia::note_launch(); }
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t k_updateu_ff(const MomConsts& k, double* u, double* rhou, const double* u0, const double* F, double dt,
+                         const double* fref, const double* fupd, double w, bool write_rhou, cudaStream_t s) {
+    const double a = 1.0 / w - 1.0;
+    const MomFF q = mom_ff_consts(k);
+    const ff dtf = ff_split(dt), wf = ff_split(w), af = ff_split(a), dtw = ff_split(dt * w);
+    if (a == 0.0) { updateu_ff_kern<true><<<igrd(k.g), blk(), 0, s>>>(k, q, u, rhou, u0, F, dtf, wf, af, dtw, fref, fupd, write_rhou); ia::note_launch(); }
+    else { updateu_ff_kern<false><<<igrd(k.g), blk(), 0, s>>>(k, q, u, rhou, u0, F, dtf, wf, af, dtw, fref, fupd, write_rhou); ia::note_launch(); }
+    return cudaGetLastError();
+}
+
+}  // namespace ia

@@ -17,15 +17,19 @@
 //    contents: the status block and list counters are cleared at the start of
 //    each call; calls whose GPU work overlaps (other streams, other host
 //    threads) race on the array and must be serialised by the caller;
-//  * the first call on a device looks up the array's device address with
-//    cudaGetSymbolAddress (with that device current) and caches it; make that
-//    first call before any stream capture on the device.
+//  * the array is per device: `stream` must belong to the current device
+//    (checked; IA_ERR_INVALID otherwise).  The first call on a device looks up
+//    the array's device address with cudaGetSymbolAddress (that device
+//    current) and caches it;
+//  * the call ends with a status read-back and a synchronisation of `stream`
+//    (like ia_advect_vof), so it cannot be made inside a stream capture.
 #include <cuda_runtime.h>
 
 #include <cmath>
 #include <cstring>
 
 #include "../../include/intfadv.h"
+#include "capi_internal.cuh"
 #include "ia_core.cuh"
 #include "vof.cuh"
 
@@ -73,6 +77,7 @@ extern "C" int ia_advect_vof_noalloc(const ia_config* cfg, void* stream, double*
                                      ia_status* status) {
     if (!cfg || !f || !u1 || !u2 || !cbar) return IA_ERR_INVALID;
     if (cfg->D != 2 && cfg->D != 3) return IA_ERR_UNSUPPORTED;
+    if (cfg->exitBC) return IA_ERR_UNSUPPORTED;   // as ia_create
     if (cfg->normal_scheme < 0 || cfg->normal_scheme > IA_NORMAL_XYLIC) return IA_ERR_INVALID;
     for (int d = 0; d < cfg->D; ++d)
         if (cfg->N[d] < 2) return IA_ERR_INVALID;
@@ -88,8 +93,12 @@ extern "C" int ia_advect_vof_noalloc(const ia_config* cfg, void* stream, double*
     double* flux = reinterpret_cast<double*>(b + kStatusBytes + 2 * kListBytes);
     double* vals = reinterpret_cast<double*>(b + kStatusBytes + 2 * kListBytes + kFluxBytes);
     cudaStream_t st = static_cast<cudaStream_t>(stream);
-    int sms = 152, dev = 0;
-    if (cudaGetDevice(&dev) == cudaSuccess) cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    int sms = 152, dev = 0, sdev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return IA_ERR_NO_DEVICE;
+    // the scratch address above is the current device's: a stream of another device would run
+    // the kernels against that device's copy of nothing this call prepared
+    if (cudaStreamGetDevice(st, &sdev) != cudaSuccess || sdev != dev) return IA_ERR_INVALID;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     const int list_blocks = sms * 8;
 
     noalloc_reset_k<<<1, 1, 0, st>>>(dst);
@@ -134,38 +143,7 @@ extern "C" int ia_advect_vof_noalloc(const ia_config* cfg, void* stream, double*
     if (cudaStreamSynchronize(st) != cudaSuccess) return IA_ERR_CUDA;
     ia_status s;
     std::memset(&s, 0, sizeof(s));
-    s.flags = hs.flags & (IA_FLAG_NAN | IA_FLAG_OVERFILL | IA_FLAG_UNDERFILL);
-    auto divergence_at = [&](long long I, double& dsum) -> bool {
-        double acc[2] = {0.0, 0.0};
-        const double* us[2] = {u1, u2};
-        for (int q = 0; q < 2; ++q)
-            for (int d = 0; d < g.D; ++d) {
-                double hi = 0.0, lo = 0.0;
-                if (cudaMemcpy(&hi, us[q] + d * g.N + I + g.s[d], 8, cudaMemcpyDeviceToHost) != cudaSuccess) return false;
-                if (cudaMemcpy(&lo, us[q] + d * g.N + I, 8, cudaMemcpyDeviceToHost) != cudaSuccess) return false;
-                acc[q] += hi - lo;
-            }
-        dsum = std::fabs(acc[0]) + std::fabs(acc[1]);
-        return true;
-    };
-    double dv = 0.0;
-    if (hs.flags & IA_FLAG_OVERFILL) {
-        s.maxf = ia::ord_dec(hs.max_enc);
-        s.maxid = (long long)(hs.max_key & 0xFFFFFFFFull);
-        s.fill_dir = int(hs.dir);
-        if (divergence_at(s.maxid, dv) && (dv > 10.0 || dv != dv)) s.flags |= IA_FLAG_DIVERGENCE;
-    }
-    if (hs.flags & IA_FLAG_UNDERFILL) {
-        s.minf = ia::ord_dec(hs.min_enc);
-        s.minid = (long long)(hs.min_key & 0xFFFFFFFFull);
-        s.fill_dir = int(hs.dir);
-        if (divergence_at(s.minid, dv) && (dv > 10.0 || dv != dv)) s.flags |= IA_FLAG_DIVERGENCE;
-    }
-    int code = IA_OK;
-    if (s.flags & IA_FLAG_NAN) code = IA_ERR_NAN;
-    else if (s.flags & IA_FLAG_DIVERGENCE) code = IA_ERR_DIVERGENCE;
-    else if (s.flags & (IA_FLAG_OVERFILL | IA_FLAG_UNDERFILL)) code = IA_WARN_FILL;
-    s.code = code;
+    const int code = ia::translate_fill_status(g, hs, u1, u2, s);
     if (status) *status = s;
     return code;
 }

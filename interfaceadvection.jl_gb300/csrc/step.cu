@@ -42,6 +42,13 @@ static MomConsts consts(ia_handle* h) {
     return k;
 }
 
+// float-float momentum arithmetic: chosen with ia_momentum_arith, else by the Poisson mode (the plain
+// FP64 mode keeps FP64 kernels throughout)
+static bool use_ff(const ia_handle* h) {
+    if (h->mom_arith >= 0) return h->mom_arith == IA_ARITH_FF;
+    return h->cfg.poisson_mode != IA_POISSON_FP64;
+}
+
 int extra_create(ia_handle*) { return IA_OK; }   // momentum / MG scratch is allocated on first use
 
 static int ensure_scratch(ia_handle* h) {
@@ -103,18 +110,25 @@ static int advect_fq(ia_handle* h, double* f, const double* u1, const double* u2
         const int d = dirs[q];
         double* fin = seq[q];
         double* fout = seq[q + 1];
+        const bool ff = use_ff(h);
+        float2* us2 = reinterpret_cast<float2*>(m->ustar);
+        float2* Phi2 = reinterpret_cast<float2*>(m->Phi);
         int tk = timing_begin(h, TK_MOM);
-        if (k_ustar(k, h->fld.rhou, fin, m->ustar, st) != cudaSuccess) return IA_ERR_CUDA;
+        cudaError_t e = ff ? k_ustar_ff(k, h->fld.rhou, fin, us2, st) : k_ustar(k, h->fld.rhou, fin, m->ustar, st);
+        if (e != cudaSuccess) return IA_ERR_CUDA;
         timing_end(h, tk);
         int rc = vof_sweep(h, fin, fout, u1, u2, dt, d, q == 0, cbar, h->fld.rhouf, 10.0 * tol, counter_base + q);
         if (rc != IA_OK) return rc;
+        const double* rj = h->fld.rhouf + (long long)d * g.N;
         tk = timing_begin(h, TK_MOM_FLUX);
-        if (k_momflux(k, d, h->cfg.limiter, m->ustar, h->fld.rhouf + (long long)d * g.N, fin, dt, m->Phi, st) !=
-            cudaSuccess)
-            return IA_ERR_CUDA;
+        e = ff ? k_momflux_ff(k, d, h->cfg.limiter, us2, rj, fin, dt, Phi2, st)
+               : k_momflux(k, d, h->cfg.limiter, m->ustar, rj, fin, dt, m->Phi, st);
+        if (e != cudaSuccess) return IA_ERR_CUDA;
         timing_end(h, tk);
         tk = timing_begin(h, TK_MOM_UPDATE);
-        if (k_momupdate(k, d, m->Phi, uOld, u1, u2, cbar, dt, h->fld.rhou, st) != cudaSuccess) return IA_ERR_CUDA;
+        e = ff ? k_momupdate_ff(k, d, Phi2, uOld, u1, u2, cbar, dt, h->fld.rhou, st)
+               : k_momupdate(k, d, m->Phi, uOld, u1, u2, cbar, dt, h->fld.rhou, st);
+        if (e != cudaSuccess) return IA_ERR_CUDA;
         timing_end(h, tk);
     }
     return IA_OK;
@@ -128,10 +142,15 @@ static int visc_surften(ia_handle* h, const double* f) {
     cudaStream_t st = h->stream;
     int tk = timing_begin(h, TK_FORCE);
     cudaError_t e;
-    if (h->cfg.mu != 0.0) e = k_visc(k, h->fld.u, f, h->cfg.lmu, h->cfg.mu, m->Phi6, h->fld.force, st);
+    if (h->cfg.mu != 0.0 && use_ff(h))
+        e = k_visc_ff(k, h->fld.u, f, h->cfg.lmu, h->cfg.mu, reinterpret_cast<float2*>(m->Phi6), h->fld.force, st);
+    else if (h->cfg.mu != 0.0) e = k_visc(k, h->fld.u, f, h->cfg.lmu, h->cfg.mu, m->Phi6, h->fld.force, st);
     else e = k_zero(h->fld.force, g.N * g.D, st);
     if (e != cudaSuccess) return IA_ERR_CUDA;
-    if (h->cfg.eta != 0.0 && k_surften(k, f, h->cfg.eta, m->fb, h->fld.force, m->slist, m->scount, st) != cudaSuccess)
+    // the high x-ghost plane of fᶠ after the last VOF sweep is zero when the x walls' normal velocity is
+    // zero (and never read when x is periodic)
+    if (h->cfg.eta != 0.0 &&
+        k_surften(k, f, nullptr, h->cfg.eta, m->fb, h->fld.force, m->slist, m->scount, st) != cudaSuccess)
         return IA_ERR_CUDA;
     timing_end(h, tk);
     return IA_OK;
@@ -225,7 +244,9 @@ int ia_mom_step(ia_handle* h, double dt, int64_t n_dt, double t_now, ia_status* 
     timing_end(h, tk);
     if ((rc = visc_surften(h, F.f0)) != IA_OK) return rc;
     tk = timing_begin(h, TK_UPDATE);
-    if (k_updateu(k, F.u, F.rhou, F.u0, F.force, dt, F.f, F.f0, 0.5, false, st) != cudaSuccess) return IA_ERR_CUDA;
+    if ((use_ff(h) ? k_updateu_ff(k, F.u, F.rhou, F.u0, F.force, dt, F.f, F.f0, 0.5, false, st)
+                   : k_updateu(k, F.u, F.rhou, F.u0, F.force, dt, F.f, F.f0, 0.5, false, st)) != cudaSuccess)
+        return IA_ERR_CUDA;
     if (k_bc_vel(k, F.u, h->cfg.uBC, st) != cudaSuccess) return IA_ERR_CUDA;
     timing_end(h, tk);
     int it0 = 0;
@@ -252,7 +273,9 @@ int ia_mom_step(ia_handle* h, double dt, int64_t n_dt, double t_now, ia_status* 
     // a = 0 for w = 1, so ρu⁰ only enters as 0·ρu⁰; u⁰ takes u(n+½) first (src/flow.jl:100)
     tk = timing_begin(h, TK_UPDATE);
     cudaMemcpyAsync(F.u0, F.u, 8 * NV, cudaMemcpyDeviceToDevice, st);
-    if (k_updateu(k, F.u, F.rhou, F.u0, F.force, dt, F.f, F.f, 1.0, true, st) != cudaSuccess) return IA_ERR_CUDA;
+    if ((use_ff(h) ? k_updateu_ff(k, F.u, F.rhou, F.u0, F.force, dt, F.f, F.f, 1.0, true, st)
+                   : k_updateu(k, F.u, F.rhou, F.u0, F.force, dt, F.f, F.f, 1.0, true, st)) != cudaSuccess)
+        return IA_ERR_CUDA;
     if (k_bc_vel(k, F.u, h->cfg.uBC, st) != cudaSuccess) return IA_ERR_CUDA;
     timing_end(h, tk);
     int it1 = 0;
@@ -368,6 +391,20 @@ int ia_advect_momentum(ia_handle* h, double* f, const double* u1, const double* 
     if (rc == IA_OK) rc = advect_fq(h, f, u1, u2, uOld, dt, dirs, 0);
     if (rc != IA_OK) return rc;
     return status_collect(h, u1, u2, status, false);
+}
+
+int ia_surften(ia_handle* h, double* forcing, const double* f, const double* fbuffer, double eta) {
+    if (!h || !forcing || !f) return IA_ERR_INVALID;
+    if (eta == 0.0) return IA_OK;   // surfTen!(…, η::Nothing) = nothing (src/surfaceTension.jl:7)
+    if (ensure_scratch(h) != IA_OK) return IA_ERR_CUDA;
+    MomScratch* m = h->mom;
+    return cuda_fail(k_surften(consts(h), f, fbuffer, eta, m->fb, forcing, m->slist, m->scount, h->stream));
+}
+
+int ia_momentum_arith(ia_handle* h, int32_t kind) {
+    if (!h || kind < -1 || kind > IA_ARITH_FF) return IA_ERR_INVALID;
+    h->mom_arith = kind;
+    return IA_OK;
 }
 
 int ia_visc_surften(ia_handle* h, const double* f) {

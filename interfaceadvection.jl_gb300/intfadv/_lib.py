@@ -32,6 +32,7 @@ LIMITERS = {"Koren": 0, "upwind": 1, "minmod": 2, "vanAlbada1": 3, "Sweby": 4, "
 POISSON_MODES = {"fp64": 0, "mixed": 1, "learned": 2}
 PRECONDS = {"hybrid": 0, "net": 1, "none": 2, "vcycle": 3}
 SMOOTHERS = {"halfsweep": 0, "blocked": 1}
+ARITH = {"default": -1, "fp64": 0, "ff": 1}
 TIMED_KERNELS = ["vof_bulk", "vof_cells", "ustar", "forcing", "mg_vcycle", "mg_residual", "mg_transfer",
                  "krylov", "other", "vof_faces", "momflux", "momupdate", "update_project", "mg_fine_rbgs", "nn_precond",
                  "mg_fine_first"]
@@ -79,6 +80,9 @@ _SIGS = {
     "ia_project": (C.c_int, [C.c_void_p, C.c_void_p, C.c_double, C.POINTER(C.c_int32), C.POINTER(C.c_double)]),
     "ia_advect_momentum": (C.c_int, [C.c_void_p] * 5 + [C.c_double, C.c_int64, C.POINTER(Status)]),
     "ia_visc_surften": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "ia_surften": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_double]),
+    "ia_momentum_arith": (C.c_int, [C.c_void_p, C.c_int32]),
+    "ia_probe_fma_rates": (C.c_int, [C.POINTER(C.c_double), C.POINTER(C.c_double)]),
     "ia_advect_vof_noalloc": (C.c_int, [C.POINTER(Config), C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                         C.c_double, C.c_int64, C.c_void_p, C.c_void_p, C.POINTER(Status)]),
     "ia_nn_param_count": (C.c_int64, []),

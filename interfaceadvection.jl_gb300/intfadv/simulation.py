@@ -33,13 +33,15 @@ class TwoPhaseSimulation:
     ``poisson="learned"`` (3D, dims multiples of 4) preconditions the inner FCG of the mixed
     solver with the conv net: ``precond`` is "hybrid" (net then V-cycle), "net", "none" or
     "vcycle"; ``nn_weights`` a parameter vector or a weights file (default: the trained
-    weights shipped with the package).
+    weights shipped with the package).  ``momentum_arith`` selects the arithmetic of the
+    momentum kernels: "fp64", "ff" (FP32 pairs) or "default" (pairs with the mixed and learned
+    solvers, FP64 with the FP64 solver).
     """
 
     def __init__(self, dims, u_BC, L, *, U=None, Δt=0.25, ν=0.0, g=None, u0=None, perdir=(), exitBC=False,
                  λμ=1e-2, λρ=1e-3, η=None, InterfaceSDF=None, λ="Koren", normalScheme="WH", T=FP64,
                  poisson="fp64", poisson_tol=1e-4, poisson_itmx=200, device="cuda", body=None, ϵ=1,
-                 precond="hybrid", nn_weights=None, inner_max=30, inner_rtol=1e-4):
+                 precond="hybrid", nn_weights=None, inner_max=30, inner_rtol=1e-4, momentum_arith="default"):
         if T != FP64:
             raise NotImplementedError("the GB300 path computes in FP64 (Poisson V-cycles optionally FP32)")
         if exitBC:
@@ -64,6 +66,7 @@ class TwoPhaseSimulation:
         self.handle.bind(u=fl.u, u0=fl.u0, force=fl.f, sigma=fl.sigma, p=fl.p, mu0=fl.mu0, f=it.f, f0=it.f0,
                          alpha=it.alpha, nhat=it.nhat, fF=it.fF, rhou=it.rhou, rhouf=it.rhouf, drho=it.drho,
                          cbar=it.cbar)
+        set_momentum_arith(self.handle, momentum_arith)
         if poisson == "learned":
             set_learned(self.handle, precond=precond, weights=nn_weights, inner_max=inner_max, inner_rtol=inner_rtol)
         _lib.check(self.handle.call("ia_bc_velocity", ptr(fl.u)), "ia_bc_velocity")   # Flow: BC!(u)
@@ -101,6 +104,11 @@ def set_learned(handle, precond="hybrid", weights=None, inner_max=30, inner_rtol
                            int(inner_max), float(inner_rtol)), "ia_poisson_precond")
 
 
+def set_momentum_arith(handle, kind: str = "default") -> None:
+    """Arithmetic of the momentum kernels: "fp64", "ff" (FP32 pairs) or "default" (ia_momentum_arith)."""
+    _lib.check(handle.call("ia_momentum_arith", C.c_int32(_lib.ARITH[kind])), "ia_momentum_arith")
+
+
 def set_smoother(handle, kind: str = "halfsweep", omega: float | None = None) -> None:
     """Smoother of the FP32 V-cycle: "halfsweep" (one launch per red-black half-sweep, the default)
     or "blocked" (all half-sweeps of a smoothing in one z-wavefront launch, relaxation factor 1 only);
@@ -122,6 +130,20 @@ def MPCFL(sim) -> float:
     out = C.c_double()
     _lib.check(sim.handle.call("ia_cfl", C.byref(out)), "ia_cfl")
     return out.value
+
+
+def surfTen(intf: cVOF, forcing, f=None, fbuffer=None, η=None) -> None:
+    """surfTen!(forcing, f, α, n̂, fbuffer, η; perdir) — src/surfaceTension.jl:8-20.
+
+    Accumulates η κ (−∂(d,I,f)) into the device vector field ``forcing`` for every direction d.
+    ``fbuffer`` (default: the cVOF's fᶠ, which the reference passes) supplies the buffer content the
+    reference reads at its never-written high x ghost; it is not modified.  α and n̂ are not touched.
+    """
+    f = intf.f if f is None else f
+    fbuffer = intf.fF if fbuffer is None else fbuffer
+    eta = intf.eta if η is None else η
+    _lib.check(intf.handle.call("ia_surften", ptr(forcing), ptr(f), ptr(fbuffer), C.c_double(eta or 0.0)),
+               "ia_surften")
 
 
 def MPFMomStep(sim, δt=None) -> _lib.Status:

@@ -10,6 +10,7 @@ length 1 resolved by N cells has h = 1/N, cell centres at loc(0,I) = I - 1.5
   A = (0, -sin²(πx)sin(2πy)sin²(πz)/π, sin²(πx)sin²(πy)sin(2πz)/π) so the
   face velocities are discretely divergence-free to round-off.
 * sphere_sdf — signed distance (grid units) to a sphere, negative inside.
+* bubble_params / swarm_layout — the rising-bubble and bubble-swarm configurations in grid units.
 """
 from __future__ import annotations
 
@@ -79,3 +80,31 @@ def discrete_divergence(u: torch.Tensor) -> torch.Tensor:
         hi = tuple(slice(2, n) if e == d else slice(1, n - 1) for e, n in enumerate(u.shape[:-1]))
         out = out + (u[hi + (d,)] - u[inner + (d,)])
     return out
+
+
+def bubble_params(N: int, Eo: float = 10.0, Mo: float = 1e-3, G: float = 1e-3, D=None):
+    """Rising bubble in grid units at N cells per unit length: Eo = ρ g D²/σ, Mo = g μ⁴/(ρ σ³) with
+    ρ_liquid = 1, gravity G (which sets the time scale), bubble diameter D (default 0.25 N)."""
+    D = 0.25 * N if D is None else D
+    sigma = G * D * D / Eo
+    mu = (Mo * sigma ** 3 / G) ** 0.25
+    return dict(dims=(N, 2 * N, N), centre=(N / 2, N / 2, N / 2), radius=0.125 * N, G=G, sigma=sigma, mu=mu,
+                lrho=1e-3, lmu=1e-2, perdir=(0, 2))
+
+
+def swarm_layout(seed=5, n=64, rmin=0.02, rmax=0.05, N=512, max_tries=200000):
+    """n non-overlapping bubbles with radii uniform in [rmin, rmax] in the unit cube (PCG64 seed), as
+    (centre, radius) in grid units of an N³ grid; rejection-sampled with a 0.01 gap."""
+    import numpy as np
+    rng = np.random.Generator(np.random.PCG64(seed))
+    out = []
+    for _ in range(max_tries):
+        if len(out) == n:
+            break
+        r = rng.uniform(rmin, rmax)
+        c = rng.uniform(r + 0.01, 1 - r - 0.01, size=3)
+        if all(np.linalg.norm(c - c2) > r + r2 + 0.01 for c2, r2 in out):
+            out.append((c, r))
+    if len(out) != n:
+        raise RuntimeError("could not place the bubbles")
+    return [(tuple(float(v) * N for v in c), float(r) * N) for c, r in out]

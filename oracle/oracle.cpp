@@ -898,7 +898,7 @@ double dot_inside(const G& g, const double* a, const double* b) {
             }
     return acc;
 }
-void poisson(const G& g, orc_state* s) {
+void poisson_jacobi_pcg(const G& g, orc_state* s) {
     double *x = s->p, *r = s->pr, *e = s->peps, *z = s->pz, *L = s->mu0;
     std::vector<double> q(g.N, 0.0);
     set_diag(g, s);
@@ -927,6 +927,232 @@ void poisson(const G& g, orc_state* s) {
     perbc(g, x);
     s->piters = it;
     s->presid = res;
+}
+/* ---- Multigrid-preconditioned flexible CG: the solver the reference's default call site uses,
+ * inproject!(…, ::MultiLevelPoisson) → WaterLily solver! (flow.jl:343-347).  WaterLily's source is not
+ * available, so this is a geometric multigrid restated from the mathematics of the operator above, not
+ * from WaterLily's code: cell-centred levels (2x coarsening while every interior extent is even and
+ * >= 4), coarse face coefficient = ½ Σ of the 2^(D-1) fine faces it covers, restriction by the sum of
+ * the 2^D children, prolongation by injection, symmetric red-black Gauss-Seidel (nu1 red→black sweeps
+ * before, nu2 black→red after), the coarsest level swept from zero on its mean-free right-hand side.
+ * The V-cycle preconditions a Polak–Ribière flexible CG that stops on the L∞ norm of the true residual
+ * (the same test as the Jacobi-PCG above).  Only the converged pressure is compared (up to its free
+ * constant), so the solver's internals need not match the product's. */
+struct MGLevel {
+    orc_grid og;
+    G g;
+    std::vector<double> Lown, Dg, x, b, r;
+    const double* L = nullptr;
+    explicit MGLevel(const orc_grid& o) : og(o), g(&og) {}
+};
+struct MGCache {
+    long key[4] = {0, 0, 0, 0};
+    std::vector<MGLevel> lv;
+    std::vector<double> r, rold, sv, p, q;
+};
+static MGCache g_mg;
+
+// neighbour offsets of interior cell I (coords c) along i, periodic ends wrapped
+inline void nbr(const G& g, int i, long I, const long c[3], long& lo, long& hi) {
+    lo = I - g.s[i];
+    hi = I + g.s[i];
+    if (g.isper(i)) {
+        if (c[i] == 1) lo = I + (g.n[i] - 3) * g.s[i];
+        if (c[i] == g.n[i] - 2) hi = I - (g.n[i] - 3) * g.s[i];
+    }
+}
+inline double mg_off(const MGLevel& l, long I, const long c[3], const double* x) {
+    const G& g = l.g;
+    double a = 0;
+    for (int i = 0; i < g.D; ++i) {
+        long lo, hi;
+        nbr(g, i, I, c, lo, hi);
+        a += l.L[I + i * g.N] * x[lo] + l.L[I + g.s[i] + i * g.N] * x[hi];
+    }
+    return a;
+}
+void mg_rbgs(MGLevel& l, int color) {
+    const G& g = l.g;
+    inside(g, [&](long I, const long* c) {
+        if (((c[0] + c[1] + c[2]) & 1) != color) return;
+        if (l.Dg[I] == 0) return;
+        l.x[I] = (l.b[I] - mg_off(l, I, c, l.x.data())) / l.Dg[I];
+    });
+}
+void mg_build(const G& gf, const double* Lf) {
+    const long key[4] = {gf.D, gf.per, gf.n[0] * 100003 + gf.n[1], gf.n[2]};
+    bool same = g_mg.lv.size() && std::equal(key, key + 4, g_mg.key);
+    if (!same) {
+        g_mg.lv.clear();
+        std::copy(key, key + 4, g_mg.key);
+        orc_grid o{gf.D, gf.per, {gf.n[0], gf.n[1], gf.D == 3 ? gf.n[2] : 1}};
+        g_mg.lv.reserve(32);
+        g_mg.lv.emplace_back(o);
+        while (true) {
+            const orc_grid& c = g_mg.lv.back().og;
+            bool ok = true;
+            for (int d = 0; d < c.D; ++d) {
+                long ni = c.n[d] - 2;
+                if (ni % 2 != 0 || ni < 4) ok = false;
+            }
+            if (!ok) break;
+            orc_grid o2{c.D, c.per, {(c.n[0] - 2) / 2 + 2, (c.n[1] - 2) / 2 + 2, c.D == 3 ? (c.n[2] - 2) / 2 + 2 : 1}};
+            g_mg.lv.emplace_back(o2);
+        }
+        for (size_t k = 0; k < g_mg.lv.size(); ++k) {
+            MGLevel& l = g_mg.lv[k];
+            const long N = l.g.N;
+            if (k > 0) l.Lown.assign(N * l.g.D, 0.0);
+            l.Dg.assign(N, 0.0);
+            l.x.assign(N, 0.0);
+            l.b.assign(N, 0.0);
+            l.r.assign(N, 0.0);
+        }
+        for (auto* v : {&g_mg.r, &g_mg.rold, &g_mg.sv, &g_mg.p, &g_mg.q}) v->assign(gf.N, 0.0);
+    }
+    g_mg.lv[0].L = Lf;
+    for (size_t k = 1; k < g_mg.lv.size(); ++k) {
+        MGLevel& l = g_mg.lv[k];
+        const MGLevel& f = g_mg.lv[k - 1];
+        const G& gc = l.g;
+        const G& gg = f.g;
+        double* Lc = l.Lown.data();
+        for (int i = 0; i < gc.D; ++i) {
+            // every coarse face 1..n-1 along i, interior elsewhere
+            long lo[3] = {1, 1, 1}, hi[3] = {gc.n[0] - 2, gc.n[1] - 2, gc.n[2] - 2};
+            hi[i] = gc.n[i] - 1;
+            box(gc, lo, hi, [&](long Ic, const long* c) {
+                long fb[3] = {2 * c[0] - 1, 2 * c[1] - 1, gc.D == 3 ? 2 * c[2] - 1 : 0};
+                double acc = 0;
+                const int o1 = i == 0 ? 1 : 0, o2 = i == 2 ? 1 : 2;
+                for (int a = 0; a < 2; ++a)
+                    for (int b2 = 0; b2 < (gc.D == 3 ? 2 : 1); ++b2) {
+                        long ff[3] = {fb[0], fb[1], fb[2]};
+                        ff[o1] += a;
+                        if (gc.D == 3) ff[o2] += b2;
+                        acc += f.L[gg.lin(ff) + i * gg.N];
+                    }
+                Lc[Ic + i * gc.N] = 0.5 * acc;
+            });
+        }
+        l.L = Lc;
+    }
+    for (auto& l : g_mg.lv) {
+        const G& g = l.g;
+        inside(g, [&](long I, const long*) {
+            double dd = 0;
+            for (int i = 0; i < g.D; ++i) dd -= l.L[I + i * g.N] + l.L[I + g.s[i] + i * g.N];
+            l.Dg[I] = dd;
+        });
+    }
+}
+void mg_vcycle(size_t k, int nu1, int nu2, int nuc) {
+    MGLevel& l = g_mg.lv[k];
+    const G& g = l.g;
+    std::fill(l.x.begin(), l.x.end(), 0.0);
+    if (k + 1 == g_mg.lv.size()) {
+        double m = 0;
+        long cnt = 0;
+        for (long I = 0; I < g.N; ++I) {
+            long c[3];
+            g.coords(I, c);
+            bool in = true;
+            for (int e = 0; e < g.D; ++e) if (c[e] < 1 || c[e] > g.n[e] - 2) in = false;
+            if (in) { m += l.b[I]; ++cnt; }
+        }
+        m /= double(cnt);
+        inside(g, [&](long I, const long*) { l.b[I] -= m; });
+        for (int it = 0; it < nuc; ++it) {
+            mg_rbgs(l, 0); mg_rbgs(l, 1);
+            mg_rbgs(l, 1); mg_rbgs(l, 0);
+        }
+        return;
+    }
+    for (int it = 0; it < nu1; ++it) { mg_rbgs(l, 0); mg_rbgs(l, 1); }
+    inside(g, [&](long I, const long* c) { l.r[I] = l.b[I] - (l.Dg[I] * l.x[I] + mg_off(l, I, c, l.x.data())); });
+    MGLevel& cl = g_mg.lv[k + 1];
+    const G& gc = cl.g;
+    const int nz = gc.D == 3 ? 2 : 1;
+    inside(gc, [&](long Ic, const long* c) {
+        long fb[3] = {2 * c[0] - 1, 2 * c[1] - 1, gc.D == 3 ? 2 * c[2] - 1 : 0};
+        double acc = 0;
+        for (int dz = 0; dz < nz; ++dz)
+            for (int dy = 0; dy < 2; ++dy)
+                for (int dx = 0; dx < 2; ++dx) acc += l.r[g.lin(fb) + dx + dy * g.s[1] + dz * g.s[2]];
+        cl.b[Ic] = acc;
+    });
+    mg_vcycle(k + 1, nu1, nu2, nuc);
+    inside(g, [&](long I, const long* c) {
+        long cc[3] = {(c[0] + 1) / 2, (c[1] + 1) / 2, g.D == 3 ? (c[2] + 1) / 2 : 0};
+        l.x[I] += cl.x[gc.lin(cc)];
+    });
+    for (int it = 0; it < nu2; ++it) { mg_rbgs(l, 1); mg_rbgs(l, 0); }
+}
+void poisson_mg_fcg(const G& g, orc_state* s) {
+    double *x = s->p, *L = s->mu0;
+    set_diag(g, s);
+    mg_build(g, L);
+    std::vector<double>& r = g_mg.r;
+    std::vector<double>& rold = g_mg.rold;
+    std::vector<double>& sv = g_mg.sv;
+    std::vector<double>& p = g_mg.p;
+    std::vector<double>& q = g_mg.q;
+    MGLevel& l0 = g_mg.lv[0];
+    const int nu1 = 2, nu2 = 2;
+    long coarse = 1;
+    for (int e = 0; e < g.D; ++e) coarse *= g_mg.lv.back().g.n[e] - 2;
+    const int nuc = int(std::min<long>(4000, std::max<long>(16, 4 * coarse)));
+    auto true_resid = [&]() {
+        perbc(g, x);
+        inside(g, [&](long I, const long*) { r[I] = s->sigma[I] - mult(g, I, L, s->pD, x); });
+        return linf_inside(g, r.data());
+    };
+    double res = true_resid();
+    int it = 0;
+    double sr_old = 0;
+    while (res > s->ptol && it < s->pitmx) {
+        std::copy(r.begin(), r.end(), l0.b.begin());
+        mg_vcycle(0, nu1, nu2, nuc);
+        std::copy(l0.x.begin(), l0.x.end(), sv.begin());
+        const double sr = dot_inside(g, sv.data(), r.data());
+        if (it == 0) {
+            inside(g, [&](long I, const long*) { p[I] = sv[I]; });
+        } else {
+            double num = 0;
+            {
+                long lo[3] = {1, 1, 1}, hi[3] = {g.n[0] - 2, g.n[1] - 2, g.n[2] - 2};
+                if (g.D == 2) lo[2] = hi[2] = 0;
+#pragma omp parallel for collapse(2) reduction(+ : num)
+                for (long kk = lo[2]; kk <= hi[2]; ++kk)
+                    for (long j = lo[1]; j <= hi[1]; ++j)
+                        for (long i = lo[0]; i <= hi[0]; ++i) {
+                            long I = i + g.s[1] * j + g.s[2] * kk;
+                            num += sv[I] * (r[I] - rold[I]);
+                        }
+            }
+            const double beta = num / sr_old;
+            inside(g, [&](long I, const long*) { p[I] = sv[I] + beta * p[I]; });
+        }
+        perbc(g, p.data());
+        inside(g, [&](long I, const long*) { q[I] = mult(g, I, L, s->pD, p.data()); });
+        const double alpha = sr / dot_inside(g, p.data(), q.data());
+        std::copy(r.begin(), r.end(), rold.begin());
+        inside(g, [&](long I, const long*) {
+            x[I] += alpha * p[I];
+            r[I] -= alpha * q[I];
+        });
+        sr_old = sr;
+        ++it;
+        res = linf_inside(g, r.data());
+        if (res <= s->ptol) res = true_resid();
+    }
+    perbc(g, x);
+    s->piters = it;
+    s->presid = res;
+}
+void poisson(const G& g, orc_state* s) {
+    if (s->psolver == ORC_POISSON_MG) poisson_mg_fcg(g, s);
+    else poisson_jacobi_pcg(g, s);
 }
 // myproject! / inproject!, flow.jl:328-347 (source z = σ, x = p, L = μ₀)
 void project(const G& g, orc_state* s, double w, double dt_last) {
@@ -1090,6 +1316,9 @@ void orc_advect_vof(const orc_grid* gg, int scheme, double* f, double* fF, doubl
         advect_vof_1d(g, scheme, f, fF, alpha, nhat, u, u0, dt, cbar, rhouf, lrho, dirO[k], tol, tol, st);
 }
 
+void orc_surften(const orc_grid* gg, double* forcing, const double* f, double* nhat, double* fbuffer, double eta) {
+    surften(G(gg), forcing, f, nhat, fbuffer, eta);
+}
 double orc_popinet_height(const orc_grid* gg, const double* f, int64_t I, int i_signed) {
     return popinet_height(G(gg), f, I, i_signed);
 }

@@ -86,6 +86,11 @@ void   orc_advect_vof(const orc_grid* g, int scheme, double* f, double* fF, doub
 /* ---- surface tension (src/surfaceTension.jl) ----------------------------- */
 double orc_popinet_height(const orc_grid* g, const double* f, int64_t I, int i_signed);
 double orc_curvature(const orc_grid* g, const double* f, int64_t I, int i_signed);
+/* surfTen!(forcing, f, α, n̂, fbuffer, η) (src/surfaceTension.jl:8-20): fbuffer is the caller's
+ * buffer, reused for every d exactly as the reference does (its high ghost along a wall d keeps the
+ * previous content); n̂ receives the WY normals. */
+void   orc_surften(const orc_grid* g, double* forcing, const double* f, double* nhat, double* fbuffer,
+                   double eta);
 
 /* ---- full two-phase step (src/flow.jl) ----------------------------------- */
 typedef struct {
@@ -111,7 +116,11 @@ typedef struct {
     int32_t pitmx;
     int32_t piters;     /* out: PCG iterations of the last solve */
     double presid;      /* out: final L-infinity residual */
+    int32_t psolver;    /* ORC_POISSON_JACOBI (psolver!, flow.jl:300-326) or ORC_POISSON_MG
+                           (multigrid-preconditioned CG in the role of MultiLevelPoisson, :343-347) */
+    int32_t pad2;
 } orc_state;
+enum { ORC_POISSON_JACOBI = 0, ORC_POISSON_MG = 1 };
 
 void   orc_mom_step(const orc_grid* g, orc_state* s, double dt, double t_now,
                     int64_t n_dt, orc_fill_status* st);

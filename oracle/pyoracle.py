@@ -57,7 +57,7 @@ class State(C.Structure):
         ("lrho", C.c_double), ("lmu", C.c_double), ("mu", C.c_double), ("eta", C.c_double), ("nu", C.c_double),
         ("g", C.c_double * 3), ("has_g", C.c_int32), ("scheme", C.c_int32), ("limiter", C.c_int32),
         ("pad", C.c_int32), ("uBC", C.c_double * 3), ("ptol", C.c_double), ("pitmx", C.c_int32),
-        ("piters", C.c_int32), ("presid", C.c_double)]
+        ("piters", C.c_int32), ("presid", C.c_double), ("psolver", C.c_int32), ("pad2", C.c_int32)]
 
 
 _lib = None
@@ -86,6 +86,7 @@ def lib():
             "orc_vof_flux": (None, [p, p, p, p, p, p, p, d, i, p, d]),
             "orc_advect_vof": (None, [p, i, p, p, p, p, p, p, d, p, p, d, p, p]),
             "orc_popinet_height": (d, [p, p, i64, i]), "orc_curvature": (d, [p, p, i64, i]),
+            "orc_surften": (None, [p, p, p, p, p, d]),
             "orc_mom_step": (None, [p, p, d, d, i64, p]), "orc_mpcfl": (d, [p, p, d]),
             "orc_poisson": (None, [p, p]),
             "orc_argabsmax": (i, [i, p]), "orc_get_xdir": (i, [i]), "orc_get_xydir": (None, [i, p, p]),

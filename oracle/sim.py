@@ -37,7 +37,7 @@ class OracleSim:
     """Fields of Flow + cVOF in host memory, stepped by the oracle."""
 
     def __init__(self, N, uBC, *, sdf=None, u0=None, Δt=0.25, ν=0.0, g=None, perdir=(), lrho=1e-3, lmu=1e-2,
-                 eta=None, scheme="WH", limiter="Koren", ptol=1e-12, pitmx=5000, mu=None):
+                 eta=None, scheme="WH", limiter="Koren", ptol=1e-12, pitmx=5000, mu=None, psolver="jacobi"):
         self.N = tuple(N)
         self.D = len(N)
         self.ng = tuple(n + 2 for n in N)
@@ -91,6 +91,9 @@ class OracleSim:
         for i in range(D):
             s.uBC[i] = float(uBC[i])
         s.ptol, s.pitmx = ptol, pitmx
+        # "jacobi": the reference's psolver! (src/flow.jl:300-326); "mg": multigrid-preconditioned CG in
+        # the role of WaterLily's MultiLevelPoisson, the reference's default (src/flow.jl:343-347)
+        s.psolver = {"jacobi": 0, "mg": 1}[psolver]
         self.s = s
         self.Δt = [float(Δt)]
         self.Δt[-1] = min(self.Δt[-1], self.mpcfl())      # src/InterfaceAdvection.jl:81

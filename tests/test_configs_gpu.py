@@ -8,7 +8,7 @@ import pytest
 import torch
 
 import intfadv as ia
-from intfadv import learned
+from intfadv import learned, workloads
 from oracle.sim import OracleSim
 
 pytestmark = pytest.mark.gpu
@@ -19,25 +19,36 @@ def npf(t):
     return np.asfortranarray(t.detach().cpu().numpy())
 
 
-def test_c1_dam_break_128x64_matches_oracle(cuda):
+@pytest.mark.parametrize("poisson", ["fp64", "mixed"])
+def test_c1_dam_break_128x64_200_steps_matches_oracle(cuda, poisson):
     # 128x64, walls everywhere, water column x < 0.25 Lx, y < 0.5 Ly; L = 64 cells, U = 1 so
-    # g = U²/L = 1/64 in grid units, ν = U L / Re with Re = 1000; λρ = 1e-3, λμ = 1/55
+    # g = U²/L = 1/64 in grid units, ν = U L / Re with Re = 1000; λρ = 1e-3, λμ = 1/55; all 200 steps.
+    # Both sides solve the pressure to an L∞ residual of 1e-13: two different solvers at 1e-12 differ
+    # by up to 1.7e-10 of max|u| in the first steps, where the column starts from rest and max|u| is
+    # of order g·Δt; at 1e-13 they stay below 1e-11 (measured with the oracle's two solvers).
+    # f is compared absolutely, u relative to max|u|, after every step, at 1e-10.
+    tol = 1e-13
     Nx, Ny = 128, 64
     a, b = 0.25 * Nx, 0.5 * Ny
     g = (0.0, -1.0 / 64)
     nu = 64 / 1000
     sim = ia.TwoPhaseSimulation((Nx, Ny), (0.0, 0.0), float(Ny), InterfaceSDF=lambda x: torch.maximum(x[0] - a, x[1] - b),
-                                λμ=1 / 55, λρ=1e-3, ν=nu, g=g, poisson="mixed", poisson_tol=PTOL, poisson_itmx=1000)
+                                λμ=1 / 55, λρ=1e-3, ν=nu, g=g, poisson=poisson, poisson_tol=tol, poisson_itmx=1000)
     orc = OracleSim((Nx, Ny), (0.0, 0.0), sdf=lambda x: np.maximum(x[0] - a, x[1] - b), lrho=1e-3, lmu=1 / 55, ν=nu,
-                    g=g, ptol=PTOL, pitmx=200000)
+                    g=g, ptol=tol, pitmx=200000, psolver="mg")
     m0 = sim.intf.mass()
-    for _ in range(30):
+    worst = (0.0, 0.0, 0)
+    for step in range(1, 201):
         st = ia.sim_step(sim)
         orc.step()
-        assert st.poisson_resid[1] <= PTOL
-    ef = float(np.abs(npf(sim.intf.f) - orc.f).max())
-    eu = float(np.abs(npf(sim.flow.u) - orc.u).max()) / float(np.abs(orc.u).max())
-    assert ef < 1e-9 and eu < 1e-9, (ef, eu)
+        assert st.code == 0 and st.poisson_resid[0] <= tol and st.poisson_resid[1] <= tol
+        assert sim.flow.Δt[-1] == pytest.approx(orc.Δt[-1], rel=1e-12)
+        ef = float(np.abs(npf(sim.intf.f) - orc.f).max())
+        eu = float(np.abs(npf(sim.flow.u) - orc.u).max()) / float(np.abs(orc.u).max())
+        if max(ef, eu) > max(worst[:2]):
+            worst = (ef, eu, step)
+        assert ef < 1e-10 and eu < 1e-10, (step, ef, eu)
+    print(f"C1 {poisson}: worst |Δf| {worst[0]:.2e}, |Δu|/max|u| {worst[1]:.2e} at step {worst[2]}")
     assert abs(sim.intf.mass() - m0) <= 1e-12 * m0
 
 
@@ -69,22 +80,8 @@ def test_c3_rising_bubble_256x512x256_properties(cuda):
     check_properties(sim, 2, 1e-12)
 
 
-def swarm_layout(seed=5, n=64, rmin=0.02, rmax=0.05, N=512, max_tries=200000):
-    rng = np.random.Generator(np.random.PCG64(seed))
-    out = []
-    for _ in range(max_tries):
-        if len(out) == n:
-            break
-        r = rng.uniform(rmin, rmax)
-        c = rng.uniform(r + 0.01, 1 - r - 0.01, size=3)
-        if all(np.linalg.norm(c - c2) > r + r2 + 0.01 for c2, r2 in out):
-            out.append((c, r))
-    assert len(out) == n
-    return [(tuple(float(v) * N for v in c), float(r) * N) for c, r in out]
-
-
 def test_c5_swarm_512_properties(cuda):
     # 512³ unit cube, 64 non-overlapping bubbles r ∈ U[0.02, 0.05] (seed 5), Eö = 5
     N = 512
-    sim = bubbly((N, N, N), swarm_layout(N=N), G=1e-3, Eo=5.0)
+    sim = bubbly((N, N, N), workloads.swarm_layout(N=N), G=1e-3, Eo=5.0)
     check_properties(sim, 2, 1e-12)

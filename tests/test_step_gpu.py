@@ -160,24 +160,48 @@ def test_mpcfl_matches_oracle(cuda):
     assert abs(ia.MPCFL(sim) - orc.mpcfl()) < 1e-12 * orc.mpcfl()
 
 
-@pytest.mark.parametrize("limiter", ["upwind", "minmod", "vanAlbada1", "Sweby", "superbee", "TVDcen", "TVDdown"])
-def test_every_limiter_matches_oracle(cuda, limiter):
-    # the λ(u,c,d) keyword of TwoPhaseSimulation (src/flow.jl:5-15), on a sheared 2D droplet
+@pytest.mark.parametrize("arith", ["fp64", "ff"])
+@pytest.mark.parametrize("limiter", ["Koren", "upwind", "minmod", "vanAlbada1", "Sweby", "superbee", "TVDcen",
+                                     "TVDdown"])
+def test_every_limiter_matches_oracle(cuda, limiter, arith):
+    # the λ(u,c,d) keyword of TwoPhaseSimulation (src/flow.jl:5-15), on a sheared 2D droplet, with the
+    # momentum kernels in FP64 and in FP32 pairs
     N = 24
     k = 2 * math.pi / N
     u0_t = lambda i, x: 0.3 * torch.sin(x[1] * k) if i == 0 else 0.2 * torch.cos(x[0] * k)
     u0_n = lambda i, x: 0.3 * np.sin(x[1] * k) if i == 0 else 0.2 * np.cos(x[0] * k)
     sdf_t = lambda x: torch.sqrt((x[0] - 10) ** 2 + (x[1] - 12) ** 2) - 5
     sdf_n = lambda x: np.sqrt((x[0] - 10) ** 2 + (x[1] - 12) ** 2) - 5
-    sim = ia.TwoPhaseSimulation((N, N), (0.0, 0.0), float(N), λρ=0.05, λμ=0.1, InterfaceSDF=sdf_t, u0=u0_t,
-                                perdir=(0, 1), λ=limiter, poisson_tol=PTOL, poisson_itmx=500)
-    orc = OracleSim((N, N), (0.0, 0.0), sdf=sdf_n, u0=u0_n, perdir=(0, 1), lrho=0.05, lmu=0.1, limiter=limiter,
-                    ptol=PTOL)
+    sim = ia.TwoPhaseSimulation((N, N), (0.0, 0.0), float(N), λρ=0.05, λμ=0.1, ν=0.01, InterfaceSDF=sdf_t, u0=u0_t,
+                                perdir=(0, 1), λ=limiter, poisson_tol=PTOL, poisson_itmx=500, momentum_arith=arith)
+    orc = OracleSim((N, N), (0.0, 0.0), sdf=sdf_n, u0=u0_n, perdir=(0, 1), lrho=0.05, lmu=0.1, ν=0.01,
+                    limiter=limiter, ptol=PTOL)
     for _ in range(3):
         ia.sim_step(sim)
         orc.step()
     ef, eu, ep = compare(sim, orc, 2)
     assert ef < 1e-10 and eu < 1e-10 and ep < 1e-6, (limiter, ef, eu, ep)
+
+
+@pytest.mark.parametrize("dims,per,eta", [((16, 12), (), 0.0), ((12, 10, 8), (0, 2), 0.05)])
+def test_float_float_momentum_agrees_with_fp64(cuda, dims, per, eta):
+    # the same step with the momentum kernels in FP32 pairs and in FP64 (both with the FP64 solver):
+    # the pair arithmetic carries ~2^-46 relative error per operation
+    D = len(dims)
+    c = tuple(0.5 * n + 0.7 for n in dims)
+    sdf = lambda x: torch.sqrt(sum((x[d] - c[d]) ** 2 for d in range(D))) - 0.3 * dims[0]
+    g = (0.0, -0.01) + ((0.0,) if D == 3 else ())
+    mk = lambda arith: ia.TwoPhaseSimulation(dims, (0.0,) * D, float(dims[0]), perdir=per, InterfaceSDF=sdf, λρ=1e-3,
+                                             λμ=1e-2, ν=0.02, g=g, η=(eta or None), poisson="fp64", poisson_tol=PTOL,
+                                             poisson_itmx=500, momentum_arith=arith)
+    a, b = mk("fp64"), mk("ff")
+    for _ in range(3):
+        ia.sim_step(a)
+        ia.sim_step(b)
+    du = float((a.flow.u - b.flow.u).abs().max()) / float(a.flow.u.abs().max())
+    df = float((a.intf.f - b.intf.f).abs().max())
+    assert du < 1e-11 and df < 1e-11, (du, df)
+    assert du > 0.0, "the two arithmetics must differ at the rounding level (is the pair path running?)"
 
 
 @pytest.mark.parametrize("dims,per", [((10, 7), ()), ((10, 7), (0, 1)), ((10, 7), (1,)), ((8, 6, 5), (0, 2)),
