@@ -397,7 +397,7 @@ def run_bubble(args, world, local_rank):
     out["e2e"] = e2e
     del sim
     torch.cuda.empty_cache()
-    if args.no_secondary:
+    if args.no_secondary or args.quick:
         return out
     k = max(2, min(args.steps, 5))
     for key, arith in (("fp64_mg", "fp64"), ("fp64_mg_ff", "ff")):

@@ -8,6 +8,7 @@
 #include <new>
 
 #include "capi_internal.cuh"
+#include "ff.cuh"
 
 using namespace ia;
 
@@ -96,7 +97,7 @@ int translate_fill_status(const Grid& g, const DevStatus& s, const double* u1, c
 
 // One advect! (src/advection.jl:17-78) or one advectVOF1d! sweep sequence.
 int vof_sweep(ia_handle* h, const double* fin, double* fout, const double* u1, const double* u2, double dt, int d,
-              bool first, int8_t* cbar, double* rhouf, double tol_rep, int counter) {
+              bool first, int8_t* cbar, double* rhouf, double tol_rep, int counter, float2* dila) {
     const Grid& g = h->g;
     {
         const int k = 0, counter_base = counter;
@@ -127,6 +128,14 @@ int vof_sweep(ia_handle* h, const double* fin, double* fout, const double* u1, c
         a.flux = h->flux;
         a.vals = h->tmp1;
         a.st = h->dst;
+        if (dila) {
+            const ff rql = ff_split(0.25 * h->cfg.lrho), rq1 = ff_split(0.25 * (h->cfg.lrho + (1.0 - h->cfg.lrho)));
+            a.dila = dila;
+            a.rq_l_hi = rql.hi;
+            a.rq_l_lo = rql.lo;
+            a.rq_1_hi = rq1.hi;
+            a.rq_1_lo = rq1.lo;
+        }
         int tk = timing_begin(h, TK_VOF_BULK);
         cudaError_t e = vof_sweep_bulk(a, h->stream);
         timing_end(h, tk);

@@ -58,9 +58,10 @@ int status_collect(ia_handle* h, const double* u1, const double* u2, ia_status* 
 // the divergence check of both velocity fields at a flagged cell) and the reportFillError return
 // code (src/advection.jl:145-189).  Shared by every entry point that reports a fill status.
 int translate_fill_status(const Grid& g, const DevStatus& s, const double* u1, const double* u2, ia_status& st);
-// one VOF sweep along d, fin -> fout (fin == fout: in place)
+// one VOF sweep along d, fin -> fout (fin == fout: in place); dila (coupled momentum step, float-float
+// arithmetic): receives the momentum update's dilation term of every cell as FP32 pairs
 int vof_sweep(ia_handle* h, const double* fin, double* fout, const double* u1, const double* u2, double dt, int d,
-              bool first, int8_t* cbar, double* rhouf, double tol_rep, int counter);
+              bool first, int8_t* cbar, double* rhouf, double tol_rep, int counter, float2* dila = nullptr);
 int advect_sweeps(ia_handle* h, double* f, const double* u1, const double* u2, double dt, const int* dirs,
                   int nsweeps, int8_t* cbar, double* rhouf, double tol_rep, bool first_writes_cbar,
                   int counter_base);

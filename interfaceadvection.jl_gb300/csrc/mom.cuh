@@ -55,8 +55,9 @@ cudaError_t k_average(double* a, const double* b, long long n, cudaStream_t s);
 cudaError_t k_ustar_ff(const MomConsts& k, const double* rhou, const double* f, float2* ustar, cudaStream_t s);
 cudaError_t k_momflux_ff(const MomConsts& k, int j, int limiter, const float2* ustar, const double* rhouf_j,
                          const double* fold, double dt, float2* Phi, cudaStream_t s);
-cudaError_t k_momupdate_ff(const MomConsts& k, int j, const float2* Phi, const double* uOld, const double* u1,
-                           const double* u2, const int8_t* cbar, double dt, double* rhou, cudaStream_t s);
+// dq: the dilation term ρ̄∂ⱼuⱼ/2 of every cell as pairs, written by the sweep's VOF bulk pass
+cudaError_t k_momupdate_ff(const MomConsts& k, int j, const float2* Phi, const float2* dq, const double* uOld, double dt,
+                           double* rhou, cudaStream_t s);
 cudaError_t k_visc_ff(const MomConsts& k, const double* u, const double* f, double lmu, double mu, float2* Phi6,
                       double* r, cudaStream_t s);
 cudaError_t k_updateu_ff(const MomConsts& k, double* u, double* rhou, const double* u0, const double* F, double dt,

@@ -76,12 +76,15 @@ __device__ __forceinline__ ff mul_rho_ff(const MomConsts& k, const MomFF& q, ff 
 }
 
 // ------------------------------------------------------------------ uStar = BC!(ρu / ρ(f))
+// (components unrolled: the boundary value of component i is then a fixed parameter offset)
+template <int D>
 __global__ void ustar_ff_kern(MomConsts k, MomFF q, const double* __restrict__ rhou, const double* __restrict__ f,
                               float2* __restrict__ us) {
     const Grid& g = k.g;
     GCELL_XYZ
     const long long O = lin(g, x, y, z);
-    for (int i = 0; i < g.D; ++i) {
+#pragma unroll
+    for (int i = 0; i < D; ++i) {
         int c[3] = {x, y, z};
         ff v;
         if (vel_bc(g, i, c)) {
@@ -95,24 +98,34 @@ __global__ void ustar_ff_kern(MomConsts k, MomFF q, const double* __restrict__ r
 }
 
 // ------------------------------------------------------------------ limiters (src/flow.jl:5-15)
+// Each limiter λ(u, c, d) is returned as its correction m = λ(u, c, d) - c, from δ₁ = c - u and
+// δ₂ = d - c: the SynDRoM blend below needs only m (v_d = c + m, c - v_d = -m).
 __device__ __forceinline__ ff ff_signed(bool pos, ff v) { return pos ? v : -v; }
+// median(a, 0, b): the one of smaller magnitude when a and b share a sign, else 0
+__device__ __forceinline__ ff ff_minmod(ff a, ff b) {
+    const bool same = (a.hi > 0.0f && b.hi > 0.0f) || (a.hi < 0.0f && b.hi < 0.0f);
+    const bool lt = ff_lt(a, b);
+    const ff r = (a.hi > 0.0f) == lt ? a : b;
+    return same ? r : ff_from(0.0f);
+}
 
 template <int LIM>
-__device__ __forceinline__ ff limiter_ff(const FluxFF& Q, ff u, ff c, ff d) {
-    if (LIM == IA_LIMITER_UPWIND) return c;
-    if (LIM == IA_LIMITER_MINMOD)
-        return ff_median3(ff_scale2(ff_sub(ff_mulf(c, 3.0f), u), 0.5f), c, ff_scale2(ff_add(c, d), 0.5f));
-    if (LIM == IA_LIMITER_VANALBADA1) {
-        const ff al = ff_sub(c, u), be = ff_sub(d, c);
-        const ff fac = (ff_zero(al) && ff_zero(be)) ? ff_from(0.0f)
-                                                    : ff_div(ff_add(al, be), ff_add(ff_mul(al, al), ff_mul(be, be)));
-        return ff_add(c, ff_scale2(ff_mul(ff_max(ff_mul(al, be), ff_from(0.0f)), fac), 0.5f));
+__device__ __forceinline__ ff limiter_corr_ff(const FluxFF& Q, ff u, ff c, ff d) {
+    if (LIM == IA_LIMITER_UPWIND) return ff_from(0.0f);
+    const ff d1 = ff_sub(c, u), d2 = ff_sub(d, c);
+    if (LIM == IA_LIMITER_MINMOD)   // median((3c - u)/2, c, (c + d)/2) = c + median(δ₁, 0, δ₂)/2
+        return ff_scale2(ff_minmod(d1, d2), 0.5f);
+    if (LIM == IA_LIMITER_VANALBADA1) {   // c + max(δ₁δ₂, 0)(δ₁ + δ₂)/(δ₁² + δ₂²)/2
+        const ff fac = (ff_zero(d1) && ff_zero(d2)) ? ff_from(0.0f)
+                                                    : ff_div(ff_add(d1, d2), ff_add(ff_mul(d1, d1), ff_mul(d2, d2)));
+        return ff_scale2(ff_mul(ff_max(ff_mul(d1, d2), ff_from(0.0f)), fac), 0.5f);
     }
     if (LIM == IA_LIMITER_SWEBY || LIM == IA_LIMITER_SUPERBEE || LIM == IA_LIMITER_TVDCEN ||
         LIM == IA_LIMITER_TVDDOWN) {
-        if (!ff_lt(ff_min(u, d), c) || !ff_lt(c, ff_max(u, d))) return c;
-        const bool s = ff_pos(ff_sub(d, u));               // c strictly between u and d: d - u != 0
-        const ff cu = ff_signed(s, ff_sub(c, u)), dc = ff_signed(s, ff_sub(d, c));
+        // c strictly between u and d, else c; s = sign(d - u)
+        if (!ff_lt(ff_min(u, d), c) || !ff_lt(c, ff_max(u, d))) return ff_from(0.0f);
+        const bool s = ff_pos(ff_sub(d, u));
+        const ff cu = ff_signed(s, d1), dc = ff_signed(s, d2);
         ff r;
         if (LIM == IA_LIMITER_TVDCEN) {
             r = ff_min(cu, ff_scale2(dc, 0.5f));
@@ -123,16 +136,16 @@ __device__ __forceinline__ ff limiter_ff(const FluxFF& Q, ff u, ff c, ff d) {
             r = ff_scale2(ff_max(ff_max(ff_from(0.0f), ff_min(ff_mulf(cu, gam), dc)), ff_min(cu, ff_mulf(dc, gam))),
                           0.5f);
         }
-        return ff_add(c, ff_signed(s, r));
+        return ff_signed(s, r);
     }
-    // Koren: median(fma(-2, u, fma(7, c, d)) / 6, c, median(2c - u, c, d))
-    const ff t = ff_mul(ff_sub(ff_add(ff_mulf(c, 7.0f), d), ff_scale2(u, 2.0f)), Q.sixth);
-    return ff_median3(t, c, ff_median3(ff_sub(ff_scale2(c, 2.0f), u), c, d));
+    // Koren: median((7c + d - 2u)/6, c, median(2c - u, c, d)) = c + median((2δ₁ + δ₂)/6, 0, median(δ₁, 0, δ₂))
+    const ff tau = ff_mul(ff_add(ff_scale2(d1, 2.0f), d2), Q.sixth);
+    return ff_minmod(tau, ff_minmod(d1, d2));
 }
 
-// SynDRoM blend Ψ (v_d + l₂ (v_I - v_d)) once l₂ is known (src/flow.jl:37-57)
-__device__ __forceinline__ ff blend(ff Psi, ff l2, ff cc, ff vd) {
-    return ff_mul(Psi, ff_add(ff_mul(l2, ff_sub(cc, vd)), vd));
+// SynDRoM blend Ψ (v_d + l₂ (v_I - v_d)) = Ψ (c + (1 - l₂) m) once l₂ is known (src/flow.jl:37-57)
+__device__ __forceinline__ ff blend(ff Psi, ff l2, ff cc, ff m) {
+    return ff_mul(Psi, ff_add(cc, ff_mul(ff_sub(ff_from(1.0f), l2), m)));
 }
 
 // l₂ = m_out / m_old on a face whose old density m is mixed, or -1 when m_old < m_out
@@ -144,7 +157,7 @@ __device__ __noinline__ double l2_from_m(double mOld, double aP, double dt) {
 
 template <int LIM>
 __device__ ff phiq_inner_ff(const FluxCtx& F, const FluxFF& Q, ff Psi, ff uu, ff cc, ff dd, double fa, double fb) {
-    const ff vd = limiter_ff<LIM>(Q, uu, cc, dd);
+    const ff m = limiter_corr_ff<LIM>(Q, uu, cc, dd);
     const ff aP = ff_abs(Psi);
     const unsigned long long a = dbits(fa), b = dbits(fb);
     ff l2;
@@ -157,14 +170,14 @@ __device__ ff phiq_inner_ff(const FluxCtx& F, const FluxFF& Q, ff Psi, ff uu, ff
         if (l < 0.0) return ff_mul(Psi, cc);
         l2 = ff_split(l);
     }
-    return blend(Psi, l2, cc, vd);
+    return blend(Psi, l2, cc, m);
 }
 
 template <int LIM>
 __device__ ff phiq_ff(const FluxCtx& F, const FluxFF& Q, int i, const int cic[3], ff Psi, ff uu, ff cc, ff dd) {
     int c[3] = {cic[0], cic[1], cic[2]};
     if (ff_pos(Psi)) c[F.j] -= 1;                        // IiCell = Ψ>0 ? Ii-δj : Ii
-    const ff vd = limiter_ff<LIM>(Q, uu, cc, dd);
+    const ff m = limiter_corr_ff<LIM>(Q, uu, cc, dd);
     const ff aP = ff_abs(Psi);
     double mOld = 0.0;
     const int kind = m_old_kind(F, i, c, mOld);
@@ -180,7 +193,7 @@ __device__ ff phiq_ff(const FluxCtx& F, const FluxFF& Q, int i, const int cic[3]
         if (l < 0.0) return ff_mul(Psi, cc);
         l2 = ff_split(l);
     }
-    return blend(Psi, l2, cc, vd);
+    return blend(Psi, l2, cc, m);
 }
 
 // Ψ = ϕ(i, CI(I,j), ρuf/δt) on a face near a boundary (a BC! face holds u_BC, not ρuf)
@@ -254,64 +267,30 @@ __global__ void __launch_bounds__(256, 4) momflux_ff_kern(FluxCtx F, FluxFF Q, c
 }
 
 // ------------------------------------------------------------------ ρu += δt (Φ(I) - Φ(I+δj) + uOld ϕ(i,I,ρ̄∂ⱼuⱼ))
-// ρ̄∂ⱼuⱼ/2 at a (ghost-mapped) cell: getρ(I,c̄,λρ)(∂(d,I,u)+∂(d,I,u⁰))/4
-__device__ __forceinline__ ff dila_q_ff(const Grid& g, ff rq_l, ff rq_1, int d, int c[3], const double* u1,
-                                        const double* u2, const int8_t* cbar) {
-    for (int e = 0; e < g.D; ++e) c[e] = bc_src(g, e, c[e]);
-    const long long P = lin3(g, c);
-    const long long sd = g.s[d];
-    const ff du = ff_add(ff_sub(ff_split(u1[P + sd]), ff_split(u1[P])), ff_sub(ff_split(u2[P + sd]), ff_split(u2[P])));
-    return ff_mul(cbar[P] ? rq_1 : rq_l, du);
-}
-
-// same z-march over 32 x 8 columns as momupdate_kern (mom.cu): each plane's ρ̄∂ⱼuⱼ/2 (plus the
-// x-1 / y-1 halo) is computed once into shared memory
+// dq = ρ̄∂ⱼuⱼ/2 of every cell (ghosts mapped), written by the sweep's VOF bulk pass, so that
+// ϕ(i, I, ρ̄∂ⱼuⱼ) = dq(I) + dq(I-δi); one interior cell per thread, every load issued first.
 template <int D>
-__global__ void __launch_bounds__(256) momupdate_ff_kern(MomConsts k, MomFF q, int j, const float2* __restrict__ Phi,
-                                                         const double* __restrict__ uOld,
-                                                         const double* __restrict__ u1d, const double* __restrict__ u2d,
-                                                         const int8_t* __restrict__ cbar, ff dt,
+__global__ void __launch_bounds__(256) momupdate_ff_kern(Grid g, long long sj, const float2* __restrict__ Phi,
+                                                         const float2* __restrict__ dq,
+                                                         const double* __restrict__ uOld, ff dt,
                                                          double* __restrict__ rhou) {
-    const Grid& g = k.g;
-    __shared__ float2 tile[9][33];
-    const int tx = threadIdx.x, ty = threadIdx.y;
-    const int x0 = 1 + blockIdx.x * 32, y0 = 1 + blockIdx.y * 8;
-    const int x = x0 + tx, y = y0 + ty;
-    const bool active = x <= g.n[0] - 2 && y <= g.n[1] - 2;
-    const ff rq_l = ff_scale2(q.lrho, 0.25f), rq_1 = ff_scale2(q.rho1, 0.25f);
-    const int zs = D == 3 ? 1 + int(blockIdx.z) * MU_ZC : 0;
-    const int ze = D == 3 ? min(zs + MU_ZC, g.n[2] - 1) : 1;
-    ff dprev = ff_from(0.0f);
-    if (D == 3 && active) {
-        int cm[3] = {x, y, zs - 1};
-        dprev = dila_q_ff(g, rq_l, rq_1, j, cm, u1d, u2d, cbar);
-    }
-    for (int z = zs; z < ze; ++z) {
-        for (int l = ty * 32 + tx; l < 9 * 33; l += 256) {
-            const int xx = x0 - 1 + l % 33, yy = y0 - 1 + l / 33;
-            ff v = ff_from(0.0f);
-            if (xx <= g.n[0] - 2 && yy <= g.n[1] - 2) {
-                int cc[3] = {xx, yy, z};
-                v = dila_q_ff(g, rq_l, rq_1, j, cc, u1d, u2d, cbar);
-            }
-            tile[l / 33][l % 33] = make_float2(v.hi, v.lo);
-        }
-        __syncthreads();
-        if (active) {
-            const long long I = lin(g, x, y, z);
-            const float2 tI = tile[ty + 1][tx + 1], tx0 = tile[ty + 1][tx], ty0 = tile[ty][tx + 1];
-            const ff dI = {tI.x, tI.y};
-            const ff dm[3] = {{tx0.x, tx0.y}, {ty0.x, ty0.y}, dprev};
-            const long long sj = g.s[j];
+    ICELL_XYZ
+    const long long I = lin(g, x, y, z);
+    const ff dI = ldff(dq + I);
+    ff dm[D], p0[D], p1[D];
+    double uo[D], r0[D];
 #pragma unroll
-            for (int i = 0; i < D; ++i) {
-                const ff flux = ff_sub(ldff(Phi + I + i * g.N), ldff(Phi + I + sj + i * g.N));
-                const ff r = ff_add(ff_mul(ff_split(uOld[I + i * g.N]), ff_add(dI, dm[i])), flux);
-                rhou[I + i * g.N] = ff_join(ff_add(ff_mul(dt, r), ff_split(rhou[I + i * g.N])));
-            }
-            dprev = dI;
-        }
-        __syncthreads();
+    for (int i = 0; i < D; ++i) {
+        dm[i] = ldff(dq + I - g.s[i]);
+        p0[i] = ldff(Phi + I + i * g.N);
+        p1[i] = ldff(Phi + I + sj + i * g.N);
+        uo[i] = uOld[I + i * g.N];
+        r0[i] = rhou[I + i * g.N];
+    }
+#pragma unroll
+    for (int i = 0; i < D; ++i) {
+        const ff r = ff_add(ff_mul(ff_split(uo[i]), ff_add(dI, dm[i])), ff_sub(p0[i], p1[i]));
+        rhou[I + i * g.N] = ff_join(ff_add(ff_mul(dt, r), ff_split(r0[i])));
     }
 }
 
@@ -325,7 +304,7 @@ __device__ __forceinline__ ff mu_ff(const ViscFF& W, double mu) {
 }
 
 template <int D>
-__global__ void __launch_bounds__(256, 4) viscflux_ff_kern(ViscCtx V, ViscFF W, float2* __restrict__ Phi6) {
+__global__ void __launch_bounds__(256, 3) viscflux_ff_kern(ViscCtx V, ViscFF W, float2* __restrict__ Phi6) {
     const Grid& g = V.k.g;
     SPLIT_XYZ
     const int c[3] = {x, y, z};
@@ -381,7 +360,7 @@ __global__ void viscacc_ff_kern(Grid g, const float2* __restrict__ Phi6, double*
 }
 
 // ------------------------------------------------------------------ updateU! (src/flow.jl:244-252)
-template <bool A0>
+template <int D, bool A0>
 __global__ void updateu_ff_kern(MomConsts k, MomFF q, double* __restrict__ u, double* __restrict__ rhou,
                                 const double* __restrict__ u0, const double* __restrict__ F, ff dt, ff w, ff a,
                                 ff dtw, const double* __restrict__ fref, const double* __restrict__ fupd,
@@ -389,25 +368,33 @@ __global__ void updateu_ff_kern(MomConsts k, MomFF q, double* __restrict__ u, do
     const Grid& g = k.g;
     ICELL_XYZ
     const long long I = lin(g, x, y, z);
-    for (int i = 0; i < g.D; ++i) {
-        const long long qI = I + i * g.N;
-        ff rn = ff_add(ff_split(rhou[qI]), ff_mul(ff_split(F[qI]), dt));
-        if (!A0) {
-            const ff rho0 = mul_rho_ff(k, q, ff_split(u0[qI]), fref[I], fref[I - g.s[i]]);   // u2ρu!(n̂, u⁰, c.f)
-            rn = ff_add(ff_mul(a, rho0), rn);
-        }
+    double rv[D], Fv[D], u0v[D], fu[D], fr[D];
+    const double fuI = fupd[I], frI = A0 ? 0.0 : fref[I];
+#pragma unroll
+    for (int i = 0; i < D; ++i) {
+        rv[i] = rhou[I + i * g.N];
+        Fv[i] = F[I + i * g.N];
+        u0v[i] = A0 ? 0.0 : u0[I + i * g.N];
+        fu[i] = fupd[I - g.s[i]];
+        fr[i] = A0 ? 0.0 : fref[I - g.s[i]];
+    }
+#pragma unroll
+    for (int i = 0; i < D; ++i) {
+        ff rn = ff_add(ff_split(rv[i]), ff_mul(ff_split(Fv[i]), dt));
+        if (!A0) rn = ff_add(ff_mul(a, mul_rho_ff(k, q, ff_split(u0v[i]), frI, fr[i])), rn);   // u2ρu!(n̂, u⁰, c.f)
         rn = ff_mul(rn, w);
-        ff v = div_rho_ff(k, q, rn, fupd[I], fupd[I - g.s[i]]);
+        ff v = div_rho_ff(k, q, rn, fuI, fu[i]);
         if (k.has_g) v = ff_add(ff_mul(dtw, q.gvec[i]), v);
-        u[qI] = ff_join(v);
-        if (write_rhou) rhou[qI] = ff_join(rn);
+        u[I + i * g.N] = ff_join(v);
+        if (write_rhou) rhou[I + i * g.N] = ff_join(rn);
     }
 }
 
 }  // namespace
 
 cudaError_t k_ustar_ff(const MomConsts& k, const double* rhou, const double* f, float2* ustar, cudaStream_t s) {
-    { ustar_ff_kern<<<ggrd(k.g), blk(), 0, s>>>(k, mom_ff_consts(k), rhou, f, ustar); ia::note_launch(); }
+    if (k.g.D == 3) { ustar_ff_kern<3><<<ggrd(k.g), blk(), 0, s>>>(k, mom_ff_consts(k), rhou, f, ustar); ia::note_launch(); }
+    else { ustar_ff_kern<2><<<ggrd(k.g), blk(), 0, s>>>(k, mom_ff_consts(k), rhou, f, ustar); ia::note_launch(); }
     return cudaGetLastError();
 }
 
@@ -449,14 +436,12 @@ cudaError_t k_momflux_ff(const MomConsts& k, int j, int limiter, const float2* u
     return cudaGetLastError();
 }
 
-cudaError_t k_momupdate_ff(const MomConsts& k, int j, const float2* Phi, const double* uOld, const double* u1,
-                           const double* u2, const int8_t* cbar, double dt, double* rhou, cudaStream_t s) {
-    const Grid& g = k.g;
-    const dim3 tg((g.n[0] - 2 + 31) / 32, (g.n[1] - 2 + 7) / 8, g.D == 3 ? (g.n[2] - 2 + MU_ZC - 1) / MU_ZC : 1);
-    const MomFF q = mom_ff_consts(k);
+cudaError_t k_momupdate_ff(const MomConsts& k, int j, const float2* Phi, const float2* dq, const double* uOld, double dt,
+                           double* rhou, cudaStream_t s) {
     const ff dtf = ff_split(dt);
-    if (g.D == 3) { momupdate_ff_kern<3><<<tg, blk(), 0, s>>>(k, q, j, Phi, uOld, u1 + j * g.N, u2 + j * g.N, cbar, dtf, rhou); ia::note_launch(); }
-    else { momupdate_ff_kern<2><<<tg, blk(), 0, s>>>(k, q, j, Phi, uOld, u1 + j * g.N, u2 + j * g.N, cbar, dtf, rhou); ia::note_launch(); }
+    const long long sj = k.g.s[j];
+    if (k.g.D == 3) { momupdate_ff_kern<3><<<igrd(k.g), blk(), 0, s>>>(k.g, sj, Phi, dq, uOld, dtf, rhou); ia::note_launch(); }
+    else { momupdate_ff_kern<2><<<igrd(k.g), blk(), 0, s>>>(k.g, sj, Phi, dq, uOld, dtf, rhou); ia::note_launch(); }
     return cudaGetLastError();
 }
 
@@ -497,8 +482,11 @@ cudaError_t k_updateu_ff(const MomConsts& k, double* u, double* rhou, const doub
     const double a = 1.0 / w - 1.0;
     const MomFF q = mom_ff_consts(k);
     const ff dtf = ff_split(dt), wf = ff_split(w), af = ff_split(a), dtw = ff_split(dt * w);
-    if (a == 0.0) { updateu_ff_kern<true><<<igrd(k.g), blk(), 0, s>>>(k, q, u, rhou, u0, F, dtf, wf, af, dtw, fref, fupd, write_rhou); ia::note_launch(); }
-    else { updateu_ff_kern<false><<<igrd(k.g), blk(), 0, s>>>(k, q, u, rhou, u0, F, dtf, wf, af, dtw, fref, fupd, write_rhou); ia::note_launch(); }
+#define UPD_FF(D_, A0_) \
+    { updateu_ff_kern<D_, A0_><<<igrd(k.g), blk(), 0, s>>>(k, q, u, rhou, u0, F, dtf, wf, af, dtw, fref, fupd, write_rhou); ia::note_launch(); }
+    if (k.g.D == 3) { if (a == 0.0) UPD_FF(3, true) else UPD_FF(3, false) }
+    else { if (a == 0.0) UPD_FF(2, true) else UPD_FF(2, false) }
+#undef UPD_FF
     return cudaGetLastError();
 }
 

@@ -20,6 +20,7 @@ struct MomScratch {
     unsigned int* scount = nullptr;   // D list lengths
     double* ft1 = nullptr;     // out-of-place VOF sweep buffers
     double* ft2 = nullptr;
+    double* dq = nullptr;      // dilation term of the float-float momentum update (N FP32 pairs)
     unsigned long long* cfl = nullptr;   // device max reductions (2)
     unsigned long long* hcfl = nullptr;  // pinned host copy
 };
@@ -66,6 +67,7 @@ static int ensure_scratch(ia_handle* h) {
     e = e ? e : cudaMalloc(&m->scount, sizeof(unsigned int) * D);
     e = e ? e : cudaMalloc(&m->ft1, 8 * N);
     e = e ? e : cudaMalloc(&m->ft2, 8 * N);
+    e = e ? e : cudaMalloc(&m->dq, 8 * N);
     e = e ? e : cudaMalloc(&m->cfl, 16);
     e = e ? e : cudaMallocHost(&m->hcfl, 16);
     if (e != cudaSuccess) return IA_ERR_CUDA;
@@ -87,6 +89,7 @@ void extra_destroy(ia_handle* h) {
     cudaFree(m->scount);
     cudaFree(m->ft1);
     cudaFree(m->ft2);
+    cudaFree(m->dq);
     cudaFree(m->cfl);
     if (m->hcfl) cudaFreeHost(m->hcfl);
     delete m;
@@ -117,7 +120,8 @@ static int advect_fq(ia_handle* h, double* f, const double* u1, const double* u2
         cudaError_t e = ff ? k_ustar_ff(k, h->fld.rhou, fin, us2, st) : k_ustar(k, h->fld.rhou, fin, m->ustar, st);
         if (e != cudaSuccess) return IA_ERR_CUDA;
         timing_end(h, tk);
-        int rc = vof_sweep(h, fin, fout, u1, u2, dt, d, q == 0, cbar, h->fld.rhouf, 10.0 * tol, counter_base + q);
+        float2* dq2 = ff ? reinterpret_cast<float2*>(m->dq) : nullptr;
+        int rc = vof_sweep(h, fin, fout, u1, u2, dt, d, q == 0, cbar, h->fld.rhouf, 10.0 * tol, counter_base + q, dq2);
         if (rc != IA_OK) return rc;
         const double* rj = h->fld.rhouf + (long long)d * g.N;
         tk = timing_begin(h, TK_MOM_FLUX);
@@ -126,7 +130,7 @@ static int advect_fq(ia_handle* h, double* f, const double* u1, const double* u2
         if (e != cudaSuccess) return IA_ERR_CUDA;
         timing_end(h, tk);
         tk = timing_begin(h, TK_MOM_UPDATE);
-        e = ff ? k_momupdate_ff(k, d, Phi2, uOld, u1, u2, cbar, dt, h->fld.rhou, st)
+        e = ff ? k_momupdate_ff(k, d, Phi2, dq2, uOld, dt, h->fld.rhou, st)
                : k_momupdate(k, d, m->Phi, uOld, u1, u2, cbar, dt, h->fld.rhou, st);
         if (e != cudaSuccess) return IA_ERR_CUDA;
         timing_end(h, tk);

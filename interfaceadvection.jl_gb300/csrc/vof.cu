@@ -28,6 +28,7 @@
 // and the next sweep reads valid ghosts.
 #include <cuda_runtime.h>
 
+#include "ff.cuh"
 #include "ia_core.cuh"
 #include "ia_geom.cuh"
 #include "vof.cuh"
@@ -201,6 +202,18 @@ __global__ void __launch_bounds__(256) vof_bulk(SweepArgs a) {
                           abs_le(bits(a.u1[S]), a.ulim) && abs_le(bits(a.u1[S + sd]), a.ulim) &&
                           abs_le(bits(a.u2[S]), a.ulim) && abs_le(bits(a.u2[S + sd]), a.ulim);
         need_cell = !bulk;
+        if (a.dila) {
+            // the momentum update's dilation term of this (ghost-mapped) cell, on FP32 pairs: c̄ of the
+            // source cell (in the first sweep from its fraction, as the c̄ pass above computes it)
+            int cs;
+            if (FIRST) cs = (((bc & ABS_MASK) <= 0x7FF0000000000000ull) && ((bc >> 63) || bc < 0x3FE0000000000000ull)) ? 0 : 1;
+            else cs = cb;
+            const ff du = ff_add(ff_sub(ff_split(a.u1[S + sd]), ff_split(a.u1[S])),
+                                 ff_sub(ff_split(a.u2[S + sd]), ff_split(a.u2[S])));
+            const ff rq = cs ? ff{a.rq_1_hi, a.rq_1_lo} : ff{a.rq_l_hi, a.rq_l_lo};
+            const ff dq = ff_mul(rq, du);
+            a.dila[O] = make_float2(dq.hi, dq.lo);
+        }
         // in place a bulk cell keeps its value and only a stale ghost copy needs a write;
         // out of place (the coupled step keeps f_old) every bulk cell is written
         if (bulk && (a.fin != a.fout || ((O != S) && bits(a.fin[O]) != bc)))

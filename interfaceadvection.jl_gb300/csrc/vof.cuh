@@ -33,6 +33,11 @@ struct SweepArgs {
     double* flux;                     // cached face fluxes of listed faces
     double* vals;                     // staged new values of listed cells
     DevStatus* st;
+    // coupled momentum step only (NULL otherwise): d = getρ(I,c̄,λρ)(∂(d,I,u1) + ∂(d,I,u2))/4 of every cell
+    // (ghosts from their boundary-condition source cell) as FP32 pairs (hi, lo), the dilation term the
+    // momentum update reads (src/flow.jl:216, 229); rq = λρ/4 and (λρ + (1-λρ))/4 as pairs
+    float2* dila = nullptr;
+    float rq_l_hi = 0.f, rq_l_lo = 0.f, rq_1_hi = 0.f, rq_1_lo = 0.f;
 };
 
 cudaError_t vof_sweep_bulk(const SweepArgs& a, cudaStream_t st);
