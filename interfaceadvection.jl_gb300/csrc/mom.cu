@@ -731,6 +731,10 @@ cudaError_t k_cfl(const MomConsts& k, const double* u, unsigned long long* out2,
     { cfl_kern<<<int(rows < 1216 ? rows : 1216), 256, 0, s>>>(k.g, u, out2); ia::note_launch(); }
     return cudaGetLastError();
 }
+cudaError_t k_scale(double* a, long long n, double f, cudaStream_t s) {
+    { scale_kern<<<1216, 256, 0, s>>>(a, n, f); ia::note_launch(); }
+    return cudaGetLastError();
+}
 cudaError_t k_average(double* a, const double* b, long long n, cudaStream_t s) {
     { average_kern<<<1216, 256, 0, s>>>(a, b, n); ia::note_launch(); }
     return cudaGetLastError();

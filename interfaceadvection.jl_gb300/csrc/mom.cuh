@@ -47,6 +47,8 @@ cudaError_t k_div_scale(const MomConsts& k, const double* u, double* z, double* 
 cudaError_t k_correct(const MomConsts& k, double* u, const double* L, double* x, double dt, cudaStream_t s);
 // max flux_out and max maxTotalFlux over interior cells into out2 (device, as bit patterns)
 cudaError_t k_cfl(const MomConsts& k, const double* u, unsigned long long* out2, cudaStream_t s);
+// a *= f over n entries
+cudaError_t k_scale(double* a, long long n, double f, cudaStream_t s);
 // a = (a + b) / 2 over n entries
 cudaError_t k_average(double* a, const double* b, long long n, cudaStream_t s);
 
@@ -60,6 +62,10 @@ cudaError_t k_momupdate_ff(const MomConsts& k, int j, const float2* Phi, const f
                            double* rhou, cudaStream_t s);
 cudaError_t k_visc_ff(const MomConsts& k, const double* u, const double* f, double lmu, double mu, float2* Phi6,
                       double* r, cudaStream_t s);
+// z = div(u) (pair sums), x *= dt; u -= L ∂x (pairs), x *= 1/dt; MPCFL's maxima with pair sums
+cudaError_t k_div_scale_ff(const MomConsts& k, const double* u, double* zz, double* xx, double dt, cudaStream_t s);
+cudaError_t k_correct_ff(const MomConsts& k, double* u, const double* L, double* xx, double dt, cudaStream_t s);
+cudaError_t k_cfl_ff(const MomConsts& k, const double* u, unsigned long long* out2, cudaStream_t s);
 cudaError_t k_updateu_ff(const MomConsts& k, double* u, double* rhou, const double* u0, const double* F, double dt,
                          const double* fref, const double* fupd, double w, bool write_rhou, cudaStream_t s);
 

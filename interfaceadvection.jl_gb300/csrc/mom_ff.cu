@@ -83,6 +83,19 @@ __global__ void ustar_ff_kern(MomConsts k, MomFF q, const double* __restrict__ r
     const Grid& g = k.g;
     GCELL_XYZ
     const long long O = lin(g, x, y, z);
+    if (x >= 2 && x <= g.n[0] - 2 && y >= 2 && y <= g.n[1] - 2 && (D == 2 || (z >= 2 && z <= g.n[2] - 2))) {
+        // no Dirichlet face and no ghost source for any component: every load first
+        double r[D], fm[D];
+        const double fO = f[O];
+#pragma unroll
+        for (int i = 0; i < D; ++i) {
+            r[i] = rhou[O + i * g.N];
+            fm[i] = f[O - g.s[i]];
+        }
+#pragma unroll
+        for (int i = 0; i < D; ++i) stff(us + O + i * g.N, div_rho_ff(k, q, ff_split(r[i]), fO, fm[i]));
+        return;
+    }
 #pragma unroll
     for (int i = 0; i < D; ++i) {
         int c[3] = {x, y, z};
@@ -206,7 +219,7 @@ __device__ __forceinline__ ff face_psi_ff(const FluxCtx& F, const FluxFF& Q, int
 }
 
 template <int LIM>
-__global__ void __launch_bounds__(256, 4) momflux_ff_kern(FluxCtx F, FluxFF Q, const float2* __restrict__ us,
+__global__ void __launch_bounds__(256, 5) momflux_ff_kern(FluxCtx F, FluxFF Q, const float2* __restrict__ us,
                                                           float2* __restrict__ Phi) {
     const Grid& g = F.k.g;
     SPLIT_XYZ
@@ -303,31 +316,12 @@ __device__ __forceinline__ ff mu_ff(const ViscFF& W, double mu) {
     return ff_split(mu);
 }
 
+// viscous fluxes of a cell within two cells of a boundary (general ghost and boundary-face rules),
+// out of line so that the bulk path above keeps its own register budget
 template <int D>
-__global__ void __launch_bounds__(256, 3) viscflux_ff_kern(ViscCtx V, ViscFF W, float2* __restrict__ Phi6) {
+__device__ __noinline__ void viscflux_ff_edge(const ViscCtx& V, const ViscFF& W, float2* __restrict__ Phi6,
+                                             const int c[3], long long K) {
     const Grid& g = V.k.g;
-    SPLIT_XYZ
-    const int c[3] = {x, y, z};
-    const long long K = lin(g, x, y, z);
-    bool inner = true;
-#pragma unroll
-    for (int e = 0; e < D; ++e)
-        if (c[e] < 3 || c[e] > g.n[e] - 3) inner = false;
-    if (inner) {
-        ff uK[D];
-#pragma unroll
-        for (int i = 0; i < D; ++i) uK[i] = ff_split(V.u[K + i * g.N]);
-#pragma unroll
-        for (int i = 0; i < D; ++i)
-#pragma unroll
-            for (int j = i; j < D; ++j) {
-                const ff mu = mu_ff(W, get_mu_inner(V, i, j, c, K));
-                const ff sji = ff_sub(uK[i], ff_split(V.u[K - g.s[j] + i * g.N]));
-                const ff sij = ff_sub(uK[j], ff_split(V.u[K - g.s[i] + j * g.N]));
-                stff(Phi6 + pair_index(D, i, j) * g.N + K, -ff_mul(mu, ff_add(sji, sij)));
-            }
-        return;
-    }
     for (int i = 0; i < D; ++i)
         for (int j = i; j < D; ++j) {
             bool ok = true;
@@ -341,6 +335,68 @@ __global__ void __launch_bounds__(256, 3) viscflux_ff_kern(ViscCtx V, ViscFF W, 
             const ff sij = ff_sub(ff_split(V.u[K + j * g.N]), ff_split(V.u[K - g.s[i] + j * g.N]));
             stff(Phi6 + pair_index(D, i, j) * g.N + K, -ff_mul(mu, ff_add(sji, sij)));
         }
+}
+
+// viscous fluxes of a bulk cell next to the interface: the viscosity of each face or edge from its own
+// fractions (get_mu_inner)
+template <int D>
+__device__ __noinline__ void viscflux_ff_mixed(const ViscCtx& V, const ViscFF& W, float2* __restrict__ Phi6,
+                                              const int c[3], long long K) {
+    const Grid& g = V.k.g;
+#pragma unroll
+    for (int i = 0; i < D; ++i)
+#pragma unroll
+        for (int j = i; j < D; ++j) {
+            const ff mu = mu_ff(W, get_mu_inner(V, i, j, c, K));
+            const ff sji = ff_sub(ff_split(V.u[K + i * g.N]), ff_split(V.u[K - g.s[j] + i * g.N]));
+            const ff s2 = (i == j) ? ff_scale2(sji, 2.0f)
+                                   : ff_add(sji, ff_sub(ff_split(V.u[K + j * g.N]), ff_split(V.u[K - g.s[i] + j * g.N])));
+            stff(Phi6 + pair_index(D, i, j) * g.N + K, -ff_mul(mu, s2));
+        }
+}
+
+template <int D>
+__global__ void __launch_bounds__(256, 4) viscflux_ff_kern(ViscCtx V, ViscFF W, float2* __restrict__ Phi6) {
+    const Grid& g = V.k.g;
+    SPLIT_XYZ
+    const int c[3] = {x, y, z};
+    const long long K = lin(g, x, y, z);
+    bool inner = true;
+#pragma unroll
+    for (int e = 0; e < D; ++e)
+        if (c[e] < 3 || c[e] > g.n[e] - 3) inner = false;
+    if (inner) {
+        // the fractions any of the D(D+1)/2 viscosities reads (get_mu_inner: K, K-s_e, K-2s_e, K-s_i-s_j):
+        // when all are the same pure phase, every viscosity is that phase's constant
+        const double* f = V.f;
+        const unsigned long long b0 = dbits(f[K]);
+        bool pure = b0 == 0ull || b0 == kOneBits;
+#pragma unroll
+        for (int e = 0; e < D; ++e) pure = pure && dbits(f[K - g.s[e]]) == b0 && dbits(f[K - 2 * g.s[e]]) == b0;
+#pragma unroll
+        for (int i = 0; i < D; ++i)
+#pragma unroll
+            for (int j = i + 1; j < D; ++j) pure = pure && dbits(f[K - g.s[i] - g.s[j]]) == b0;
+        if (!pure) {   // interface cells (a few percent): per-face viscosities, out of line
+            viscflux_ff_mixed<D>(V, W, Phi6, c, K);
+            return;
+        }
+        const ff mu = b0 == 0ull ? W.mu_face0 : W.mu_face1;
+        ff uK[D];
+#pragma unroll
+        for (int i = 0; i < D; ++i) uK[i] = ff_split(V.u[K + i * g.N]);
+#pragma unroll
+        for (int i = 0; i < D; ++i)
+#pragma unroll
+            for (int j = i; j < D; ++j) {
+                // ∂ⱼuᵢ + ∂ᵢuⱼ; on the diagonal the two are the same difference
+                const ff sji = ff_sub(uK[i], ff_split(V.u[K - g.s[j] + i * g.N]));
+                const ff s2 = (i == j) ? ff_scale2(sji, 2.0f) : ff_add(sji, ff_sub(uK[j], ff_split(V.u[K - g.s[i] + j * g.N])));
+                stff(Phi6 + pair_index(D, i, j) * g.N + K, -ff_mul(mu, s2));
+            }
+        return;
+    }
+    viscflux_ff_edge<D>(V, W, Phi6, c, K);
 }
 
 template <int D>
@@ -387,6 +443,106 @@ __global__ void updateu_ff_kern(MomConsts k, MomFF q, double* __restrict__ u, do
         if (k.has_g) v = ff_add(ff_mul(dtw, q.gvec[i]), v);
         u[I + i * g.N] = ff_join(v);
         if (write_rhou) rhou[I + i * g.N] = ff_join(rn);
+    }
+}
+
+// ------------------------------------------------------------------ projection and CFL on pairs
+// z = div(u) on interior cells (WaterLily div, the source of myproject!, src/flow.jl:328-347), x *= dt on
+// every cell (one FP64 product, as in the FP64 kernel)
+template <int D>
+__global__ void div_scale_ff_kern(Grid g, const double* __restrict__ u, double* __restrict__ zz, double* __restrict__ xx,
+                                  double dt) {
+    GCELL_XYZ
+    const long long I = lin(g, x, y, z);
+    xx[I] *= dt;
+    if (x < 1 || x > g.n[0] - 2 || y < 1 || y > g.n[1] - 2 || (D == 3 && (z < 1 || z > g.n[2] - 2))) return;
+    double hi[D], lo[D];
+#pragma unroll
+    for (int d = 0; d < D; ++d) {
+        hi[d] = u[I + g.s[d] + d * g.N];
+        lo[d] = u[I + d * g.N];
+    }
+    ff s = ff_sub(ff_split(hi[0]), ff_split(lo[0]));
+#pragma unroll
+    for (int d = 1; d < D; ++d) s = ff_add(s, ff_sub(ff_split(hi[d]), ff_split(lo[d])));
+    zz[I] = ff_join(s);
+}
+
+// u -= L ∂x on interior cells (src/flow.jl:332)
+template <int D>
+__global__ void correct_ff_kern(Grid g, double* __restrict__ u, const double* __restrict__ L,
+                                const double* __restrict__ xx) {
+    ICELL_XYZ
+    const long long I = lin(g, x, y, z);
+    const ff xI = ff_split(xx[I]);
+    double uv[D], Lv[D], xm[D];
+#pragma unroll
+    for (int i = 0; i < D; ++i) {
+        uv[i] = u[I + i * g.N];
+        Lv[i] = L[I + i * g.N];
+        xm[i] = xx[I - g.s[i]];
+    }
+#pragma unroll
+    for (int i = 0; i < D; ++i)
+        u[I + i * g.N] = ff_join(ff_sub(ff_split(uv[i]), ff_mul(ff_split(Lv[i]), ff_sub(xI, ff_split(xm[i])))));
+}
+
+__device__ __forceinline__ unsigned long long nonneg_bits_ff(double v) {
+    const unsigned long long b = dbits(v);
+    return (b == 0x8000000000000000ull) ? 0ull : b;
+}
+__device__ __forceinline__ unsigned long long warp_umax_ff(unsigned long long v) {
+    for (int o = 16; o > 0; o >>= 1) {
+        const unsigned long long w = __shfl_down_sync(0xffffffffu, v, o);
+        v = w > v ? w : v;
+    }
+    return v;
+}
+
+// MPCFL's two maxima (src/flow.jl:262-289) with the per-cell sums on pairs: flux_out Σ max(0,u_hi) +
+// max(0,-u_lo) and maxTotalFlux Σ max(|u_lo|,|u_hi|); the terms are selected on the sign / magnitude bits,
+// the sums joined to FP64 and reduced as non-negative bit patterns (whole x-rows per block, as cfl_kern)
+template <int D>
+__global__ void cfl_ff_kern(Grid g, const double* __restrict__ u, unsigned long long* out) {
+    __shared__ unsigned long long s1[32], s2[32];
+    unsigned long long a1 = 0ull, a2 = 0ull;
+    const int nxi = g.n[0] - 2, nyi = g.n[1] - 2;
+    const int rows = nyi * (D == 3 ? g.n[2] - 2 : 1);
+    const int dy = int(gridDim.x) % nyi, dz = int(gridDim.x) / nyi;
+    int y = 1 + int(blockIdx.x) % nyi, z = (D == 3 ? 1 : 0) + int(blockIdx.x) / nyi;
+    for (int rw = blockIdx.x; rw < rows; rw += gridDim.x, y += dy, z += dz + (y > nyi ? 1 : 0), y -= (y > nyi ? nyi : 0)) {
+        for (int x = 1 + threadIdx.x; x <= nxi; x += blockDim.x) {
+            const long long I = lin(g, x, y, z);
+            ff fo = ff_from(0.0f), mt = ff_from(0.0f);
+#pragma unroll
+            for (int i = 0; i < D; ++i) {
+                const double lo = u[I + i * g.N], hi = u[I + g.s[i] + i * g.N];
+                const ff flo = ff_split(lo), fhi = ff_split(hi);
+                fo = ff_add(fo, ff_add(ff_pos(fhi) ? fhi : ff_from(0.0f), ff_neg(flo) ? -flo : ff_from(0.0f)));
+                const bool lo_big = (dbits(lo) & kAbsMask) >= (dbits(hi) & kAbsMask);
+                mt = ff_add(mt, ff_abs(lo_big ? flo : fhi));
+            }
+            const unsigned long long b1 = nonneg_bits_ff(ff_join(fo)), b2 = nonneg_bits_ff(ff_join(mt));
+            a1 = b1 > a1 ? b1 : a1;
+            a2 = b2 > a2 ? b2 : a2;
+        }
+    }
+    a1 = warp_umax_ff(a1);
+    a2 = warp_umax_ff(a2);
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    if (lane == 0) {
+        s1[w] = a1;
+        s2[w] = a2;
+    }
+    __syncthreads();
+    if (w == 0) {
+        const int nw = blockDim.x >> 5;
+        a1 = warp_umax_ff(lane < nw ? s1[lane] : 0ull);
+        a2 = warp_umax_ff(lane < nw ? s2[lane] : 0ull);
+        if (lane == 0) {
+            atomicMax(out, a1);
+            atomicMax(out + 1, a2);
+        }
     }
 }
 
@@ -487,6 +643,28 @@ cudaError_t k_updateu_ff(const MomConsts& k, double* u, double* rhou, const doub
     if (k.g.D == 3) { if (a == 0.0) UPD_FF(3, true) else UPD_FF(3, false) }
     else { if (a == 0.0) UPD_FF(2, true) else UPD_FF(2, false) }
 #undef UPD_FF
+    return cudaGetLastError();
+}
+
+}  // namespace ia
+
+namespace ia {
+
+cudaError_t k_div_scale_ff(const MomConsts& k, const double* u, double* zz, double* xx, double dt, cudaStream_t s) {
+    if (k.g.D == 3) { div_scale_ff_kern<3><<<ggrd(k.g), blk(), 0, s>>>(k.g, u, zz, xx, dt); ia::note_launch(); }
+    else { div_scale_ff_kern<2><<<ggrd(k.g), blk(), 0, s>>>(k.g, u, zz, xx, dt); ia::note_launch(); }
+    return cudaGetLastError();
+}
+cudaError_t k_correct_ff(const MomConsts& k, double* u, const double* L, double* xx, double dt, cudaStream_t s) {
+    if (k.g.D == 3) { correct_ff_kern<3><<<igrd(k.g), blk(), 0, s>>>(k.g, u, L, xx); ia::note_launch(); }
+    else { correct_ff_kern<2><<<igrd(k.g), blk(), 0, s>>>(k.g, u, L, xx); ia::note_launch(); }
+    return k_scale(xx, k.g.N, 1.0 / dt, s);
+}
+cudaError_t k_cfl_ff(const MomConsts& k, const double* u, unsigned long long* out2, cudaStream_t s) {
+    const long long rows = (long long)(k.g.n[1] - 2) * (k.g.D == 3 ? k.g.n[2] - 2 : 1);
+    const int nb = int(rows < 1216 ? rows : 1216);
+    if (k.g.D == 3) { cfl_ff_kern<3><<<nb, 256, 0, s>>>(k.g, u, out2); ia::note_launch(); }
+    else { cfl_ff_kern<2><<<nb, 256, 0, s>>>(k.g, u, out2); ia::note_launch(); }
     return cudaGetLastError();
 }
 

@@ -166,13 +166,17 @@ static int project(ia_handle* h, const double* f, double dtp, int* iters, double
     cudaStream_t st = h->stream;
     int tk = timing_begin(h, TK_UPDATE);
     if (k_updatel(k, h->fld.mu0, f, st) != cudaSuccess) return IA_ERR_CUDA;
-    if (k_div_scale(k, h->fld.u, h->fld.sigma, h->fld.p, dtp, st) != cudaSuccess) return IA_ERR_CUDA;
+    if ((use_ff(h) ? k_div_scale_ff(k, h->fld.u, h->fld.sigma, h->fld.p, dtp, st)
+                   : k_div_scale(k, h->fld.u, h->fld.sigma, h->fld.p, dtp, st)) != cudaSuccess)
+        return IA_ERR_CUDA;
     timing_end(h, tk);
     int rc = poisson_solve(h, h->fld.p, h->fld.sigma, h->fld.mu0, h->cfg.poisson_tol, h->cfg.poisson_itmx, iters,
                            resid);
     if (rc != IA_OK && rc != IA_WARN_NOT_CONVERGED) return rc;
     tk = timing_begin(h, TK_UPDATE);
-    if (k_correct(k, h->fld.u, h->fld.mu0, h->fld.p, dtp, st) != cudaSuccess) return IA_ERR_CUDA;
+    if ((use_ff(h) ? k_correct_ff(k, h->fld.u, h->fld.mu0, h->fld.p, dtp, st)
+                   : k_correct(k, h->fld.u, h->fld.mu0, h->fld.p, dtp, st)) != cudaSuccess)
+        return IA_ERR_CUDA;
     const double zero[3] = {h->cfg.uBC[0], h->cfg.uBC[1], h->cfg.uBC[2]};
     if (k_bc_vel(k, h->fld.u, zero, st) != cudaSuccess) return IA_ERR_CUDA;
     timing_end(h, tk);
@@ -185,7 +189,8 @@ static int mpcfl(ia_handle* h, double* out) {
     const MomConsts k = consts(h);
     cudaStream_t st = h->stream;
     cudaMemsetAsync(m->cfl, 0, 16, st);
-    if (k_cfl(k, h->fld.u, m->cfl, st) != cudaSuccess) return IA_ERR_CUDA;
+    if ((use_ff(h) ? k_cfl_ff(k, h->fld.u, m->cfl, st) : k_cfl(k, h->fld.u, m->cfl, st)) != cudaSuccess)
+        return IA_ERR_CUDA;
     cudaMemcpyAsync(m->hcfl, m->cfl, 16, cudaMemcpyDeviceToHost, st);
     if (cudaStreamSynchronize(st) != cudaSuccess) return IA_ERR_CUDA;
     double fo, mt;

@@ -73,8 +73,9 @@ def read_vti(path: str):
 
 
 class VTKWriter:
-    """vtkWriter(fname; dir) collection: ``save(sim)`` writes <dir>/<fname>_<k>.vti and rewrites
-    <fname>.pvd with every file and its simulation time (sim_time)."""
+    """vtkWriter(fname; dir) collection: ``save(sim)`` writes <dir>/<name>_<k>.vti (name: the base name
+    of fname) and rewrites <fname>.pvd with every file, relative to the .pvd's directory, and its
+    simulation time (sim_time)."""
 
     def __init__(self, fname: str = "WaterLily", dir: str = "vtk_data", k: int = 0, entries=None):
         self.fname, self.dir, self.k = fname, dir, k
@@ -84,20 +85,27 @@ class VTKWriter:
     def save(self, sim) -> str:
         shape = tuple(sim.flow.p.shape)
         arrays = {"p": (_host(sim.flow.p), 1), "f": (_host(sim.intf.f), 1), "u": (_host(sim.flow.u), len(shape))}
-        path = os.path.join(self.dir, f"{self.fname}_{self.k:06d}.vti")
+        path = os.path.join(self.dir, f"{os.path.basename(self.fname)}_{self.k:06d}.vti")
         write_vti(path, arrays, shape)
         self.entries.append((sim.sim_time(), path))
         self.k += 1
-        rows = "\n".join(f'    <DataSet timestep="{t!r}" part="0" file="{p}"/>' for t, p in self.entries)
-        with open(self.fname + ".pvd", "w") as fh:
+        # DataSet paths are relative to the collection file's directory, where ReadVTK's PVDFile
+        # resolves them
+        pvd = self.fname + ".pvd"
+        base = os.path.dirname(os.path.abspath(pvd))
+        rows = "\n".join(f'    <DataSet timestep="{t!r}" part="0" file="{os.path.relpath(os.path.abspath(p), base)}"/>'
+                         for t, p in self.entries)
+        with open(pvd, "w") as fh:
             fh.write('<?xml version="1.0" encoding="utf-8"?>\n<VTKFile type="Collection" version="1.0">\n'
                      f'  <Collection>\n{rows}\n  </Collection>\n</VTKFile>\n')
         return path
 
 
 def read_pvd(fname: str):
+    """(timestep, file) of every DataSet, the files resolved against the collection's directory."""
     root = ET.parse(fname).getroot()
-    return [(float(ds.get("timestep")), ds.get("file")) for ds in root.iter("DataSet")]
+    base = os.path.dirname(os.path.abspath(fname))
+    return [(float(ds.get("timestep")), os.path.join(base, ds.get("file"))) for ds in root.iter("DataSet")]
 
 
 def load(sim, fname: str = "WaterLily.pvd") -> VTKWriter:
@@ -122,4 +130,5 @@ def load(sim, fname: str = "WaterLily.pvd") -> VTKWriter:
     sim.flow.Δt[-1] = t * sim.L / sim.U
     sim.flow.Δt.append(MPCFL(sim))
     base = fname[:-4] if fname.endswith(".pvd") else fname
-    return VTKWriter(base, os.path.dirname(path) or ".", k=len(entries), entries=entries)
+    return VTKWriter(base, os.path.dirname(path) or ".", k=len(entries),
+                     entries=[(tt, os.path.relpath(pp)) for tt, pp in entries])
