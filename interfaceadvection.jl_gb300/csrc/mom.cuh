@@ -55,16 +55,17 @@ cudaError_t k_average(double* a, const double* b, long long n, cudaStream_t s);
 // Float-float (FP32-pair) counterparts of the momentum chain (mom_ff.cu): uStar, the face fluxes and
 // the viscous fluxes are pairs (float2); ρu, u and the forcing r stay FP64 fields.
 cudaError_t k_ustar_ff(const MomConsts& k, const double* rhou, const double* f, float2* ustar, cudaStream_t s);
+// the bulk faces directly, every other cell through a list (list: N entries, count: one counter)
 cudaError_t k_momflux_ff(const MomConsts& k, int j, int limiter, const float2* ustar, const double* rhouf_j,
-                         const double* fold, double dt, float2* Phi, cudaStream_t s);
+                         const double* fold, double dt, float2* Phi, unsigned int* list, unsigned int* count,
+                         int list_blocks, cudaStream_t s);
 // dq: the dilation term ρ̄∂ⱼuⱼ/2 of every cell as pairs, written by the sweep's VOF bulk pass
 cudaError_t k_momupdate_ff(const MomConsts& k, int j, const float2* Phi, const float2* dq, const double* uOld, double dt,
                            double* rhou, cudaStream_t s);
 cudaError_t k_visc_ff(const MomConsts& k, const double* u, const double* f, double lmu, double mu, float2* Phi6,
-                      double* r, cudaStream_t s);
-// z = div(u) (pair sums), x *= dt; u -= L ∂x (pairs), x *= 1/dt; MPCFL's maxima with pair sums
+                      double* r, unsigned int* list, unsigned int* count, int list_blocks, cudaStream_t s);
+// z = div(u) (pair sums), x *= dt; MPCFL's maxima with pair sums
 cudaError_t k_div_scale_ff(const MomConsts& k, const double* u, double* zz, double* xx, double dt, cudaStream_t s);
-cudaError_t k_correct_ff(const MomConsts& k, double* u, const double* L, double* xx, double dt, cudaStream_t s);
 cudaError_t k_cfl_ff(const MomConsts& k, const double* u, unsigned long long* out2, cudaStream_t s);
 cudaError_t k_updateu_ff(const MomConsts& k, double* u, double* rhou, const double* u0, const double* F, double dt,
                          const double* fref, const double* fupd, double w, bool write_rhou, cudaStream_t s);

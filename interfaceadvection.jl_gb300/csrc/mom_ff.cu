@@ -218,11 +218,12 @@ __device__ __forceinline__ ff face_psi_ff(const FluxCtx& F, const FluxFF& Q, int
     return ff_scale2(ff_add(ba ? a : ff_mul(a, Q.inv_dt), bb ? b : ff_mul(b, Q.inv_dt)), 0.5f);
 }
 
+// The face fluxes of one cell with every rule: boundary faces, periodic images, mixed donor faces
+// (the list kernel's work)
 template <int LIM>
-__global__ void __launch_bounds__(256, 5) momflux_ff_kern(FluxCtx F, FluxFF Q, const float2* __restrict__ us,
-                                                          float2* __restrict__ Phi) {
+__device__ __forceinline__ void momflux_ff_cell(const FluxCtx& F, const FluxFF& Q, const float2* __restrict__ us,
+                                                float2* __restrict__ Phi, int x, int y, int z) {
     const Grid& g = F.k.g;
-    SPLIT_XYZ
     const int j = F.j;
     int c[3] = {x, y, z};
     bool inner = true;
@@ -276,6 +277,94 @@ __global__ void __launch_bounds__(256, 5) momflux_ff_kern(FluxCtx F, FluxFF Q, c
             else { uu = ldff(u + Kk + sj); cc = ldff(u + Kk); dd = ldff(u + Kk - sj); }
         }
         stff(Phi + K + i * g.N, phiq_ff<LIM>(F, Q, i, c, Psi, uu, cc, dd));
+    }
+}
+
+// warp-aggregated append of the cells a bulk pass leaves to its list kernel
+__device__ __forceinline__ void list_append(unsigned int* list, unsigned int* count, bool want, unsigned int val) {
+    const unsigned int bal = __ballot_sync(__activemask(), want);
+    if (want) {
+        const int lane = int(threadIdx.x + threadIdx.y * blockDim.x) & 31;
+        const int leader = __ffs(bal) - 1;
+        unsigned int base = 0;
+        if (lane == leader) base = atomicAdd(count, unsigned(__popc(bal)));
+        base = __shfl_sync(bal, base, leader);
+        list[base + __popc(bal & ((1u << lane) - 1u))] = val;
+    }
+}
+
+// Bulk pass: faces whose stencil no boundary rule reaches and whose donor cells' old fractions are all
+// one pure phase (for every component) take the short path below; every other cell goes to the list.
+// No out-of-line calls and no local arrays on this path.
+template <int LIM>
+__global__ void __launch_bounds__(256, 5) momflux_ff_bulk(FluxCtx F, FluxFF Q, const float2* __restrict__ us,
+                                                          float2* __restrict__ Phi, unsigned int* __restrict__ list,
+                                                          unsigned int* __restrict__ count) {
+    const Grid& g = F.k.g;
+    SPLIT_XYZ
+    const int j = F.j;
+    bool in_range = true, inner = true;
+    {
+        const int c[3] = {x, y, z};
+#pragma unroll
+        for (int e = 0; e < 3; ++e) {
+            if (e >= g.D) break;
+            const int hi = (e == j) ? g.n[e] - 1 : g.n[e] - 2;
+            if (c[e] < 1 || c[e] > hi) in_range = false;
+            if (c[e] < 3 || c[e] > g.n[e] - 3) inner = false;
+        }
+    }
+    const long long K = lin(g, x, y, z);
+    bool defer = in_range && !inner;
+    if (in_range && inner) {
+        const long long sj = g.s[j];
+        const ff rK = ff_split(F.rj[K]);
+        ff Psi[3];
+        long long P[3];
+        unsigned long long ph = 0ull;
+        bool pure = true;
+#pragma unroll
+        for (int i = 0; i < 3; ++i) {
+            if (i >= g.D) break;
+            const long long si = g.s[i];
+            Psi[i] = ff_mul(ff_add(rK, ff_split(F.rj[K - si])), Q.half_inv_dt);
+            P[i] = ff_pos(Psi[i]) ? K - sj : K;
+            const unsigned long long a = dbits(F.fold[P[i]]), b = dbits(F.fold[P[i] - si]);
+            if (i == 0) ph = a;
+            pure = pure && a == ph && b == ph && (a == 0ull || a == kOneBits);
+        }
+        if (!pure) {
+            defer = true;
+        } else {
+            const bool light = ph == 0ull;
+            const ff thr = light ? Q.thr_l : Q.thr_1, kl = light ? Q.kl_l : Q.kl_1;
+#pragma unroll
+            for (int i = 0; i < 3; ++i) {
+                if (i >= g.D) break;
+                const float2* u = us + i * g.N;
+                const bool pos = ff_pos(Psi[i]);
+                const ff uu = ldff(u + (pos ? K - 2 * sj : K + sj));
+                const ff cc = ldff(u + (pos ? K - sj : K));
+                const ff dd = ldff(u + (pos ? K : K - sj));
+                const ff m = limiter_corr_ff<LIM>(Q, uu, cc, dd);
+                const ff aP = ff_abs(Psi[i]);
+                const ff v = ff_lt(thr, aP) ? ff_mul(Psi[i], cc) : blend(Psi[i], ff_mul(aP, kl), cc, m);
+                stff(Phi + K + i * g.N, v);
+            }
+        }
+    }
+    list_append(list, count, defer, (unsigned int)K);
+}
+
+template <int LIM>
+__global__ void __launch_bounds__(128) momflux_ff_list(FluxCtx F, FluxFF Q, const float2* __restrict__ us,
+                                                       float2* __restrict__ Phi, const unsigned int* __restrict__ list,
+                                                       const unsigned int* __restrict__ count) {
+    const unsigned int n = *count;
+    for (unsigned int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
+        int c[3];
+        coords3(F.k.g, list[k], c);
+        momflux_ff_cell<LIM>(F, Q, us, Phi, c[0], c[1], c[2]);
     }
 }
 
@@ -355,32 +444,32 @@ __device__ __noinline__ void viscflux_ff_mixed(const ViscCtx& V, const ViscFF& W
         }
 }
 
+// Bulk pass: cells whose faces and edges no boundary rule reaches and whose viscosities all read one pure
+// phase; every other cell goes to the list (mixed viscosities or boundary rules, viscflux_ff_list)
 template <int D>
-__global__ void __launch_bounds__(256, 4) viscflux_ff_kern(ViscCtx V, ViscFF W, float2* __restrict__ Phi6) {
+__global__ void __launch_bounds__(256, 4) viscflux_ff_bulk(ViscCtx V, ViscFF W, float2* __restrict__ Phi6,
+                                                           unsigned int* __restrict__ list,
+                                                           unsigned int* __restrict__ count) {
     const Grid& g = V.k.g;
     SPLIT_XYZ
-    const int c[3] = {x, y, z};
     const long long K = lin(g, x, y, z);
-    bool inner = true;
-#pragma unroll
-    for (int e = 0; e < D; ++e)
-        if (c[e] < 3 || c[e] > g.n[e] - 3) inner = false;
+    bool inner = x >= 3 && x <= g.n[0] - 3 && y >= 3 && y <= g.n[1] - 3;
+    if (D == 3) inner = inner && z >= 3 && z <= g.n[2] - 3;
+    bool pure = false;
+    unsigned long long b0 = 0ull;
     if (inner) {
-        // the fractions any of the D(D+1)/2 viscosities reads (get_mu_inner: K, K-s_e, K-2s_e, K-s_i-s_j):
-        // when all are the same pure phase, every viscosity is that phase's constant
+        // the fractions any of the D(D+1)/2 viscosities reads (get_mu_inner: K, K-s_e, K-2s_e, K-s_i-s_j)
         const double* f = V.f;
-        const unsigned long long b0 = dbits(f[K]);
-        bool pure = b0 == 0ull || b0 == kOneBits;
+        b0 = dbits(f[K]);
+        pure = b0 == 0ull || b0 == kOneBits;
 #pragma unroll
         for (int e = 0; e < D; ++e) pure = pure && dbits(f[K - g.s[e]]) == b0 && dbits(f[K - 2 * g.s[e]]) == b0;
 #pragma unroll
-        for (int i = 0; i < D; ++i)
+        for (int a = 0; a < D; ++a)
 #pragma unroll
-            for (int j = i + 1; j < D; ++j) pure = pure && dbits(f[K - g.s[i] - g.s[j]]) == b0;
-        if (!pure) {   // interface cells (a few percent): per-face viscosities, out of line
-            viscflux_ff_mixed<D>(V, W, Phi6, c, K);
-            return;
-        }
+            for (int b = a + 1; b < D; ++b) pure = pure && dbits(f[K - g.s[a] - g.s[b]]) == b0;
+    }
+    if (pure) {
         const ff mu = b0 == 0ull ? W.mu_face0 : W.mu_face1;
         ff uK[D];
 #pragma unroll
@@ -394,9 +483,26 @@ __global__ void __launch_bounds__(256, 4) viscflux_ff_kern(ViscCtx V, ViscFF W, 
                 const ff s2 = (i == j) ? ff_scale2(sji, 2.0f) : ff_add(sji, ff_sub(uK[j], ff_split(V.u[K - g.s[i] + j * g.N])));
                 stff(Phi6 + pair_index(D, i, j) * g.N + K, -ff_mul(mu, s2));
             }
-        return;
     }
-    viscflux_ff_edge<D>(V, W, Phi6, c, K);
+    list_append(list, count, !pure, (unsigned int)K);
+}
+
+template <int D>
+__global__ void __launch_bounds__(128) viscflux_ff_list(ViscCtx V, ViscFF W, float2* __restrict__ Phi6,
+                                                        const unsigned int* __restrict__ list,
+                                                        const unsigned int* __restrict__ count) {
+    const Grid& g = V.k.g;
+    const unsigned int n = *count;
+    for (unsigned int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
+        const long long K = list[k];
+        int c[3];
+        coords3(g, K, c);
+        bool inner = true;
+        for (int e = 0; e < D; ++e)
+            if (c[e] < 3 || c[e] > g.n[e] - 3) inner = false;
+        if (inner) viscflux_ff_mixed<D>(V, W, Phi6, c, K);
+        else viscflux_ff_edge<D>(V, W, Phi6, c, K);
+    }
 }
 
 template <int D>
@@ -468,25 +574,6 @@ __global__ void div_scale_ff_kern(Grid g, const double* __restrict__ u, double* 
     zz[I] = ff_join(s);
 }
 
-// u -= L ∂x on interior cells (src/flow.jl:332)
-template <int D>
-__global__ void correct_ff_kern(Grid g, double* __restrict__ u, const double* __restrict__ L,
-                                const double* __restrict__ xx) {
-    ICELL_XYZ
-    const long long I = lin(g, x, y, z);
-    const ff xI = ff_split(xx[I]);
-    double uv[D], Lv[D], xm[D];
-#pragma unroll
-    for (int i = 0; i < D; ++i) {
-        uv[i] = u[I + i * g.N];
-        Lv[i] = L[I + i * g.N];
-        xm[i] = xx[I - g.s[i]];
-    }
-#pragma unroll
-    for (int i = 0; i < D; ++i)
-        u[I + i * g.N] = ff_join(ff_sub(ff_split(uv[i]), ff_mul(ff_split(Lv[i]), ff_sub(xI, ff_split(xm[i])))));
-}
-
 __device__ __forceinline__ unsigned long long nonneg_bits_ff(double v) {
     const unsigned long long b = dbits(v);
     return (b == 0x8000000000000000ull) ? 0ull : b;
@@ -555,7 +642,8 @@ cudaError_t k_ustar_ff(const MomConsts& k, const double* rhou, const double* f, 
 }
 
 cudaError_t k_momflux_ff(const MomConsts& k, int j, int limiter, const float2* ustar, const double* rhouf_j,
-                         const double* fold, double dt, float2* Phi, cudaStream_t s) {
+                         const double* fold, double dt, float2* Phi, unsigned int* list, unsigned int* count,
+                         int list_blocks, cudaStream_t s) {
     FluxCtx F;
     F.k = k;
     F.j = j;
@@ -579,16 +667,24 @@ cudaError_t k_momflux_ff(const MomConsts& k, int j, int limiter, const float2* u
     Q.kl_1 = ff_split(F.kl_1);
     Q.sixth = ff_split(1.0 / 6.0);
     const dim3 gr = split_grid(k.g);
-    switch (limiter) {
-        case IA_LIMITER_UPWIND: { momflux_ff_kern<IA_LIMITER_UPWIND><<<gr, blk(), 0, s>>>(F, Q, ustar, Phi); ia::note_launch(); } break;
-        case IA_LIMITER_MINMOD: { momflux_ff_kern<IA_LIMITER_MINMOD><<<gr, blk(), 0, s>>>(F, Q, ustar, Phi); ia::note_launch(); } break;
-        case IA_LIMITER_VANALBADA1: { momflux_ff_kern<IA_LIMITER_VANALBADA1><<<gr, blk(), 0, s>>>(F, Q, ustar, Phi); ia::note_launch(); } break;
-        case IA_LIMITER_SWEBY: { momflux_ff_kern<IA_LIMITER_SWEBY><<<gr, blk(), 0, s>>>(F, Q, ustar, Phi); ia::note_launch(); } break;
-        case IA_LIMITER_SUPERBEE: { momflux_ff_kern<IA_LIMITER_SUPERBEE><<<gr, blk(), 0, s>>>(F, Q, ustar, Phi); ia::note_launch(); } break;
-        case IA_LIMITER_TVDCEN: { momflux_ff_kern<IA_LIMITER_TVDCEN><<<gr, blk(), 0, s>>>(F, Q, ustar, Phi); ia::note_launch(); } break;
-        case IA_LIMITER_TVDDOWN: { momflux_ff_kern<IA_LIMITER_TVDDOWN><<<gr, blk(), 0, s>>>(F, Q, ustar, Phi); ia::note_launch(); } break;
-        default: { momflux_ff_kern<IA_LIMITER_KOREN><<<gr, blk(), 0, s>>>(F, Q, ustar, Phi); ia::note_launch(); } break;
+    if (cudaMemsetAsync(count, 0, sizeof(unsigned int), s) != cudaSuccess) return cudaGetLastError();
+#define MF_FF(L_)                                                                                         \
+    {                                                                                                     \
+        momflux_ff_bulk<L_><<<gr, blk(), 0, s>>>(F, Q, ustar, Phi, list, count);                         \
+        momflux_ff_list<L_><<<list_blocks, 128, 0, s>>>(F, Q, ustar, Phi, list, count);                  \
+        ia::note_launches(2);                                                                             \
     }
+    switch (limiter) {
+        case IA_LIMITER_UPWIND: MF_FF(IA_LIMITER_UPWIND) break;
+        case IA_LIMITER_MINMOD: MF_FF(IA_LIMITER_MINMOD) break;
+        case IA_LIMITER_VANALBADA1: MF_FF(IA_LIMITER_VANALBADA1) break;
+        case IA_LIMITER_SWEBY: MF_FF(IA_LIMITER_SWEBY) break;
+        case IA_LIMITER_SUPERBEE: MF_FF(IA_LIMITER_SUPERBEE) break;
+        case IA_LIMITER_TVDCEN: MF_FF(IA_LIMITER_TVDCEN) break;
+        case IA_LIMITER_TVDDOWN: MF_FF(IA_LIMITER_TVDDOWN) break;
+        default: MF_FF(IA_LIMITER_KOREN) break;
+    }
+#undef MF_FF
     return cudaGetLastError();
 }
 
@@ -602,7 +698,7 @@ cudaError_t k_momupdate_ff(const MomConsts& k, int j, const float2* Phi, const f
 }
 
 cudaError_t k_visc_ff(const MomConsts& k, const double* u, const double* f, double lmu, double mu, float2* Phi6,
-                      double* r, cudaStream_t s) {
+                      double* r, unsigned int* list, unsigned int* count, int list_blocks, cudaStream_t s) {
     ViscCtx V;
     V.k = k;
     V.u = u;
@@ -623,11 +719,14 @@ cudaError_t k_visc_ff(const MomConsts& k, const double* u, const double* f, doub
     std::memcpy(&W.mu1bits, &V.mu_face1, 8);
     W.mu_face0 = ff_split(V.mu_face0);
     W.mu_face1 = ff_split(V.mu_face1);
+    if (cudaMemsetAsync(count, 0, sizeof(unsigned int), s) != cudaSuccess) return cudaGetLastError();
     if (k.g.D == 3) {
-        { viscflux_ff_kern<3><<<split_grid(k.g), blk(), 0, s>>>(V, W, Phi6); ia::note_launch(); }
+        { viscflux_ff_bulk<3><<<split_grid(k.g), blk(), 0, s>>>(V, W, Phi6, list, count); ia::note_launch(); }
+        { viscflux_ff_list<3><<<list_blocks, 128, 0, s>>>(V, W, Phi6, list, count); ia::note_launch(); }
         { viscacc_ff_kern<3><<<igrd(k.g), blk(), 0, s>>>(k.g, Phi6, r); ia::note_launch(); }
     } else {
-        { viscflux_ff_kern<2><<<split_grid(k.g), blk(), 0, s>>>(V, W, Phi6); ia::note_launch(); }
+        { viscflux_ff_bulk<2><<<split_grid(k.g), blk(), 0, s>>>(V, W, Phi6, list, count); ia::note_launch(); }
+        { viscflux_ff_list<2><<<list_blocks, 128, 0, s>>>(V, W, Phi6, list, count); ia::note_launch(); }
         { viscacc_ff_kern<2><<<igrd(k.g), blk(), 0, s>>>(k.g, Phi6, r); ia::note_launch(); }
     }
     return cudaGetLastError();
@@ -654,11 +753,6 @@ cudaError_t k_div_scale_ff(const MomConsts& k, const double* u, double* zz, doub
     if (k.g.D == 3) { div_scale_ff_kern<3><<<ggrd(k.g), blk(), 0, s>>>(k.g, u, zz, xx, dt); ia::note_launch(); }
     else { div_scale_ff_kern<2><<<ggrd(k.g), blk(), 0, s>>>(k.g, u, zz, xx, dt); ia::note_launch(); }
     return cudaGetLastError();
-}
-cudaError_t k_correct_ff(const MomConsts& k, double* u, const double* L, double* xx, double dt, cudaStream_t s) {
-    if (k.g.D == 3) { correct_ff_kern<3><<<igrd(k.g), blk(), 0, s>>>(k.g, u, L, xx); ia::note_launch(); }
-    else { correct_ff_kern<2><<<igrd(k.g), blk(), 0, s>>>(k.g, u, L, xx); ia::note_launch(); }
-    return k_scale(xx, k.g.N, 1.0 / dt, s);
 }
 cudaError_t k_cfl_ff(const MomConsts& k, const double* u, unsigned long long* out2, cudaStream_t s) {
     const long long rows = (long long)(k.g.n[1] - 2) * (k.g.D == 3 ? k.g.n[2] - 2 : 1);

@@ -21,6 +21,7 @@ struct MomScratch {
     double* ft1 = nullptr;     // out-of-place VOF sweep buffers
     double* ft2 = nullptr;
     double* dq = nullptr;      // dilation term of the float-float momentum update (N FP32 pairs)
+    unsigned int* lcount = nullptr;   // length of the cell list a float-float bulk pass leaves (in slist)
     unsigned long long* cfl = nullptr;   // device max reductions (2)
     unsigned long long* hcfl = nullptr;  // pinned host copy
 };
@@ -68,6 +69,7 @@ static int ensure_scratch(ia_handle* h) {
     e = e ? e : cudaMalloc(&m->ft1, 8 * N);
     e = e ? e : cudaMalloc(&m->ft2, 8 * N);
     e = e ? e : cudaMalloc(&m->dq, 8 * N);
+    e = e ? e : cudaMalloc(&m->lcount, sizeof(unsigned int));
     e = e ? e : cudaMalloc(&m->cfl, 16);
     e = e ? e : cudaMallocHost(&m->hcfl, 16);
     if (e != cudaSuccess) return IA_ERR_CUDA;
@@ -90,6 +92,7 @@ void extra_destroy(ia_handle* h) {
     cudaFree(m->ft1);
     cudaFree(m->ft2);
     cudaFree(m->dq);
+    cudaFree(m->lcount);
     cudaFree(m->cfl);
     if (m->hcfl) cudaFreeHost(m->hcfl);
     delete m;
@@ -125,7 +128,9 @@ static int advect_fq(ia_handle* h, double* f, const double* u1, const double* u2
         if (rc != IA_OK) return rc;
         const double* rj = h->fld.rhouf + (long long)d * g.N;
         tk = timing_begin(h, TK_MOM_FLUX);
-        e = ff ? k_momflux_ff(k, d, h->cfg.limiter, us2, rj, fin, dt, Phi2, st)
+        // the surface-tension lists are rebuilt after the sweeps: their buffer holds this pass's list
+        unsigned int* lst = reinterpret_cast<unsigned int*>(m->slist);
+        e = ff ? k_momflux_ff(k, d, h->cfg.limiter, us2, rj, fin, dt, Phi2, lst, m->lcount, h->list_blocks, st)
                : k_momflux(k, d, h->cfg.limiter, m->ustar, rj, fin, dt, m->Phi, st);
         if (e != cudaSuccess) return IA_ERR_CUDA;
         timing_end(h, tk);
@@ -147,7 +152,8 @@ static int visc_surften(ia_handle* h, const double* f) {
     int tk = timing_begin(h, TK_FORCE);
     cudaError_t e;
     if (h->cfg.mu != 0.0 && use_ff(h))
-        e = k_visc_ff(k, h->fld.u, f, h->cfg.lmu, h->cfg.mu, reinterpret_cast<float2*>(m->Phi6), h->fld.force, st);
+        e = k_visc_ff(k, h->fld.u, f, h->cfg.lmu, h->cfg.mu, reinterpret_cast<float2*>(m->Phi6), h->fld.force,
+                      reinterpret_cast<unsigned int*>(m->slist), m->lcount, h->list_blocks, st);
     else if (h->cfg.mu != 0.0) e = k_visc(k, h->fld.u, f, h->cfg.lmu, h->cfg.mu, m->Phi6, h->fld.force, st);
     else e = k_zero(h->fld.force, g.N * g.D, st);
     if (e != cudaSuccess) return IA_ERR_CUDA;
@@ -174,9 +180,7 @@ static int project(ia_handle* h, const double* f, double dtp, int* iters, double
                            resid);
     if (rc != IA_OK && rc != IA_WARN_NOT_CONVERGED) return rc;
     tk = timing_begin(h, TK_UPDATE);
-    if ((use_ff(h) ? k_correct_ff(k, h->fld.u, h->fld.mu0, h->fld.p, dtp, st)
-                   : k_correct(k, h->fld.u, h->fld.mu0, h->fld.p, dtp, st)) != cudaSuccess)
-        return IA_ERR_CUDA;
+    if (k_correct(k, h->fld.u, h->fld.mu0, h->fld.p, dtp, st) != cudaSuccess) return IA_ERR_CUDA;
     const double zero[3] = {h->cfg.uBC[0], h->cfg.uBC[1], h->cfg.uBC[2]};
     if (k_bc_vel(k, h->fld.u, zero, st) != cudaSuccess) return IA_ERR_CUDA;
     timing_end(h, tk);
