@@ -342,6 +342,13 @@ int ia_poisson_smoother(ia_handle* h, int32_t kind);
  * iterations per step; 1 is plain Gauss-Seidel); the coarsest-level sweeps stay at 1.  The blocked
  * smoother runs only at omega = 1 (the half-sweeps are used otherwise) */
 int ia_poisson_mg_relax(ia_handle* h, double omega);
+/* coefficient storage of the finest level's V-cycle smoother in the MIXED / LEARNED modes (no reference
+ * counterpart): 1 = an FP16 copy of the FP32 face coefficients (relative precision 2^-11) for the
+ * red-black half-sweeps and the residual restriction of that level, 0 = the FP32 coefficients.  The inner
+ * FCG's operator, the coarse levels and the FP64 defect correction are not affected, so the solve still
+ * stops on the FP64 true residual.  Default 1 when the coefficients 1/ρ (between 1/max(λρ,1) and
+ * 1/min(λρ,1)) fit FP16's range, which IA_ERR_UNSUPPORTED reports otherwise. */
+int ia_poisson_coef16(ia_handle* h, int32_t on);
 /* counters since the handle's creation: [0] net applications, [1] V-cycles, [2] fallbacks
  * to the V-cycle, [3] inner FCG iterations, [4] outer corrections */
 int ia_poisson_stats(ia_handle* h, int64_t* out5);

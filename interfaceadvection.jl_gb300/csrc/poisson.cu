@@ -57,6 +57,11 @@ __device__ __forceinline__ T offdiag(const Grid& g, const T* L, const T* x, long
     return a;
 }
 
+// face coefficient as the arithmetic type of the sweep (the finest mixed level may store them as FP16)
+__device__ __forceinline__ float cf(float v) { return v; }
+__device__ __forceinline__ double cf(double v) { return v; }
+__device__ __forceinline__ float cf(__half v) { return __half2float(v); }
+
 // ---- dimension-specialised stencil with 32-bit cell offsets (a grid holds < 2^31 cells)
 struct Nb {
     int xl, xh, yl, yh, zl, zh;   // offsets of the six neighbours; periodic ends wrap
@@ -77,29 +82,30 @@ __device__ __forceinline__ Nb nb_of(const Grid& g, int x, int y, int z) {
     return o;
 }
 // Σ_i L[I,i] v[I-δi] + L[I+δi,i] v[I+δi]  (same order as offdiag)
-template <int D, class T>
-__device__ __forceinline__ T off7(const Grid& g, const T* __restrict__ L, const T* v, int I, const Nb& o) {
+template <int D, class T, class TL>
+__device__ __forceinline__ T off7(const Grid& g, const TL* __restrict__ L, const T* v, int I, const Nb& o) {
     const int s1 = int(g.s[1]), s2 = int(g.s[2]);
-    const T* L1 = L + g.N;
-    T a = L[I] * v[I + o.xl] + L[I + 1] * v[I + o.xh];
-    a += L1[I] * v[I + o.yl] + L1[I + s1] * v[I + o.yh];
+    const TL* L1 = L + g.N;
+    T a = cf(L[I]) * v[I + o.xl] + cf(L[I + 1]) * v[I + o.xh];
+    a += cf(L1[I]) * v[I + o.yl] + cf(L1[I + s1]) * v[I + o.yh];
     if (D == 3) {
-        const T* L2 = L1 + g.N;
-        a += L2[I] * v[I + o.zl] + L2[I + s2] * v[I + o.zh];
+        const TL* L2 = L1 + g.N;
+        a += cf(L2[I]) * v[I + o.zl] + cf(L2[I + s2]) * v[I + o.zh];
     }
     return a;
 }
 // D_I = -Σ_i (L[I,i] + L[I+δi,i])
-template <int D, class T>
-__device__ __forceinline__ T diag7(const Grid& g, const T* __restrict__ L, int I) {
+template <int D, class TL>
+__device__ __forceinline__ auto diag7(const Grid& g, const TL* __restrict__ L, int I) -> decltype(cf(L[0])) {
+    using T = decltype(cf(L[0]));
     const int s1 = int(g.s[1]), s2 = int(g.s[2]);
-    const T* L1 = L + g.N;
+    const TL* L1 = L + g.N;
     T dd = T(0);
-    dd -= L[I] + L[I + 1];
-    dd -= L1[I] + L1[I + s1];
+    dd -= cf(L[I]) + cf(L[I + 1]);
+    dd -= cf(L1[I]) + cf(L1[I + s1]);
     if (D == 3) {
-        const T* L2 = L1 + g.N;
-        dd -= L2[I] + L2[I + s2];
+        const TL* L2 = L1 + g.N;
+        dd -= cf(L2[I]) + cf(L2[I + s2]);
     }
     return dd;
 }
@@ -175,8 +181,8 @@ __global__ void restrict_L_k(Grid gc, Grid gf, const T* __restrict__ Lf, T* __re
 // (same value and zero-diagonal rule as set_diag_k).
 // With PROL (over-relaxed first red half-sweep of a post-smoothing whose prolongation is fused
 // into the sweeps) the cell's previous value is x + the injected coarse correction.
-template <class T, int D, bool PROL = false>
-__global__ void rbgs_pair_k(Grid g, const T* __restrict__ L, const T* __restrict__ b, T* __restrict__ xv,
+template <class T, int D, bool PROL = false, class TL = T>
+__global__ void rbgs_pair_k(Grid g, const TL* __restrict__ L, const T* __restrict__ b, T* __restrict__ xv,
                             int color, T omega, Grid gc = Grid(), const T* __restrict__ xc = nullptr) {
     const int y = 1 + blockIdx.y * blockDim.y + threadIdx.y;
     const int z = D == 3 ? 1 + int(blockIdx.z) : 0;
@@ -218,8 +224,8 @@ __device__ __forceinline__ T first_nb(const Grid& g, const Grid& gc, const T* __
     return omega == T(1) ? b[J] * iD[J] : omega * (b[J] * iD[J]);
 }
 
-template <class T, int D, bool PROL>
-__global__ void rbgs_first_k(Grid g, Grid gc, const T* __restrict__ L, const T* __restrict__ b,
+template <class T, int D, bool PROL, class TL = T>
+__global__ void rbgs_first_k(Grid g, Grid gc, const TL* __restrict__ L, const T* __restrict__ b,
                              const T* __restrict__ iD, const T* __restrict__ xc, T* __restrict__ xv, int write_red,
                              T omega) {
     const int y = 1 + blockIdx.y * blockDim.y + threadIdx.y;
@@ -235,8 +241,8 @@ __global__ void rbgs_first_k(Grid g, Grid gc, const T* __restrict__ L, const T* 
     }
     if (x > g.n[0] - 2) return;
     const int I = x + y * s1 + z * s2;
-    const T* L1 = L + g.N;
-    const T* L2 = L1 + g.N;
+    const TL* L1 = L + g.N;
+    const TL* L2 = L1 + g.N;
     // the six neighbour values, then one shared accumulation (the same sums in the same order
     // whichever way the values were found)
     T v[6] = {T(0), T(0), T(0), T(0), T(0), T(0)};
@@ -269,9 +275,9 @@ __global__ void rbgs_first_k(Grid g, Grid gc, const T* __restrict__ L, const T* 
             v[5] = first_nb<T, PROL>(g, gc, b, iD, xc, xv, I + o.zh, x, y, zh, omega);
         }
     }
-    T a = L[I] * v[0] + L[I + 1] * v[1];
-    a += L1[I] * v[2] + L1[I + s1] * v[3];
-    if (D == 3) a += L2[I] * v[4] + L2[I + s2] * v[5];
+    T a = cf(L[I]) * v[0] + cf(L[I + 1]) * v[1];
+    a += cf(L1[I]) * v[2] + cf(L1[I + s1]) * v[3];
+    if (D == 3) a += cf(L2[I]) * v[4] + cf(L2[I + s2]) * v[5];
     const T dd = diag7<D>(g, L, I);
     const T eps = sizeof(T) == 8 ? T(2.220446049250313e-16) : T(1.1920929e-7);
     const T iDI = (dd * dd < T(2) * eps) ? T(0) : T(1) / dd;
@@ -491,8 +497,8 @@ __global__ void residual_k(Grid g, const T* __restrict__ L, const T* __restrict_
 
 // residual of the 2^D fine children of each coarse cell, summed straight into the coarse
 // right-hand side (residual_k + restrict_k without the fine residual array; same sums, same order)
-template <class T, int D>
-__global__ void resid_restrict_k(Grid gc, Grid gf, const T* __restrict__ L, const T* __restrict__ b,
+template <class T, int D, class TL = T>
+__global__ void resid_restrict_k(Grid gc, Grid gf, const TL* __restrict__ L, const T* __restrict__ b,
                                  const T* __restrict__ xv, T* __restrict__ bc) {
     const int xc = 1 + blockIdx.x * blockDim.x + threadIdx.x;
     const int yc = 1 + blockIdx.y * blockDim.y + threadIdx.y;
@@ -578,6 +584,10 @@ template <class T>
 __global__ void zero_k(long long n, T* a) {
     for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < n; q += (long long)gridDim.x * blockDim.x)
         a[q] = T(0);
+}
+__global__ void to_f16_k(long long n, const float* __restrict__ a, __half* __restrict__ b) {
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+        b[i] = __float2half_rn(a[i]);
 }
 __global__ void to_f32_k(long long n, const double* __restrict__ a, float* __restrict__ b) {
     for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < n; q += (long long)gridDim.x * blockDim.x)
@@ -1013,10 +1023,19 @@ static cudaError_t vcycle(ia_handle* h, PoissonMG* mg, int l, cudaStream_t st, i
             return cudaGetLastError();
         }
     }
+    // the finest mixed level's half-sweeps and residual restriction read the FP16 coefficient copy
+    const __half* L16 = nullptr;
+    if constexpr (sizeof(T) == 4) L16 = (l == 0 && mg->coef16) ? L.L16 : nullptr;
     auto half = [&](int color) {
         const int tk = (l == 0) ? timing_begin(h, TK_MG_FINE) : -1;
-        if (L.g.D == 3) { rbgs_pair_k<T, 3><<<pair_grid(L.g), blk(), 0, st>>>(L.g, Lc, b, x, color, T(mg->omega)); ia::note_launch(); }
-        else { rbgs_pair_k<T, 2><<<pair_grid(L.g), blk(), 0, st>>>(L.g, Lc, b, x, color, T(mg->omega)); ia::note_launch(); }
+        if (L16) {
+            if (L.g.D == 3) rbgs_pair_k<T, 3, false, __half><<<pair_grid(L.g), blk(), 0, st>>>(L.g, L16, b, x, color, T(mg->omega));
+            else rbgs_pair_k<T, 2, false, __half><<<pair_grid(L.g), blk(), 0, st>>>(L.g, L16, b, x, color, T(mg->omega));
+        } else {
+            if (L.g.D == 3) rbgs_pair_k<T, 3><<<pair_grid(L.g), blk(), 0, st>>>(L.g, Lc, b, x, color, T(mg->omega));
+            else rbgs_pair_k<T, 2><<<pair_grid(L.g), blk(), 0, st>>>(L.g, Lc, b, x, color, T(mg->omega));
+        }
+        ia::note_launch();
         timing_end(h, tk);
     };
     auto& C = mg->lev[l + 1];
@@ -1029,7 +1048,13 @@ static cudaError_t vcycle(ia_handle* h, PoissonMG* mg, int l, cudaStream_t st, i
     auto first = [&](bool prol) {
         const int tk = (l == 0) ? timing_begin(h, TK_MG_FIRST) : -1;
         const T* xc = C.template x_<T>();
-        if (L.g.D == 3) {
+        if (L16 && L.g.D == 3) {
+            if (prol) rbgs_first_k<T, 3, true, __half><<<pair_grid(L.g), blk(), 0, st>>>(L.g, C.g, L16, b, iD, xc, x, 0, T(mg->omega));
+            else rbgs_first_k<T, 3, false, __half><<<pair_grid(L.g), blk(), 0, st>>>(L.g, C.g, L16, b, iD, xc, x, write_red, T(mg->omega));
+        } else if (L16) {
+            if (prol) rbgs_first_k<T, 2, true, __half><<<pair_grid(L.g), blk(), 0, st>>>(L.g, C.g, L16, b, iD, xc, x, 0, T(mg->omega));
+            else rbgs_first_k<T, 2, false, __half><<<pair_grid(L.g), blk(), 0, st>>>(L.g, C.g, L16, b, iD, xc, x, write_red, T(mg->omega));
+        } else if (L.g.D == 3) {
             if (prol) rbgs_first_k<T, 3, true><<<pair_grid(L.g), blk(), 0, st>>>(L.g, C.g, Lc, b, iD, xc, x, 0, T(mg->omega));
             else rbgs_first_k<T, 3, false><<<pair_grid(L.g), blk(), 0, st>>>(L.g, C.g, Lc, b, iD, xc, x, write_red, T(mg->omega));
         } else {
@@ -1044,8 +1069,11 @@ static cudaError_t vcycle(ia_handle* h, PoissonMG* mg, int l, cudaStream_t st, i
         half(0);
         half(1);
     }
-    if (L.g.D == 3) { resid_restrict_k<T, 3><<<cell_grid(C.g), blk(), 0, st>>>(C.g, L.g, Lc, b, x, C.template b_<T>()); ia::note_launch(); }
-    else { resid_restrict_k<T, 2><<<cell_grid(C.g), blk(), 0, st>>>(C.g, L.g, Lc, b, x, C.template b_<T>()); ia::note_launch(); }
+    if (L16 && L.g.D == 3) resid_restrict_k<T, 3, __half><<<cell_grid(C.g), blk(), 0, st>>>(C.g, L.g, L16, b, x, C.template b_<T>());
+    else if (L16) resid_restrict_k<T, 2, __half><<<cell_grid(C.g), blk(), 0, st>>>(C.g, L.g, L16, b, x, C.template b_<T>());
+    else if (L.g.D == 3) resid_restrict_k<T, 3><<<cell_grid(C.g), blk(), 0, st>>>(C.g, L.g, Lc, b, x, C.template b_<T>());
+    else resid_restrict_k<T, 2><<<cell_grid(C.g), blk(), 0, st>>>(C.g, L.g, Lc, b, x, C.template b_<T>());
+    ia::note_launch();
     cudaError_t e = vcycle<T>(h, mg, l + 1, st, nu1, nu2, nuc);
     if (e != cudaSuccess) return e;
     if (nu2 == 0) {
@@ -1056,7 +1084,9 @@ static cudaError_t vcycle(ia_handle* h, PoissonMG* mg, int l, cudaStream_t st, i
     if (relax) {   // the red cells still hold x without the coarse correction
         const int tk = (l == 0) ? timing_begin(h, TK_MG_FINE) : -1;
         const T* xc = C.template x_<T>();
-        if (L.g.D == 3) rbgs_pair_k<T, 3, true><<<pair_grid(L.g), blk(), 0, st>>>(L.g, Lc, b, x, 0, T(mg->omega), C.g, xc);
+        if (L16 && L.g.D == 3) rbgs_pair_k<T, 3, true, __half><<<pair_grid(L.g), blk(), 0, st>>>(L.g, L16, b, x, 0, T(mg->omega), C.g, xc);
+        else if (L16) rbgs_pair_k<T, 2, true, __half><<<pair_grid(L.g), blk(), 0, st>>>(L.g, L16, b, x, 0, T(mg->omega), C.g, xc);
+        else if (L.g.D == 3) rbgs_pair_k<T, 3, true><<<pair_grid(L.g), blk(), 0, st>>>(L.g, Lc, b, x, 0, T(mg->omega), C.g, xc);
         else rbgs_pair_k<T, 2, true><<<pair_grid(L.g), blk(), 0, st>>>(L.g, Lc, b, x, 0, T(mg->omega), C.g, xc);
         ia::note_launch();
         timing_end(h, tk);
@@ -1077,7 +1107,7 @@ static cudaError_t vcycle_run(ia_handle* h, PoissonMG* mg, cudaStream_t st) {
     const int k = sizeof(T) == 4 ? 0 : 1;
     int* nu = mg->vgraph_nu[k];
     if (mg->vgraph[k] && (nu[0] != mg->nu1 || nu[1] != mg->nu2 || nu[2] != mg->nuc || nu[3] != mg->smoother ||
-                          mg->vgraph_omega[k] != mg->omega)) {
+                          mg->vgraph_omega[k] != mg->omega || mg->vgraph_c16[k] != mg->coef16)) {
         cudaGraphExecDestroy(mg->vgraph[k]);
         mg->vgraph[k] = nullptr;
     }
@@ -1107,9 +1137,17 @@ static cudaError_t vcycle_run(ia_handle* h, PoissonMG* mg, cudaStream_t st) {
         nu[2] = mg->nuc;
         nu[3] = mg->smoother;
         mg->vgraph_omega[k] = mg->omega;
+        mg->vgraph_c16[k] = mg->coef16;
     }
     note_launches(mg->vgraph_kernels[k]);
     return cudaGraphLaunch(mg->vgraph[k], st);
+}
+
+// the finest-level coefficients L = 1/ρ_face lie in [1/max(λρ,1), 1/min(λρ,1)] (0 on wall faces): FP16
+// holds them (relative precision 2^-11) when that interval lies inside its normal range
+bool coef16_fits(double lrho) {
+    const double lo = lrho < 1.0 ? lrho : 1.0, hi = lrho < 1.0 ? 1.0 : lrho;
+    return lo > 0.0 && 1.0 / lo <= 60000.0 && 1.0 / hi >= 1e-4;
 }
 
 int mg_create(ia_handle* h) {
@@ -1118,6 +1156,7 @@ int mg_create(ia_handle* h) {
     const Grid& g0 = h->g;
     long long Nint[3] = {g0.n[0] - 2, g0.n[1] - 2, g0.D == 3 ? g0.n[2] - 2 : 1};
     const bool mixed = h->cfg.poisson_mode != IA_POISSON_FP64;
+    mg->coef16 = (mixed && coef16_fits(h->cfg.lrho)) ? 1 : 0;
     int nl = 0;
     while (nl < MG_MAX_LEVELS) {
         int64_t N[3] = {Nint[0], Nint[1], Nint[2]};
@@ -1145,6 +1184,7 @@ int mg_create(ia_handle* h) {
             e = e ? e : cudaMalloc(&L.r32, 4 * n);
             e = e ? e : cudaMalloc(&L.L32, 4 * n * g0.D);
             e = e ? e : cudaMalloc(&L.iD32, 4 * n);
+            if (nl == 0) e = e ? e : cudaMalloc(&L.L16, 2 * n * g0.D);
             if (!e) {
                 cudaMemset(L.x32, 0, 4 * n);
                 cudaMemset(L.b32, 0, 4 * n);
@@ -1218,7 +1258,7 @@ void mg_destroy(ia_handle* h) {
     for (int l = 0; l < MG_MAX_LEVELS; ++l) {
         MGLevel& L = mg->lev[l];
         cudaFree(L.x); cudaFree(L.b); cudaFree(L.r); cudaFree(L.L); cudaFree(L.iD);
-        cudaFree(L.x32); cudaFree(L.b32); cudaFree(L.r32); cudaFree(L.L32); cudaFree(L.iD32);
+        cudaFree(L.x32); cudaFree(L.b32); cudaFree(L.r32); cudaFree(L.L32); cudaFree(L.iD32); cudaFree(L.L16);
     }
     cudaFree(mg->r); cudaFree(mg->s); cudaFree(mg->p); cudaFree(mg->q);
     cudaFree(mg->p32); cudaFree(mg->q32); cudaFree(mg->e32);
@@ -1252,6 +1292,7 @@ static cudaError_t mg_setup(ia_handle* h, const double* L0) {
         // the FP64 -> FP32 conversion runs in a memory-bound pass of its own: conversions issue on
         // the FP64 pipe, which the FP64 diagonal pass already saturates
         { to_f32_k<<<1216, 256, 0, st>>>(nv, L0, F.L32); ia::note_launch(); }
+        if (mg->coef16) { to_f16_k<<<1216, 256, 0, st>>>(nv, F.L32, F.L16); ia::note_launch(); }
         { set_diag_k<float><<<grd(F.g), blk(), 0, st>>>(F.g, F.L32, F.iD32); ia::note_launch(); }
         for (int l = 1; l < mg->nlev; ++l) {
             { restrict_L_k<float><<<grd(mg->lev[l].g), blk(), 0, st>>>(mg->lev[l].g, mg->lev[l - 1].g,

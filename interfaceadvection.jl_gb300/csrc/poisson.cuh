@@ -1,5 +1,6 @@
 // Multigrid hierarchy and Krylov state of the pressure solve (poisson.cu).
 #pragma once
+#include <cuda_fp16.h>
 #include <cuda_runtime.h>
 
 #include "ia_core.cuh"
@@ -16,6 +17,8 @@ struct MGLevel {
     double *x = nullptr, *b = nullptr, *r = nullptr, *L = nullptr, *iD = nullptr;
     // FP32 operator and vectors (IA_POISSON_MIXED)
     float *x32 = nullptr, *b32 = nullptr, *r32 = nullptr, *L32 = nullptr, *iD32 = nullptr;
+    // finest level of the mixed V-cycle: FP16 copy of L32 for the smoother and the residual restriction
+    __half* L16 = nullptr;
     template <class T> T* x_();
     template <class T> T* b_();
     template <class T> T* r_();
@@ -53,6 +56,7 @@ struct PoissonMG {
     int nu1 = 2, nu2 = 2, nuc = 16;
     int smoother = 0;                                                 // IA_SMOOTHER_* (FP32 V-cycle)
     double omega = 1.15;                                              // smoother relaxation factor
+    int coef16 = 0;                                                   // finest-level smoother on L16 (mixed)
     int nsm = 0;                                                      // multiprocessors of the device
     // each precision's finest-level V-cycle is captured once into a CUDA graph (its launch
     // sequence and arguments are fixed for the handle) and replayed; recaptured when the
@@ -61,11 +65,13 @@ struct PoissonMG {
     long long vgraph_kernels[2] = {0, 0};
     int vgraph_nu[2][4] = {{0, 0, 0, 0}, {0, 0, 0, 0}};
     double vgraph_omega[2] = {1.0, 1.0};
+    int vgraph_c16[2] = {0, 0};
     cudaStream_t capture = nullptr;
 };
 
 namespace ia {
 int mg_create(ia_handle* h);
+bool coef16_fits(double lrho);
 void mg_destroy(ia_handle* h);
 int poisson_solve(ia_handle* h, double* x, const double* z, const double* L, double tol, int itmx, int* iters,
                   double* resid);

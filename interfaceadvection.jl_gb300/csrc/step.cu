@@ -377,6 +377,15 @@ int ia_poisson_smoother(ia_handle* h, int32_t kind) {
     return IA_OK;
 }
 
+int ia_poisson_coef16(ia_handle* h, int32_t on) {
+    if (!h || (on != 0 && on != 1)) return IA_ERR_INVALID;
+    if (h->cfg.poisson_mode == IA_POISSON_FP64) return on ? IA_ERR_UNSUPPORTED : IA_OK;
+    if (on && !coef16_fits(h->cfg.lrho)) return IA_ERR_UNSUPPORTED;
+    if (ensure_scratch(h) != IA_OK) return IA_ERR_CUDA;
+    h->mg->coef16 = on;
+    return IA_OK;
+}
+
 int ia_poisson_stats(ia_handle* h, int64_t* out5) {
     if (!h || !out5) return IA_ERR_INVALID;
     for (int i = 0; i < 5; ++i) out5[i] = h->mg ? h->mg->stats[i] : 0;

@@ -109,6 +109,11 @@ def set_momentum_arith(handle, kind: str = "default") -> None:
     _lib.check(handle.call("ia_momentum_arith", C.c_int32(_lib.ARITH[kind])), "ia_momentum_arith")
 
 
+def set_poisson_coef16(handle, on: bool) -> None:
+    """FP16 face coefficients for the finest-level smoother of the mixed V-cycle (ia_poisson_coef16)."""
+    _lib.check(handle.call("ia_poisson_coef16", C.c_int32(1 if on else 0)), "ia_poisson_coef16")
+
+
 def set_smoother(handle, kind: str = "halfsweep", omega: float | None = None) -> None:
     """Smoother of the FP32 V-cycle: "halfsweep" (one launch per red-black half-sweep, the default)
     or "blocked" (all half-sweeps of a smoothing in one z-wavefront launch, relaxation factor 1 only);
