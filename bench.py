@@ -68,6 +68,8 @@ def parse():
     ap.add_argument("--no-secondary", action="store_true", help="skip the side runs")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--ref-steps", type=int, default=2, help="oracle steps timed by the reference arm")
+    ap.add_argument("--no-coef16", action="store_true",
+                    help="FP32 face coefficients in the finest-level smoother of the mixed V-cycle")
     return ap.parse_args()
 
 
@@ -338,6 +340,8 @@ def run_bubble(args, world, local_rank):
     barrier = (lambda: torch.distributed.barrier()) if world > 1 else (lambda: None)
     L = _lib.load()
     sim = make_bubble(N, "mixed", dev)
+    if args.no_coef16:
+        ia.set_poisson_coef16(sim.handle, False)
     m0 = sim.intf.mass()
     for _ in range(args.warmup):
         ia.sim_step(sim)

@@ -7,7 +7,8 @@ iterations and land on the same pressure whichever smoother runs, on periodic
 and wall dimensions, on sizes that are not multiples of the 32 x 16 tile and
 on every level of the hierarchy (relaxation factor 1, where both apply).
 Over-relaxed half-sweeps (the default factor) must reach the same pressure in no
-more iterations.
+more iterations.  These comparisons run on the FP32 face coefficients; the FP16
+copy of the finest level's coefficients is checked on its own at the end.
 """
 import ctypes as C
 
@@ -33,8 +34,10 @@ def system(dims, perdir):
     return sim.flow.mu0.clone(), sim.flow.sigma.clone()
 
 
-def solve(dims, perdir, L, z, smoother, nu=(2, 2), omega=1.0):
+def solve(dims, perdir, L, z, smoother, nu=(2, 2), omega=1.0, coef16=False):
+    # the smoother comparisons run on the FP32 coefficients (the blocked smoother has no FP16 form)
     h = ia.Handle(ia.make_config(dims, perdir=perdir, poisson="mixed", lrho=1e-3))
+    ia.set_poisson_coef16(h, coef16)
     ia.set_smoother(h, smoother, omega)
     _lib.check(h.call("ia_poisson_mg_params", nu[0], nu[1], 16), "ia_poisson_mg_params")
     x = fzeros(z.shape)
