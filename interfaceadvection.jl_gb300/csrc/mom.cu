@@ -350,6 +350,10 @@ __device__ __forceinline__ bool mixed(double v) {
 // d > 0 it is the previous direction's value there (whose own ghost rules send the d coordinate to
 // n-2; every other coordinate is already mapped); for d = 0 it is the last VOF sweep's flux fᶠ, read
 // from prev0 (NULL: zero, which is that flux on the plane whenever the wall's normal velocity is 0).
+// (fa + fm)/2 of a face whose two cells differ; out of line so that pure faces, which take fa, issue no
+// predicated-off FP64 instructions
+__device__ __noinline__ double face_avg(double fa, double fm) { return (fa + fm) / 2.0; }
+
 __device__ __forceinline__ double fbuffer_at(const Grid& g, const double* __restrict__ f, int d, const int c0[3],
                                              const double* __restrict__ prev0) {
     int c[3] = {c0[0], c0[1], c0[2]};
@@ -361,7 +365,7 @@ __device__ __forceinline__ double fbuffer_at(const Grid& g, const double* __rest
     }
     const long long P = lin3(g, c);
     const double fa = f[P], fm = f[P - g.s[dd]];
-    return (dbits(fa) == dbits(fm)) ? fa : (fa + fm) / 2.0;
+    return (dbits(fa) == dbits(fm)) ? fa : face_avg(fa, fm);
 }
 
 // fbuffer along every d in one pass over f, and per d the list of interior cells where it is mixed
@@ -374,8 +378,16 @@ __global__ void fbuffer_kern(MomConsts k, const double* __restrict__ f, const do
     const bool inner = is_interior(g, c0);
     const long long I = lin(g, x, y, z);
     const int lane = int(threadIdx.x) & 31;
+    // interior cells: no ghost or never-written position, the face fractions of this cell directly
+    const bool deep = inner && x <= g.n[0] - 2 && y <= g.n[1] - 2;
     for (int d = 0; d < g.D; ++d) {
-        const double v = fbuffer_at(g, f, d, c0, prev0);
+        double v;
+        if (deep) {
+            const double fa = f[I], fm = f[I - g.s[d]];
+            v = (dbits(fa) == dbits(fm)) ? fa : face_avg(fa, fm);
+        } else {
+            v = fbuffer_at(g, f, d, c0, prev0);
+        }
         fb[d * g.N + I] = v;
         const bool want = inner && mixed(v);
         const unsigned int bal = __ballot_sync(__activemask(), want);

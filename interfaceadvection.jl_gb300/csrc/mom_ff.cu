@@ -318,7 +318,7 @@ __global__ void __launch_bounds__(256, 5) momflux_ff_bulk(FluxCtx F, FluxFF Q, c
     bool defer = in_range && !inner;
     if (in_range && inner) {
         const long long sj = g.s[j];
-        const ff rK = ff_split(F.rj[K]);
+        const double rK = F.rj[K];
         ff Psi[3];
         long long P[3];
         unsigned long long ph = 0ull;
@@ -327,7 +327,9 @@ __global__ void __launch_bounds__(256, 5) momflux_ff_bulk(FluxCtx F, FluxFF Q, c
         for (int i = 0; i < 3; ++i) {
             if (i >= g.D) break;
             const long long si = g.s[i];
-            Psi[i] = ff_mul(ff_add(rK, ff_split(F.rj[K - si])), Q.half_inv_dt);
+            // Ψ = (ρuf[K] + ρuf[K-δi])/(2δt) in FP64, the reference's two operations, on a pipe this
+            // kernel leaves almost idle; then one split
+            Psi[i] = ff_split((rK + F.rj[K - si]) * F.half_inv_dt);
             P[i] = ff_pos(Psi[i]) ? K - sj : K;
             const unsigned long long a = dbits(F.fold[P[i]]), b = dbits(F.fold[P[i] - si]);
             if (i == 0) ph = a;

@@ -208,10 +208,11 @@ __global__ void __launch_bounds__(256) vof_bulk(SweepArgs a) {
             int cs;
             if (FIRST) cs = (((bc & ABS_MASK) <= 0x7FF0000000000000ull) && ((bc >> 63) || bc < 0x3FE0000000000000ull)) ? 0 : 1;
             else cs = cb;
-            const ff du = ff_add(ff_sub(ff_split(a.u1[S + sd]), ff_split(a.u1[S])),
-                                 ff_sub(ff_split(a.u2[S + sd]), ff_split(a.u2[S])));
+            // the velocity differences in FP64, as the reference forms them (three FP64 additions on a
+            // pipe this kernel leaves mostly idle), then one split and a pair product
+            const double du = (a.u1[S + sd] - a.u1[S]) + (a.u2[S + sd] - a.u2[S]);
             const ff rq = cs ? ff{a.rq_1_hi, a.rq_1_lo} : ff{a.rq_l_hi, a.rq_l_lo};
-            const ff dq = ff_mul(rq, du);
+            const ff dq = ff_mul(rq, ff_split(du));
             a.dila[O] = make_float2(dq.hi, dq.lo);
         }
         // in place a bulk cell keeps its value and only a stale ghost copy needs a write;
