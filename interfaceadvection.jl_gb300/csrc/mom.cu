@@ -44,6 +44,28 @@ __global__ void u2rhou_kern(MomConsts k, double* __restrict__ rhou, const double
     for (int i = 0; i < g.D; ++i) rhou[I + i * g.N] = mul_rho(k, u[I + i * g.N], f[I], f[I - g.s[i]]);
 }
 
+// Start of an RK2 stage (src/flow.jl:61, 69 and 89, 92): f_dst = f_src and, when u_dst is given,
+// u_dst = u_src over every cell; ρu = u_src · getρ(f_src) on interior cells (u2ρu!).  One pass instead of
+// two device copies and a u2ρu! pass that reads them back.
+template <int D>
+__global__ void stage_start_kern(MomConsts k, const double* __restrict__ us, double* __restrict__ ud,
+                                 const double* __restrict__ fs, double* __restrict__ fd, double* __restrict__ rhou) {
+    const Grid& g = k.g;
+    GCELL_XYZ
+    const long long O = lin(g, x, y, z);
+    const double fO = fs[O];
+    fd[O] = fO;
+    double uv[D];
+#pragma unroll
+    for (int i = 0; i < D; ++i) {
+        uv[i] = us[O + i * g.N];
+        if (ud) ud[O + i * g.N] = uv[i];
+    }
+    if (x < 1 || x > g.n[0] - 2 || y < 1 || y > g.n[1] - 2 || (D == 3 && (z < 1 || z > g.n[2] - 2))) return;
+#pragma unroll
+    for (int i = 0; i < D; ++i) rhou[O + i * g.N] = mul_rho(k, uv[i], fO, fs[O - g.s[i]]);
+}
+
 // BC! at one cell: Dirichlet A[i] on the normal faces, ghost copies elsewhere
 __device__ __forceinline__ void bcvel_cell(const Grid& g, double* a, const double A[3], const int c0[3]) {
     const bool inner = is_interior(g, c0);
@@ -632,6 +654,12 @@ __global__ void cfl_kern(Grid g, const double* __restrict__ u, unsigned long lon
 
 cudaError_t k_ustar(const MomConsts& k, const double* rhou, const double* f, double* ustar, cudaStream_t s) {
     { ustar_kern<<<ggrd(k.g), blk(), 0, s>>>(k, rhou, f, ustar); ia::note_launch(); }
+    return cudaGetLastError();
+}
+cudaError_t k_stage_start(const MomConsts& k, const double* us, double* ud, const double* fs, double* fd, double* rhou,
+                          cudaStream_t s) {
+    if (k.g.D == 3) { stage_start_kern<3><<<ggrd(k.g), blk(), 0, s>>>(k, us, ud, fs, fd, rhou); ia::note_launch(); }
+    else { stage_start_kern<2><<<ggrd(k.g), blk(), 0, s>>>(k, us, ud, fs, fd, rhou); ia::note_launch(); }
     return cudaGetLastError();
 }
 cudaError_t k_u2rhou(const MomConsts& k, double* rhou, const double* u, const double* f, cudaStream_t s) {

@@ -17,6 +17,9 @@ struct MomConsts {
 
 // ρu2u! + BC! → uStar (src/VOFutil.jl:198-201; WaterLily BC!)
 cudaError_t k_ustar(const MomConsts& k, const double* rhou, const double* f, double* ustar, cudaStream_t s);
+// stage start: fd = fs, ud = us (when ud is given) on every cell, ρu = us·getρ(fs) on interior cells
+cudaError_t k_stage_start(const MomConsts& k, const double* us, double* ud, const double* fs, double* fd, double* rhou,
+                          cudaStream_t s);
 // u2ρu! on interior cells (src/VOFutil.jl:208-211)
 cudaError_t k_u2rhou(const MomConsts& k, double* rhou, const double* u, const double* f, cudaStream_t s);
 // WaterLily BC! on a vector field in place

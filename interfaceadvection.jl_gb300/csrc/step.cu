@@ -240,9 +240,8 @@ int ia_mom_step(ia_handle* h, double dt, int64_t n_dt, double t_now, ia_status* 
     std::memset(&S, 0, sizeof(S));
     // ---- predictor: u(n) → u(n+½) with u(n)
     int tk = timing_begin(h, TK_UPDATE);
-    cudaMemcpyAsync(F.u0, F.u, 8 * NV, cudaMemcpyDeviceToDevice, st);
-    cudaMemcpyAsync(F.f0, F.f, 8 * N, cudaMemcpyDeviceToDevice, st);
-    if (k_u2rhou(k, F.rhou, F.u0, F.f0, st) != cudaSuccess) return IA_ERR_CUDA;
+    // copyto!(u⁰,u); copyto!(f⁰,f); u2ρu!(ρu,u⁰,f⁰) in one pass
+    if (k_stage_start(k, F.u, F.u0, F.f, F.f0, F.rhou, st) != cudaSuccess) return IA_ERR_CUDA;
     timing_end(h, tk);
     int rc = status_reset(h);
     if (rc == IA_OK) rc = advect_fq(h, F.f0, F.u0, F.u, F.u, dt, dirs, 0);
@@ -271,8 +270,8 @@ int ia_mom_step(ia_handle* h, double dt, int64_t n_dt, double t_now, ia_status* 
     S.poisson_resid[0] = r0;
     // ---- corrector: u(n) → u(n+1) with u(n+½)
     tk = timing_begin(h, TK_UPDATE);
-    cudaMemcpyAsync(F.f0, F.f, 8 * N, cudaMemcpyDeviceToDevice, st);
-    if (k_u2rhou(k, F.rhou, F.u0, F.f, st) != cudaSuccess) return IA_ERR_CUDA;
+    // copyto!(f⁰,f); u2ρu!(ρu,u⁰,f) in one pass
+    if (k_stage_start(k, F.u0, nullptr, F.f, F.f0, F.rhou, st) != cudaSuccess) return IA_ERR_CUDA;
     timing_end(h, tk);
     rc = status_reset(h);
     if (rc == IA_OK) rc = advect_fq(h, F.f, F.u, F.u, F.u0, dt, dirs, 8);
