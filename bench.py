@@ -70,6 +70,9 @@ def parse():
     ap.add_argument("--ref-steps", type=int, default=2, help="oracle steps timed by the reference arm")
     ap.add_argument("--no-coef16", action="store_true",
                     help="FP32 face coefficients in the finest-level smoother of the mixed V-cycle")
+    ap.add_argument("--slab-rows", type=int, default=None,
+                    help="rows per slab of the finest-level smoothing wavefront (0: whole-level half-sweeps; "
+                         "default: the library's, from the L2 size)")
     return ap.parse_args()
 
 
@@ -342,6 +345,8 @@ def run_bubble(args, world, local_rank):
     sim = make_bubble(N, "mixed", dev)
     if args.no_coef16:
         ia.set_poisson_coef16(sim.handle, False)
+    if args.slab_rows is not None:
+        ia.set_poisson_slab_rows(sim.handle, args.slab_rows)
     m0 = sim.intf.mass()
     for _ in range(args.warmup):
         ia.sim_step(sim)

@@ -349,6 +349,12 @@ int ia_poisson_mg_relax(ia_handle* h, double omega);
  * stops on the FP64 true residual.  Default 1 when the coefficients 1/ρ (between 1/max(λρ,1) and
  * 1/min(λρ,1)) fit FP16's range, which IA_ERR_UNSUPPORTED reports otherwise. */
 int ia_poisson_coef16(ia_handle* h, int32_t on);
+/* rows per slab of the finest-level wavefront in the MIXED / LEARNED modes (no reference counterpart):
+ * the red-black half-sweeps and the residual restriction of a smoothing run slab by slab over y, each
+ * half-sweep one row behind the previous, so that the later half-sweeps read the slab from L2.  Same
+ * results as whole-level half-sweeps, bit for bit.  0 = whole-level half-sweeps; otherwise at least 8.
+ * Applies in 3D with walls in y; default from the device's L2 size (about 3/5 of it per slab). */
+int ia_poisson_slab_rows(ia_handle* h, int32_t rows);
 /* counters since the handle's creation: [0] net applications, [1] V-cycles, [2] fallbacks
  * to the V-cycle, [3] inner FCG iterations, [4] outer corrections */
 int ia_poisson_stats(ia_handle* h, int64_t* out5);

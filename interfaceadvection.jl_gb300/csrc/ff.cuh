@@ -162,4 +162,30 @@ FF_HD double ff_widen(float v) {
 // hi + lo rounded to FP64 (one FP64 addition of the two exact widenings)
 FF_HD double ff_join(ff x) { return ff_widen(x.hi) + ff_widen(x.lo); }
 
+// the conversion instruction, out of line on the device: inlined, the compiler if-converts the rare
+// branch into every call and the conversion (an FP64-pipe instruction) issues for every value
+#ifdef __CUDA_ARCH__
+static __device__ __noinline__ float ff_f32_cvt(double v) { return __double2float_rn(v); }
+#else
+inline float ff_f32_cvt(double v) { return (float)v; }
+#endif
+// FP64 -> FP32 rounded to nearest even (= float(v), bit for bit) with integer operations where the
+// result is a normal FP32 number or a zero, so that no conversion issues on the FP64 pipe; any other
+// value (the FP32 subnormal range, overflow to inf, inf, NaN) takes the conversion.
+FF_HD float f32_rn(double v) {
+    const uint64_t b = ff_dbits(v);
+    const uint32_t h32 = uint32_t(b >> 32), l32 = uint32_t(b);
+    const int e = int((h32 >> 20) & 0x7FFu);
+    if (e >= 897 && e <= 1150) {
+        // FP32 exponent e - 896 in [1, 254]; the top 23 significand bits kept, the other 29 rounded
+        // away (a carry out of the significand moves into the exponent, up to inf, as rounding does)
+        uint32_t f = (uint32_t(e - 896) << 23) | ((h32 & 0xFFFFFu) << 3) | (l32 >> 29);
+        const uint32_t rem = l32 & 0x1FFFFFFFu;
+        f += (rem > 0x10000000u || (rem == 0x10000000u && (f & 1u))) ? 1u : 0u;
+        return ff_bitsf((h32 & 0x80000000u) | f);
+    }
+    if ((b << 1) == 0) return ff_bitsf(h32 & 0x80000000u);
+    return ff_f32_cvt(v);
+}
+
 }  // namespace ia

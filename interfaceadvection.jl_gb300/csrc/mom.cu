@@ -544,16 +544,22 @@ __global__ void updateu_kern(MomConsts k, double* __restrict__ u, double* __rest
     }
 }
 
+template <int D>
 __global__ void updatel_kern(MomConsts k, double* __restrict__ mu0, const double* __restrict__ f) {
     const Grid& g = k.g;
     GCELL_XYZ
     const long long O = lin(g, x, y, z);
-    if (x >= 2 && x <= g.n[0] - 2 && y >= 2 && y <= g.n[1] - 2 && (g.D == 2 || (z >= 2 && z <= g.n[2] - 2))) {
+    if (x >= 2 && x <= g.n[0] - 2 && y >= 2 && y <= g.n[1] - 2 && (D == 2 || (z >= 2 && z <= g.n[2] - 2))) {
+        // no boundary rule: every load first
         const double fo = f[O];
-        for (int i = 0; i < g.D; ++i) mu0[O + i * g.N] = div_rho(k, 1.0, fo, f[O - g.s[i]]);
+        double fm[D];
+#pragma unroll
+        for (int i = 0; i < D; ++i) fm[i] = f[O - g.s[i]];
+#pragma unroll
+        for (int i = 0; i < D; ++i) mu0[O + i * g.N] = div_rho(k, 1.0, fo, fm[i]);
         return;
     }
-    for (int i = 0; i < g.D; ++i) {
+    for (int i = 0; i < D; ++i) {
         int c[3] = {x, y, z};
         if (vel_bc(g, i, c)) { mu0[O + i * g.N] = 0.0; continue; }
         const long long P = lin3(g, c);
@@ -754,7 +760,8 @@ cudaError_t k_updateu(const MomConsts& k, double* u, double* rhou, const double*
     return cudaGetLastError();
 }
 cudaError_t k_updatel(const MomConsts& k, double* mu0, const double* f, cudaStream_t s) {
-    { updatel_kern<<<ggrd(k.g), blk(), 0, s>>>(k, mu0, f); ia::note_launch(); }
+    if (k.g.D == 3) { updatel_kern<3><<<ggrd(k.g), blk(), 0, s>>>(k, mu0, f); ia::note_launch(); }
+    else { updatel_kern<2><<<ggrd(k.g), blk(), 0, s>>>(k, mu0, f); ia::note_launch(); }
     return cudaGetLastError();
 }
 cudaError_t k_div_scale(const MomConsts& k, const double* u, double* zz, double* xx, double dt, cudaStream_t s) {

@@ -297,7 +297,7 @@ __device__ __forceinline__ void list_append(unsigned int* list, unsigned int* co
 // one pure phase (for every component) take the short path below; every other cell goes to the list.
 // No out-of-line calls and no local arrays on this path.
 template <int LIM>
-__global__ void __launch_bounds__(256, 5) momflux_ff_bulk(FluxCtx F, FluxFF Q, const float2* __restrict__ us,
+__global__ void __launch_bounds__(256, 4) momflux_ff_bulk(FluxCtx F, FluxFF Q, const float2* __restrict__ us,
                                                           float2* __restrict__ Phi, unsigned int* __restrict__ list,
                                                           unsigned int* __restrict__ count) {
     const Grid& g = F.k.g;
@@ -317,24 +317,42 @@ __global__ void __launch_bounds__(256, 5) momflux_ff_bulk(FluxCtx F, FluxFF Q, c
     const long long K = lin(g, x, y, z);
     bool defer = in_range && !inner;
     if (in_range && inner) {
+        // every load first, for both signs of Ψ (the donor row K - δj or K, the upwind stencil
+        // K - 2δj .. K or K + δj .. K - δj), so that no load waits for the FP64 Ψ or the pure-phase test
         const long long sj = g.s[j];
         const double rK = F.rj[K];
+        const unsigned long long oK = dbits(F.fold[K]), oKj = dbits(F.fold[K - sj]);
+        double rI[3];
+        unsigned long long oKi[3], oKji[3];
+        ff um2[3], um1[3], u00[3], up1[3];
+#pragma unroll
+        for (int i = 0; i < 3; ++i) {
+            if (i >= g.D) break;
+            const long long si = g.s[i];
+            rI[i] = F.rj[K - si];
+            oKi[i] = dbits(F.fold[K - si]);
+            oKji[i] = dbits(F.fold[K - sj - si]);
+            const float2* u = us + i * g.N;
+            um2[i] = ldff(u + K - 2 * sj);
+            um1[i] = ldff(u + K - sj);
+            u00[i] = ldff(u + K);
+            up1[i] = ldff(u + K + sj);
+        }
         ff Psi[3];
-        long long P[3];
         unsigned long long ph = 0ull;
         bool pure = true;
 #pragma unroll
         for (int i = 0; i < 3; ++i) {
             if (i >= g.D) break;
-            const long long si = g.s[i];
             // Ψ = (ρuf[K] + ρuf[K-δi])/(2δt) in FP64, the reference's two operations, on a pipe this
             // kernel leaves almost idle; then one split
-            Psi[i] = ff_split((rK + F.rj[K - si]) * F.half_inv_dt);
-            P[i] = ff_pos(Psi[i]) ? K - sj : K;
-            const unsigned long long a = dbits(F.fold[P[i]]), b = dbits(F.fold[P[i] - si]);
+            Psi[i] = ff_split((rK + rI[i]) * F.half_inv_dt);
+            const bool pos = ff_pos(Psi[i]);   // donor row P = K - δj (Ψ > 0) or K
+            const unsigned long long a = pos ? oKj : oK, b = pos ? oKji[i] : oKi[i];
             if (i == 0) ph = a;
-            pure = pure && a == ph && b == ph && (a == 0ull || a == kOneBits);
+            pure = pure & (a == ph) & (b == ph);
         }
+        pure = pure & ((ph == 0ull) | (ph == kOneBits));
         if (!pure) {
             defer = true;
         } else {
@@ -343,11 +361,10 @@ __global__ void __launch_bounds__(256, 5) momflux_ff_bulk(FluxCtx F, FluxFF Q, c
 #pragma unroll
             for (int i = 0; i < 3; ++i) {
                 if (i >= g.D) break;
-                const float2* u = us + i * g.N;
                 const bool pos = ff_pos(Psi[i]);
-                const ff uu = ldff(u + (pos ? K - 2 * sj : K + sj));
-                const ff cc = ldff(u + (pos ? K - sj : K));
-                const ff dd = ldff(u + (pos ? K : K - sj));
+                const ff uu = pos ? um2[i] : up1[i];
+                const ff cc = pos ? um1[i] : u00[i];
+                const ff dd = pos ? u00[i] : um1[i];
                 const ff m = limiter_corr_ff<LIM>(Q, uu, cc, dd);
                 const ff aP = ff_abs(Psi[i]);
                 const ff v = ff_lt(thr, aP) ? ff_mul(Psi[i], cc) : blend(Psi[i], ff_mul(aP, kl), cc, m);
@@ -449,7 +466,7 @@ __device__ __noinline__ void viscflux_ff_mixed(const ViscCtx& V, const ViscFF& W
 // Bulk pass: cells whose faces and edges no boundary rule reaches and whose viscosities all read one pure
 // phase; every other cell goes to the list (mixed viscosities or boundary rules, viscflux_ff_list)
 template <int D>
-__global__ void __launch_bounds__(256, 4) viscflux_ff_bulk(ViscCtx V, ViscFF W, float2* __restrict__ Phi6,
+__global__ void __launch_bounds__(256, 5) viscflux_ff_bulk(ViscCtx V, ViscFF W, float2* __restrict__ Phi6,
                                                            unsigned int* __restrict__ list,
                                                            unsigned int* __restrict__ count) {
     const Grid& g = V.k.g;
@@ -461,15 +478,18 @@ __global__ void __launch_bounds__(256, 4) viscflux_ff_bulk(ViscCtx V, ViscFF W, 
     unsigned long long b0 = 0ull;
     if (inner) {
         // the fractions any of the D(D+1)/2 viscosities reads (get_mu_inner: K, K-s_e, K-2s_e, K-s_i-s_j)
+        // (every compare evaluated, no short circuit: the loads issue together instead of one after
+        // another's compare)
         const double* f = V.f;
         b0 = dbits(f[K]);
-        pure = b0 == 0ull || b0 == kOneBits;
+        bool same = true;
 #pragma unroll
-        for (int e = 0; e < D; ++e) pure = pure && dbits(f[K - g.s[e]]) == b0 && dbits(f[K - 2 * g.s[e]]) == b0;
+        for (int e = 0; e < D; ++e) same = same & (dbits(f[K - g.s[e]]) == b0) & (dbits(f[K - 2 * g.s[e]]) == b0);
 #pragma unroll
         for (int a = 0; a < D; ++a)
 #pragma unroll
-            for (int b = a + 1; b < D; ++b) pure = pure && dbits(f[K - g.s[a] - g.s[b]]) == b0;
+            for (int b = a + 1; b < D; ++b) same = same & (dbits(f[K - g.s[a] - g.s[b]]) == b0);
+        pure = same & ((b0 == 0ull) | (b0 == kOneBits));
     }
     if (pure) {
         const ff mu = b0 == 0ull ? W.mu_face0 : W.mu_face1;
@@ -576,6 +596,15 @@ __global__ void div_scale_ff_kern(Grid g, const double* __restrict__ u, double* 
     zz[I] = ff_join(s);
 }
 
+// v truncated to its top 20 significand bits as FP32 (|result| <= |v|, short by less than 2^-20 of
+// itself); 0 below the FP32 normal range (where ff_split gives 0 as well), NaN above it
+__device__ __forceinline__ float est20(double v) {
+    const unsigned h = unsigned(dbits(v) >> 32);
+    const int e = int((h >> 20) & 0x7FFu);
+    if (e < 897) return 0.0f;
+    if (e > 1150) return __uint_as_float(0x7FC00000u);
+    return __uint_as_float((h & 0x80000000u) | (unsigned(e - 896) << 23) | ((h & 0xFFFFFu) << 3));
+}
 __device__ __forceinline__ unsigned long long nonneg_bits_ff(double v) {
     const unsigned long long b = dbits(v);
     return (b == 0x8000000000000000ull) ? 0ull : b;
@@ -595,6 +624,7 @@ template <int D>
 __global__ void cfl_ff_kern(Grid g, const double* __restrict__ u, unsigned long long* out) {
     __shared__ unsigned long long s1[32], s2[32];
     unsigned long long a1 = 0ull, a2 = 0ull;
+    float t1 = 0.0f, t2 = 0.0f;
     const int nxi = g.n[0] - 2, nyi = g.n[1] - 2;
     const int rows = nyi * (D == 3 ? g.n[2] - 2 : 1);
     const int dy = int(gridDim.x) % nyi, dz = int(gridDim.x) / nyi;
@@ -602,18 +632,46 @@ __global__ void cfl_ff_kern(Grid g, const double* __restrict__ u, unsigned long 
     for (int rw = blockIdx.x; rw < rows; rw += gridDim.x, y += dy, z += dz + (y > nyi ? 1 : 0), y -= (y > nyi ? nyi : 0)) {
         for (int x = 1 + threadIdx.x; x <= nxi; x += blockDim.x) {
             const long long I = lin(g, x, y, z);
-            ff fo = ff_from(0.0f), mt = ff_from(0.0f);
+            double lo[D], hi[D];
 #pragma unroll
             for (int i = 0; i < D; ++i) {
-                const double lo = u[I + i * g.N], hi = u[I + g.s[i] + i * g.N];
-                const ff flo = ff_split(lo), fhi = ff_split(hi);
-                fo = ff_add(fo, ff_add(ff_pos(fhi) ? fhi : ff_from(0.0f), ff_neg(flo) ? -flo : ff_from(0.0f)));
-                const bool lo_big = (dbits(lo) & kAbsMask) >= (dbits(hi) & kAbsMask);
-                mt = ff_add(mt, ff_abs(lo_big ? flo : fhi));
+                lo[i] = u[I + i * g.N];
+                hi[i] = u[I + g.s[i] + i * g.N];
             }
-            const unsigned long long b1 = nonneg_bits_ff(ff_join(fo)), b2 = nonneg_bits_ff(ff_join(mt));
-            a1 = b1 > a1 ? b1 : a1;
-            a2 = b2 > a2 ? b2 : a2;
+            // FP32 upper bounds of the cell's two sums (terms from the top 20 significand bits, each low
+            // by less than 2^-20 of itself; FP32 sums of non-negative terms): the pair sums below run only
+            // where a bound is above the largest pair sum this thread has seen (t1, t2 are lower bounds
+            // of those), so the maxima are those of every cell's pair sums.  inf and NaN take the exact
+            // path (a NaN bound fails every comparison).
+            float e1 = 0.0f, e2 = 0.0f;
+#pragma unroll
+            for (int i = 0; i < D; ++i) {
+                const float l = est20(lo[i]), h = est20(hi[i]);
+                e1 += fmaxf(h, 0.0f) + fmaxf(-l, 0.0f);
+                e2 += fmaxf(fabsf(l), fabsf(h));
+            }
+            if (!(e1 * 1.0001f <= t1)) {
+                ff fo = ff_from(0.0f);
+#pragma unroll
+                for (int i = 0; i < D; ++i) {
+                    const ff flo = ff_split(lo[i]), fhi = ff_split(hi[i]);
+                    fo = ff_add(fo, ff_add(ff_pos(fhi) ? fhi : ff_from(0.0f), ff_neg(flo) ? -flo : ff_from(0.0f)));
+                }
+                const unsigned long long b1 = nonneg_bits_ff(ff_join(fo));
+                a1 = b1 > a1 ? b1 : a1;
+                t1 = fmaxf(t1, fo.hi * 0.999999f);
+            }
+            if (!(e2 * 1.0001f <= t2)) {
+                ff mt = ff_from(0.0f);
+#pragma unroll
+                for (int i = 0; i < D; ++i) {
+                    const bool lo_big = (dbits(lo[i]) & kAbsMask) >= (dbits(hi[i]) & kAbsMask);
+                    mt = ff_add(mt, ff_abs(ff_split(lo_big ? lo[i] : hi[i])));
+                }
+                const unsigned long long b2 = nonneg_bits_ff(ff_join(mt));
+                a2 = b2 > a2 ? b2 : a2;
+                t2 = fmaxf(t2, mt.hi * 0.999999f);
+            }
         }
     }
     a1 = warp_umax_ff(a1);

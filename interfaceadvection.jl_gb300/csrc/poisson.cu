@@ -25,12 +25,14 @@
 // the FP64 true residual switches the rest of the solve to the plain V-cycle.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cmath>
 #include <cstring>
 #include <vector>
 
 #include "capi_internal.cuh"
 #include "ia_bc.cuh"
+#include "ff.cuh"
 #include "poisson.cuh"
 
 namespace ia {
@@ -182,11 +184,12 @@ __global__ void restrict_L_k(Grid gc, Grid gf, const T* __restrict__ Lf, T* __re
 // With PROL (over-relaxed first red half-sweep of a post-smoothing whose prolongation is fused
 // into the sweeps) the cell's previous value is x + the injected coarse correction.
 template <class T, int D, bool PROL = false, class TL = T>
-__global__ void rbgs_pair_k(Grid g, const TL* __restrict__ L, const T* __restrict__ b, T* __restrict__ xv,
-                            int color, T omega, Grid gc = Grid(), const T* __restrict__ xc = nullptr) {
-    const int y = 1 + blockIdx.y * blockDim.y + threadIdx.y;
+__global__ void rbgs_pair_k(Grid g, int y0, int y1, const TL* __restrict__ L, const T* __restrict__ b,
+                            T* __restrict__ xv, int color, T omega, Grid gc = Grid(),
+                            const T* __restrict__ xc = nullptr) {
+    const int y = y0 + int(blockIdx.y * blockDim.y + threadIdx.y);   // rows [y0, y1) of the interior
     const int z = D == 3 ? 1 + int(blockIdx.z) : 0;
-    if (y > g.n[1] - 2) return;
+    if (y >= y1) return;
     int x = 1 + 2 * (blockIdx.x * blockDim.x + threadIdx.x);
     if (((x + y + z) & 1) != color) ++x;
     if (x > g.n[0] - 2) return;
@@ -225,12 +228,12 @@ __device__ __forceinline__ T first_nb(const Grid& g, const Grid& gc, const T* __
 }
 
 template <class T, int D, bool PROL, class TL = T>
-__global__ void rbgs_first_k(Grid g, Grid gc, const TL* __restrict__ L, const T* __restrict__ b,
+__global__ void rbgs_first_k(Grid g, int y0, int y1, Grid gc, const TL* __restrict__ L, const T* __restrict__ b,
                              const T* __restrict__ iD, const T* __restrict__ xc, T* __restrict__ xv, int write_red,
                              T omega) {
-    const int y = 1 + blockIdx.y * blockDim.y + threadIdx.y;
+    const int y = y0 + int(blockIdx.y * blockDim.y + threadIdx.y);   // rows [y0, y1) of the interior
     const int z = D == 3 ? 1 + int(blockIdx.z) : 0;
-    if (y > g.n[1] - 2) return;
+    if (y >= y1) return;
     const int x0 = 1 + 2 * (blockIdx.x * blockDim.x + threadIdx.x);
     const bool blk0 = ((x0 + y + z) & 1) == 1;
     const int x = blk0 ? x0 : x0 + 1, xr = blk0 ? x0 + 1 : x0;   // black and red cell of the pair
@@ -498,12 +501,12 @@ __global__ void residual_k(Grid g, const T* __restrict__ L, const T* __restrict_
 // residual of the 2^D fine children of each coarse cell, summed straight into the coarse
 // right-hand side (residual_k + restrict_k without the fine residual array; same sums, same order)
 template <class T, int D, class TL = T>
-__global__ void resid_restrict_k(Grid gc, Grid gf, const TL* __restrict__ L, const T* __restrict__ b,
-                                 const T* __restrict__ xv, T* __restrict__ bc) {
+__global__ void resid_restrict_k(Grid gc, int yc0, int yc1, Grid gf, const TL* __restrict__ L,
+                                 const T* __restrict__ b, const T* __restrict__ xv, T* __restrict__ bc) {
     const int xc = 1 + blockIdx.x * blockDim.x + threadIdx.x;
-    const int yc = 1 + blockIdx.y * blockDim.y + threadIdx.y;
+    const int yc = yc0 + int(blockIdx.y * blockDim.y + threadIdx.y);   // coarse rows [yc0, yc1)
     const int zc = D == 3 ? 1 + int(blockIdx.z) : 0;
-    if (xc > gc.n[0] - 2 || yc > gc.n[1] - 2) return;
+    if (xc > gc.n[0] - 2 || yc >= yc1) return;
     const int s1 = int(gf.s[1]), s2 = int(gf.s[2]);
     T sum = T(0);
     for (int k = 0; k < (D == 3 ? 2 : 1); ++k)
@@ -585,13 +588,9 @@ __global__ void zero_k(long long n, T* a) {
     for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < n; q += (long long)gridDim.x * blockDim.x)
         a[q] = T(0);
 }
-__global__ void to_f16_k(long long n, const float* __restrict__ a, __half* __restrict__ b) {
-    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
-        b[i] = __float2half_rn(a[i]);
-}
 __global__ void to_f32_k(long long n, const double* __restrict__ a, float* __restrict__ b) {
     for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < n; q += (long long)gridDim.x * blockDim.x)
-        b[q] = float(a[q]);
+        b[q] = f32_rn(a[q]);
 }
 __global__ void to_f64_k(long long n, const float* __restrict__ a, double* __restrict__ b) {
     for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < n; q += (long long)gridDim.x * blockDim.x)
@@ -687,13 +686,95 @@ __device__ __forceinline__ double diag_of(const Grid& g, const double* L, long l
     for (int i = 0; i < g.D; ++i) dd -= L[I + i * g.N] + L[I + g.s[i] + i * g.N];
     return dd;
 }
+// diag_of (same sums, same order) out of line, with scalar arguments, for kernels whose common path
+// must not carry its FP64 additions (inlined in a branch of pure arithmetic, the compiler if-converts
+// it into every thread)
+template <int D>
+__device__ __noinline__ double diag_of_cold(const double* L, long long I, long long s1, long long s2, long long N) {
+    double dd = 0.0;
+    dd -= L[I] + L[I + 1];
+    dd -= L[I + N] + L[I + s1 + N];
+    if (D == 3) dd -= L[I + 2 * N] + L[I + s2 + 2 * N];
+    return dd;
+}
+
 __global__ void set_diag64_k(Grid g, const double* __restrict__ L, double* __restrict__ diag) {
     ROWS_BEGIN(g)
     diag[I] = diag_of(g, L, I);
     ROWS_END
 }
 
-// r = z - A x over interior cells, L∞(r) into *linf; diag precomputed (or NULL: from L)
+// Finest-level set-up of the mixed solver in one pass over the FP64 face coefficients L (one
+// thread per cell of the ghost-inclusive grid):
+//  - the FP32 copy L32 of every coefficient (and its FP16 copy L16, when given), = float(L);
+//  - on interior cells the FP64 diagonal D_I = -Σ_i (L[I,i] + L[I+δi,i]) in diag_of's order, and the
+//    FP32 inverse diagonal of the FP32 copy with set_diag_k's sums and zero rule.
+// Where the 2D coefficients of a cell are bit-identical (pure-phase cells away from walls), the
+// FP64 sum ((0 - 2a) - 2a) - 2a (3D; (0 - 2a) - 2a in 2D) is exactly fma(-2D, a, 0): the partial
+// sums are exact multiples of a and only the last one rounds, as the fma does; both give +0 for a = ±0.
+template <int D>
+__global__ void setup_fine_k(Grid g, const double* __restrict__ L, double* __restrict__ diag,
+                             float* __restrict__ L32, __half* __restrict__ L16, float* __restrict__ iD32) {
+    const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y;
+    const int z = D == 3 ? int(blockIdx.z) : 0;
+    if (x >= g.n[0] || y >= g.n[1]) return;
+    const long long I = lin(g, x, y, z);
+    double a[D];
+    float fa[D];
+#pragma unroll
+    for (int i = 0; i < D; ++i) {
+        a[i] = L[I + i * g.N];
+        fa[i] = f32_rn(a[i]);
+        L32[I + i * g.N] = fa[i];
+        if (L16) L16[I + i * g.N] = __float2half_rn(fa[i]);
+    }
+    if (x < 1 || y < 1 || x > g.n[0] - 2 || y > g.n[1] - 2) return;
+    if (D == 3 && (z < 1 || z > g.n[2] - 2)) return;
+    double b[D];
+    bool same = true;
+    const unsigned long long a0 = (unsigned long long)__double_as_longlong(a[0]);
+#pragma unroll
+    for (int i = 0; i < D; ++i) {
+        b[i] = L[I + g.s[i] + i * g.N];
+        same = same && (unsigned long long)__double_as_longlong(a[i]) == a0 &&
+               (unsigned long long)__double_as_longlong(b[i]) == a0;
+    }
+    diag[I] = same ? fma(-2.0 * D, a[0], 0.0) : diag_of_cold<D>(L, I, g.s[1], g.s[2], g.N);
+    float df = 0.0f;
+#pragma unroll
+    for (int i = 0; i < D; ++i) df -= fa[i] + f32_rn(b[i]);
+    const float eps = 1.1920929e-7f;
+    iD32[I] = (df * df < 2.0f * eps) ? 0.0f : 1.0f / df;
+}
+
+constexpr int MV_ZT = 4;   // z planes per block of the tiled stencil kernels
+inline dim3 mv_tile_grid(const Grid& g) {
+    return dim3((g.n[0] - 2 + 31) / 32, (g.n[1] - 2 + 7) / 8, g.D == 3 ? (g.n[2] - 2 + MV_ZT - 1) / MV_ZT : 1);
+}
+
+// z_I - D_I x_I - Σ L x_nb as one FMA chain: 2D + 1 FP64 operations where pairwise sums take 3D + 1
+// (the residual kernels are bound by the FP64 pipe)
+template <int D>
+__device__ __forceinline__ double resid_cell(const Grid& g, const double* __restrict__ L, double dd,
+                                             const double* __restrict__ zz, const double* __restrict__ xv, int I,
+                                             const Nb& o) {
+    const int s1 = int(g.s[1]), s2 = int(g.s[2]);
+    const double* L1 = L + g.N;
+    double v = fma(-dd, xv[I], zz[I]);
+    v = fma(-L[I], xv[I + o.xl], v);
+    v = fma(-L[I + 1], xv[I + o.xh], v);
+    v = fma(-L1[I], xv[I + o.yl], v);
+    v = fma(-L1[I + s1], xv[I + o.yh], v);
+    if (D == 3) {
+        const double* L2 = L1 + g.N;
+        v = fma(-L2[I], xv[I + o.zl], v);
+        v = fma(-L2[I + s2], xv[I + o.zh], v);
+    }
+    return v;
+}
+
+// r = z - A x over interior cells, L∞(r) into *linf (zeroed by the caller); diag precomputed (or NULL:
+// from L).  Row loop over a grid of at most KBLOCKS blocks (no per-block scratch).
 template <int D>
 __global__ void true_resid_k(Grid g, const double* __restrict__ L, const double* __restrict__ diag,
                              const double* __restrict__ zz, const double* __restrict__ xv, double* __restrict__ r,
@@ -701,14 +782,48 @@ __global__ void true_resid_k(Grid g, const double* __restrict__ L, const double*
     unsigned long long m = 0ull;
     ROWS_BEGIN_D(g)
     const Nb o = nb_of<D>(g, x, y, z);
-    const double dd = diag ? diag[I] : diag7<D>(g, L, I);
-    const double v = zz[I] - (off7<D>(g, L, xv, I, o) + dd * xv[I]);
+    const double v = resid_cell<D>(g, L, diag ? diag[I] : diag7<D>(g, L, I), zz, xv, I, o);
     r[I] = v;
     const unsigned long long b = abs_bits(v);
     m = b > m ? b : m;
     ROWS_END
     m = block_max(m);
     if (threadIdx.x == 0) atomicMax(linf, m);
+}
+
+// The same on the x-y tiles of matvec32_tile_k (32 x 8 cells, MV_ZT z planes per block of 256 threads) with
+// the precomputed diagonal; each block's L∞ (as the bit pattern of |r|) into pmax[block], reduced by
+// finalize_max_k.
+template <int D>
+__global__ void __launch_bounds__(256) true_resid_tile_k(Grid g, const double* __restrict__ L,
+                                                         const double* __restrict__ diag,
+                                                         const double* __restrict__ zz,
+                                                         const double* __restrict__ xv, double* __restrict__ r,
+                                                         unsigned long long* __restrict__ pmax) {
+    const int x = 1 + int(blockIdx.x) * 32 + int(threadIdx.x & 31), y = 1 + int(blockIdx.y) * 8 + int(threadIdx.x >> 5);
+    const int z0 = D == 3 ? 1 + MV_ZT * int(blockIdx.z) : 0;
+    unsigned long long m = 0ull;
+    if (x <= g.n[0] - 2 && y <= g.n[1] - 2) {
+#pragma unroll
+        for (int k = 0; k < (D == 3 ? MV_ZT : 1); ++k) {
+            const int z = z0 + k;
+            if (D == 3 && z > g.n[2] - 2) break;
+            const int I = x + y * int(g.s[1]) + z * int(g.s[2]);
+            const Nb o = nb_of<D>(g, x, y, z);
+            const double v = resid_cell<D>(g, L, diag[I], zz, xv, I, o);
+            r[I] = v;
+            const unsigned long long b = abs_bits(v);
+            m = b > m ? b : m;
+        }
+    }
+    m = block_max(m);
+    if (threadIdx.x == 0) pmax[blockIdx.x + gridDim.x * (blockIdx.y + gridDim.y * blockIdx.z)] = m;
+}
+__global__ void finalize_max_k(const unsigned long long* __restrict__ pmax, long long n, unsigned long long* out) {
+    unsigned long long m = 0ull;
+    for (long long i = threadIdx.x; i < n; i += blockDim.x) m = pmax[i] > m ? pmax[i] : m;
+    m = block_max(m);
+    if (threadIdx.x == 0) *out = m;
 }
 
 // q = A p and partial dot p·q
@@ -742,19 +857,53 @@ __global__ void dot2_k(Grid g, const double* __restrict__ sv, const double* __re
 }
 
 // fixed-order sum of `n` partials for `k` quantities → out[0..k)
-__global__ void finalize_k(const double* __restrict__ partial, long long n, int k, double* out) {
+// Σ partial[qd·n + i] over i in a fixed order, valid in thread 0 (a block of 1024 threads)
+__device__ double finalize_sum(const double* __restrict__ partial, long long n, int qd) {
     __shared__ double sm[1024];
+    double acc = 0.0;
+    for (long long i = threadIdx.x; i < n; i += blockDim.x) acc += partial[qd * n + i];
+    sm[threadIdx.x] = acc;
+    __syncthreads();
+    for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+        if (threadIdx.x < w) sm[threadIdx.x] += sm[threadIdx.x + w];
+        __syncthreads();
+    }
+    const double v = sm[0];
+    __syncthreads();
+    return v;
+}
+__global__ void finalize_k(const double* __restrict__ partial, long long n, int k, double* out) {
     for (int qd = 0; qd < k; ++qd) {
-        double acc = 0.0;
-        for (long long i = threadIdx.x; i < n; i += blockDim.x) acc += partial[qd * n + i];
-        sm[threadIdx.x] = acc;
-        __syncthreads();
-        for (int w = blockDim.x / 2; w > 0; w >>= 1) {
-            if (threadIdx.x < w) sm[threadIdx.x] += sm[threadIdx.x + w];
-            __syncthreads();
+        const double v = finalize_sum(partial, n, qd);
+        if (threadIdx.x == 0) out[qd] = v;
+    }
+}
+// The inner FCG's scalars on the device, in the host's former FP64 operations: β from the partials of
+// s·q and s·r (β = 0 on the first step), then α = (s·r)/(p·q) with the breakdown test; on a breakdown
+// the update is skipped and α, s·r are not carried to the next step.
+__global__ void fcg_beta_k(const double* __restrict__ partial, long long n, FcgDev* S, int first) {
+    const double sq = finalize_sum(partial, n, 0);
+    const double sr = finalize_sum(partial, n, 1);
+    if (threadIdx.x == 0) {
+        const double beta = first ? 0.0 : (-S->alpha_prev * sq) / S->rho_prev;
+        S->sr = sr;
+        S->beta = beta;
+        S->beta32 = float(beta);
+    }
+}
+__global__ void fcg_alpha_k(const double* __restrict__ partial, long long n, FcgDev* S) {
+    const double pq = finalize_sum(partial, n, 0);
+    if (threadIdx.x == 0) {
+        const double sr = S->sr;
+        const bool stop = !(pq != 0.0) || !isfinite(pq) || !isfinite(sr) || !isfinite(S->beta);
+        const double alpha = sr / pq;
+        S->alpha32 = float(alpha);
+        S->stop = stop ? 1 : 0;
+        S->rin = 0u;
+        if (!stop) {
+            S->rho_prev = sr;
+            S->alpha_prev = alpha;
         }
-        if (threadIdx.x == 0) out[qd] = sm[0];
-        __syncthreads();
     }
 }
 
@@ -781,19 +930,42 @@ __global__ void update_k(Grid g, double alpha, const double* __restrict__ pv, co
 
 // ---- FP32 inner Krylov kernels (mixed / learned): FP32 products, per-thread sums in FP32
 // over its cells, FP64 block and cross-block sums.
+// q = A p and per-block partial sums of p·q on x-y tiles: a block of 256 threads takes 32 x 8 cells of
+// MV_ZT consecutive z planes (one plane in 2D), so that the stencil's x and y neighbours come from L1 and
+// every load of a cell issues at once (a row loop, one row per block and step, waits for each row's
+// loads and fetches the y neighbours from other SMs' rows through L2).  The partials, one per block,
+// are summed in a fixed order.
+
 template <int D>
-__global__ void matvec32_dot_k(Grid g, const float* __restrict__ L, const float* __restrict__ pv,
-                               float* __restrict__ q, double* __restrict__ partial) {
+__global__ void __launch_bounds__(256) matvec32_tile_k(Grid g, const float* __restrict__ L,
+                                                       const float* __restrict__ pv, float* __restrict__ q,
+                                                       double* __restrict__ partial) {
+    const int x = 1 + int(blockIdx.x) * 32 + int(threadIdx.x & 31), y = 1 + int(blockIdx.y) * 8 + int(threadIdx.x >> 5);
+    const int z0 = D == 3 ? 1 + MV_ZT * int(blockIdx.z) : 0;
     float acc = 0.f;
-    ROWS_BEGIN_D(g)
-    const Nb o = nb_of<D>(g, x, y, z);
-    const float v = off7<D>(g, L, pv, I, o) + diag7<D>(g, L, I) * pv[I];
-    q[I] = v;
-    acc += pv[I] * v;
-    ROWS_END
-    double a = acc, unused = 0.0;
-    block_sum2(a, unused);
-    if (threadIdx.x == 0) partial[blockIdx.x] = a;
+    if (x <= g.n[0] - 2 && y <= g.n[1] - 2) {
+#pragma unroll
+        for (int k = 0; k < (D == 3 ? MV_ZT : 1); ++k) {
+            const int z = z0 + k;
+            if (D == 3 && z > g.n[2] - 2) break;
+            const int I = x + y * int(g.s[1]) + z * int(g.s[2]);
+            const Nb o = nb_of<D>(g, x, y, z);
+            const float v = off7<D>(g, L, pv, I, o) + diag7<D>(g, L, I) * pv[I];
+            q[I] = v;
+            acc += pv[I] * v;
+        }
+    }
+    // the warp's sum in FP32 (a fixed shuffle tree), the block's eight warp sums in FP64 by one thread:
+    // a per-thread FP64 reduction costs more FP64-pipe time than the stencil itself
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
+    __shared__ double ws[8];
+    if ((threadIdx.x & 31) == 0) ws[threadIdx.x >> 5] = double(acc);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double a = 0.0;
+        for (int w = 0; w < 8; ++w) a += ws[w];
+        partial[blockIdx.x + gridDim.x * (blockIdx.y + gridDim.y * blockIdx.z)] = a;
+    }
 }
 
 // Whole-array FP32 vector kernels of the inner solve.  Only interior cells of these vectors are
@@ -828,7 +1000,9 @@ __global__ void dot2_32_k(long long n, const float* __restrict__ sv, const float
 
 // p = s + β p; β = 0 restarts from s without reading the old direction (which a rejected
 // preconditioner output may have left non-finite)
-__global__ void xpby32_k(long long n, const float* __restrict__ sv, float beta, float* __restrict__ pv) {
+__global__ void xpby32_k(long long n, const float* __restrict__ sv, const FcgDev* __restrict__ S,
+                         float* __restrict__ pv) {
+    const float beta = S->beta32;
     const long long n4 = n / 4, stride = (long long)gridDim.x * blockDim.x;
     const long long t0 = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     const float4* s4 = reinterpret_cast<const float4*>(sv);
@@ -849,9 +1023,12 @@ __global__ void xpby32_k(long long n, const float* __restrict__ sv, float beta, 
     }
 }
 
-// e += α p ; r -= α q ; L∞(r) as float bits
-__global__ void update32_k(long long n, float alpha, const float* __restrict__ pv, const float* __restrict__ q,
-                           float* __restrict__ e, float* __restrict__ r, unsigned int* linf) {
+// e += α p ; r -= α q ; L∞(r) as float bits into S->rin (nothing after a breakdown)
+__global__ void update32_k(long long n, FcgDev* __restrict__ S, const float* __restrict__ pv,
+                           const float* __restrict__ q, float* __restrict__ e, float* __restrict__ r) {
+    if (S->stop) return;
+    const float alpha = S->alpha32;
+    unsigned int* linf = &S->rin;
     unsigned long long m = 0ull;
     const long long n4 = n / 4, stride = (long long)gridDim.x * blockDim.x;
     const long long t0 = blockIdx.x * (long long)blockDim.x + threadIdx.x;
@@ -916,10 +1093,27 @@ __global__ void add_scaled_k(Grid g, const double* __restrict__ dots, const floa
 }
 
 // x += e (FP64 += FP32), interior cells
-__global__ void add_correction_k(Grid g, const float* __restrict__ e, double* __restrict__ xv) {
-    ROWS_BEGIN(g)
-    xv[I] += double(e[I]);
-    ROWS_END
+// double(v) with integer operations for zeros, normal numbers, inf and NaN (the conversion instruction
+// issues on the FP64 pipe); FP32 subnormals take the conversion, out of line
+__device__ __noinline__ double widen_cold(float v) { return double(v); }
+__device__ __forceinline__ double widen_exact(float v) {
+    const unsigned b = __float_as_uint(v);
+    return (((b >> 23) & 0xFFu) != 0u || (b << 1) == 0u) ? ff_widen(v) : widen_cold(v);
+}
+
+// x += e over interior cells, on the tiles of matvec32_tile_k (one cell per thread and plane)
+template <int D>
+__global__ void __launch_bounds__(256) add_correction_k(Grid g, const float* __restrict__ e, double* __restrict__ xv) {
+    const int x = 1 + int(blockIdx.x) * 32 + int(threadIdx.x & 31), y = 1 + int(blockIdx.y) * 8 + int(threadIdx.x >> 5);
+    const int z0 = D == 3 ? 1 + MV_ZT * int(blockIdx.z) : 0;
+    if (x > g.n[0] - 2 || y > g.n[1] - 2) return;
+#pragma unroll
+    for (int k = 0; k < (D == 3 ? MV_ZT : 1); ++k) {
+        const int z = z0 + k;
+        if (D == 3 && z > g.n[2] - 2) break;
+        const int I = x + y * int(g.s[1]) + z * int(g.s[2]);
+        xv[I] += widen_exact(e[I]);
+    }
 }
 
 // periodic ghosts of a scalar (WaterLily perBC!), one thread per cell of the boundary planes
@@ -1010,7 +1204,7 @@ static cudaError_t vcycle(ia_handle* h, PoissonMG* mg, int l, cudaStream_t st, i
             int tk = (l == 0) ? timing_begin(h, TK_MG_FINE) : -1;
             tb_launch(mg, ta, 2 * nu1, st);
             timing_end(h, tk);
-            { resid_restrict_k<T, 3><<<cell_grid(C.g), blk(), 0, st>>>(C.g, L.g, Lc, b, L.r32, C.template b_<T>()); ia::note_launch(); }
+            { resid_restrict_k<T, 3><<<cell_grid(C.g), blk(), 0, st>>>(C.g, 1, C.g.n[1] - 1, L.g, Lc, b, L.r32, C.template b_<T>()); ia::note_launch(); }
             cudaError_t e = vcycle<T>(h, mg, l + 1, st, nu1, nu2, nuc);
             if (e != cudaSuccess) return e;
             ta.xin = L.r32;
@@ -1026,77 +1220,125 @@ static cudaError_t vcycle(ia_handle* h, PoissonMG* mg, int l, cudaStream_t st, i
     // the finest mixed level's half-sweeps and residual restriction read the FP16 coefficient copy
     const __half* L16 = nullptr;
     if constexpr (sizeof(T) == 4) L16 = (l == 0 && mg->coef16) ? L.L16 : nullptr;
-    auto half = [&](int color) {
+    auto& C = mg->lev[l + 1];
+    const T om = T(mg->omega);
+    // each launch takes the interior rows [y0, y1)
+    auto rows = [](dim3 gr, int y0, int y1) {
+        gr.y = unsigned((y1 - y0 + 7) / 8);
+        return gr;
+    };
+    auto half = [&](int color, int y0, int y1) {
         const int tk = (l == 0) ? timing_begin(h, TK_MG_FINE) : -1;
+        const dim3 gr = rows(pair_grid(L.g), y0, y1);
         if (L16) {
-            if (L.g.D == 3) rbgs_pair_k<T, 3, false, __half><<<pair_grid(L.g), blk(), 0, st>>>(L.g, L16, b, x, color, T(mg->omega));
-            else rbgs_pair_k<T, 2, false, __half><<<pair_grid(L.g), blk(), 0, st>>>(L.g, L16, b, x, color, T(mg->omega));
+            if (L.g.D == 3) rbgs_pair_k<T, 3, false, __half><<<gr, blk(), 0, st>>>(L.g, y0, y1, L16, b, x, color, om);
+            else rbgs_pair_k<T, 2, false, __half><<<gr, blk(), 0, st>>>(L.g, y0, y1, L16, b, x, color, om);
         } else {
-            if (L.g.D == 3) rbgs_pair_k<T, 3><<<pair_grid(L.g), blk(), 0, st>>>(L.g, Lc, b, x, color, T(mg->omega));
-            else rbgs_pair_k<T, 2><<<pair_grid(L.g), blk(), 0, st>>>(L.g, Lc, b, x, color, T(mg->omega));
+            if (L.g.D == 3) rbgs_pair_k<T, 3><<<gr, blk(), 0, st>>>(L.g, y0, y1, Lc, b, x, color, om);
+            else rbgs_pair_k<T, 2><<<gr, blk(), 0, st>>>(L.g, y0, y1, Lc, b, x, color, om);
         }
         ia::note_launch();
         timing_end(h, tk);
     };
-    auto& C = mg->lev[l + 1];
+    // the relaxed first red half-sweep of a post-smoothing: the red cells still hold x without the
+    // coarse correction, which it adds to the value it reads
+    auto half_prol = [&](int y0, int y1) {
+        const int tk = (l == 0) ? timing_begin(h, TK_MG_FINE) : -1;
+        const dim3 gr = rows(pair_grid(L.g), y0, y1);
+        const T* xc = C.template x_<T>();
+        if (L16 && L.g.D == 3) rbgs_pair_k<T, 3, true, __half><<<gr, blk(), 0, st>>>(L.g, y0, y1, L16, b, x, 0, om, C.g, xc);
+        else if (L16) rbgs_pair_k<T, 2, true, __half><<<gr, blk(), 0, st>>>(L.g, y0, y1, L16, b, x, 0, om, C.g, xc);
+        else if (L.g.D == 3) rbgs_pair_k<T, 3, true><<<gr, blk(), 0, st>>>(L.g, y0, y1, Lc, b, x, 0, om, C.g, xc);
+        else rbgs_pair_k<T, 2, true><<<gr, blk(), 0, st>>>(L.g, y0, y1, Lc, b, x, 0, om, C.g, xc);
+        ia::note_launch();
+        timing_end(h, tk);
+    };
     // over-relaxed updates read the cell's own previous value: the red values of the first sweep
     // are then stored, and the post-smoothing's first red half-sweep adds the coarse correction
     // to the value it reads
     const bool relax = mg->omega != 1.0;
     const int write_red = (nu1 == 1 || relax) ? 1 : 0;
     // first black half-sweep: from x = 0 (pre) or from x + P(x_coarse) (post)
-    auto first = [&](bool prol) {
+    auto first = [&](bool prol, int y0, int y1) {
         const int tk = (l == 0) ? timing_begin(h, TK_MG_FIRST) : -1;
+        const dim3 gr = rows(pair_grid(L.g), y0, y1);
         const T* xc = C.template x_<T>();
+        const int wr = prol ? 0 : write_red;
         if (L16 && L.g.D == 3) {
-            if (prol) rbgs_first_k<T, 3, true, __half><<<pair_grid(L.g), blk(), 0, st>>>(L.g, C.g, L16, b, iD, xc, x, 0, T(mg->omega));
-            else rbgs_first_k<T, 3, false, __half><<<pair_grid(L.g), blk(), 0, st>>>(L.g, C.g, L16, b, iD, xc, x, write_red, T(mg->omega));
+            if (prol) rbgs_first_k<T, 3, true, __half><<<gr, blk(), 0, st>>>(L.g, y0, y1, C.g, L16, b, iD, xc, x, wr, om);
+            else rbgs_first_k<T, 3, false, __half><<<gr, blk(), 0, st>>>(L.g, y0, y1, C.g, L16, b, iD, xc, x, wr, om);
         } else if (L16) {
-            if (prol) rbgs_first_k<T, 2, true, __half><<<pair_grid(L.g), blk(), 0, st>>>(L.g, C.g, L16, b, iD, xc, x, 0, T(mg->omega));
-            else rbgs_first_k<T, 2, false, __half><<<pair_grid(L.g), blk(), 0, st>>>(L.g, C.g, L16, b, iD, xc, x, write_red, T(mg->omega));
+            if (prol) rbgs_first_k<T, 2, true, __half><<<gr, blk(), 0, st>>>(L.g, y0, y1, C.g, L16, b, iD, xc, x, wr, om);
+            else rbgs_first_k<T, 2, false, __half><<<gr, blk(), 0, st>>>(L.g, y0, y1, C.g, L16, b, iD, xc, x, wr, om);
         } else if (L.g.D == 3) {
-            if (prol) rbgs_first_k<T, 3, true><<<pair_grid(L.g), blk(), 0, st>>>(L.g, C.g, Lc, b, iD, xc, x, 0, T(mg->omega));
-            else rbgs_first_k<T, 3, false><<<pair_grid(L.g), blk(), 0, st>>>(L.g, C.g, Lc, b, iD, xc, x, write_red, T(mg->omega));
+            if (prol) rbgs_first_k<T, 3, true><<<gr, blk(), 0, st>>>(L.g, y0, y1, C.g, Lc, b, iD, xc, x, wr, om);
+            else rbgs_first_k<T, 3, false><<<gr, blk(), 0, st>>>(L.g, y0, y1, C.g, Lc, b, iD, xc, x, wr, om);
         } else {
-            if (prol) rbgs_first_k<T, 2, true><<<pair_grid(L.g), blk(), 0, st>>>(L.g, C.g, Lc, b, iD, xc, x, 0, T(mg->omega));
-            else rbgs_first_k<T, 2, false><<<pair_grid(L.g), blk(), 0, st>>>(L.g, C.g, Lc, b, iD, xc, x, write_red, T(mg->omega));
+            if (prol) rbgs_first_k<T, 2, true><<<gr, blk(), 0, st>>>(L.g, y0, y1, C.g, Lc, b, iD, xc, x, wr, om);
+            else rbgs_first_k<T, 2, false><<<gr, blk(), 0, st>>>(L.g, y0, y1, C.g, Lc, b, iD, xc, x, wr, om);
         }
         ia::note_launch();
         timing_end(h, tk);
     };
-    first(false);
-    for (int k = 1; k < nu1; ++k) {
-        half(0);
-        half(1);
-    }
-    if (L16 && L.g.D == 3) resid_restrict_k<T, 3, __half><<<cell_grid(C.g), blk(), 0, st>>>(C.g, L.g, L16, b, x, C.template b_<T>());
-    else if (L16) resid_restrict_k<T, 2, __half><<<cell_grid(C.g), blk(), 0, st>>>(C.g, L.g, L16, b, x, C.template b_<T>());
-    else if (L.g.D == 3) resid_restrict_k<T, 3><<<cell_grid(C.g), blk(), 0, st>>>(C.g, L.g, Lc, b, x, C.template b_<T>());
-    else resid_restrict_k<T, 2><<<cell_grid(C.g), blk(), 0, st>>>(C.g, L.g, Lc, b, x, C.template b_<T>());
-    ia::note_launch();
+    // residual restriction of the coarse rows [yc0, yc1)
+    auto restrict_rows = [&](int yc0, int yc1) {
+        const dim3 gr = rows(cell_grid(C.g), yc0, yc1);
+        T* bc = C.template b_<T>();
+        if (L16 && L.g.D == 3) resid_restrict_k<T, 3, __half><<<gr, blk(), 0, st>>>(C.g, yc0, yc1, L.g, L16, b, x, bc);
+        else if (L16) resid_restrict_k<T, 2, __half><<<gr, blk(), 0, st>>>(C.g, yc0, yc1, L.g, L16, b, x, bc);
+        else if (L.g.D == 3) resid_restrict_k<T, 3><<<gr, blk(), 0, st>>>(C.g, yc0, yc1, L.g, Lc, b, x, bc);
+        else resid_restrict_k<T, 2><<<gr, blk(), 0, st>>>(C.g, yc0, yc1, L.g, Lc, b, x, bc);
+        ia::note_launch();
+    };
+    // A smoothing is a chain of stages, each a half-sweep of one colour that reads the previous
+    // stage's values in rows y-1 .. y+1 (and its own colour's values from two stages back).  On the
+    // finest FP32 level with walls in y, the chain runs as a wavefront over slabs of slab_rows rows:
+    // for slab k the stage s takes rows [a_k - s, a_(k+1) - s), one row behind stage s-1, so every row
+    // a stage reads is final for its predecessor and not yet rewritten by its successor (red-black
+    // updates read only the other colour).  The results are those of whole-level half-sweeps, bit for
+    // bit, while a slab's rows are still in L2 for the next stage.  The restriction follows with the
+    // coarse rows whose fine rows (and their neighbours) are final.
+    const bool slab = sizeof(T) == 4 && l == 0 && mg->slab_rows > 0 && L.g.D == 3 && !L.g.isper(1) &&
+                      L.g.n[1] - 2 > mg->slab_rows;
+    auto chain = [&](int S, auto&& stage, bool with_restrict) {
+        const int ny = L.g.n[1] - 2, yend = L.g.n[1] - 1;
+        const int R = slab ? std::max(mg->slab_rows, 2 * S) : ny;
+        const int K = (ny + R - 1) / R;
+        int yc_done = 1;
+        for (int k = 0; k < K; ++k) {
+            const bool lastk = k + 1 == K;
+            const int a0 = 1 + k * R, a1 = lastk ? yend : 1 + (k + 1) * R;
+            for (int s = 0; s < S; ++s) {
+                const int y0 = (k == 0) ? 1 : a0 - s, y1 = lastk ? yend : a1 - s;
+                if (y1 > y0) stage(s, y0, y1);
+            }
+            if (with_restrict) {
+                const int yc1 = lastk ? C.g.n[1] - 1 : std::min(C.g.n[1] - 1, (a1 - S - 1) / 2 + 1);
+                if (yc1 > yc_done) {
+                    restrict_rows(yc_done, yc1);
+                    yc_done = yc1;
+                }
+            }
+        }
+    };
+    // pre-smoothing: first (black with the red values in place), then (red, black) nu1 - 1 times
+    chain(2 * nu1 - 1, [&](int s, int y0, int y1) {
+        if (s == 0) first(false, y0, y1);
+        else half((s & 1) ? 0 : 1, y0, y1);
+    }, true);
     cudaError_t e = vcycle<T>(h, mg, l + 1, st, nu1, nu2, nuc);
     if (e != cudaSuccess) return e;
     if (nu2 == 0) {
         { prolong_k<T><<<grd(L.g), blk(), 0, st>>>(L.g, C.g, C.template x_<T>(), x); ia::note_launch(); }
         return cudaGetLastError();
     }
-    first(true);
-    if (relax) {   // the red cells still hold x without the coarse correction
-        const int tk = (l == 0) ? timing_begin(h, TK_MG_FINE) : -1;
-        const T* xc = C.template x_<T>();
-        if (L16 && L.g.D == 3) rbgs_pair_k<T, 3, true, __half><<<pair_grid(L.g), blk(), 0, st>>>(L.g, L16, b, x, 0, T(mg->omega), C.g, xc);
-        else if (L16) rbgs_pair_k<T, 2, true, __half><<<pair_grid(L.g), blk(), 0, st>>>(L.g, L16, b, x, 0, T(mg->omega), C.g, xc);
-        else if (L.g.D == 3) rbgs_pair_k<T, 3, true><<<pair_grid(L.g), blk(), 0, st>>>(L.g, Lc, b, x, 0, T(mg->omega), C.g, xc);
-        else rbgs_pair_k<T, 2, true><<<pair_grid(L.g), blk(), 0, st>>>(L.g, Lc, b, x, 0, T(mg->omega), C.g, xc);
-        ia::note_launch();
-        timing_end(h, tk);
-    } else {
-        half(0);
-    }
-    for (int k = 1; k < nu2; ++k) {
-        half(1);
-        half(0);
-    }
+    // post-smoothing: first (black from x + P(x_coarse)), red (adding the correction when relaxed),
+    // then (black, red) nu2 - 1 times
+    chain(2 * nu2, [&](int s, int y0, int y1) {
+        if (s == 0) first(true, y0, y1);
+        else if (s == 1 && relax) half_prol(y0, y1);
+        else half((s & 1) ? 0 : 1, y0, y1);
+    }, false);
     return cudaGetLastError();
 }
 
@@ -1107,7 +1349,8 @@ static cudaError_t vcycle_run(ia_handle* h, PoissonMG* mg, cudaStream_t st) {
     const int k = sizeof(T) == 4 ? 0 : 1;
     int* nu = mg->vgraph_nu[k];
     if (mg->vgraph[k] && (nu[0] != mg->nu1 || nu[1] != mg->nu2 || nu[2] != mg->nuc || nu[3] != mg->smoother ||
-                          mg->vgraph_omega[k] != mg->omega || mg->vgraph_c16[k] != mg->coef16)) {
+                          mg->vgraph_omega[k] != mg->omega || mg->vgraph_c16[k] != mg->coef16 ||
+                          mg->vgraph_slab[k] != mg->slab_rows)) {
         cudaGraphExecDestroy(mg->vgraph[k]);
         mg->vgraph[k] = nullptr;
     }
@@ -1138,6 +1381,7 @@ static cudaError_t vcycle_run(ia_handle* h, PoissonMG* mg, cudaStream_t st) {
         nu[3] = mg->smoother;
         mg->vgraph_omega[k] = mg->omega;
         mg->vgraph_c16[k] = mg->coef16;
+        mg->vgraph_slab[k] = mg->slab_rows;
     }
     note_launches(mg->vgraph_kernels[k]);
     return cudaGraphLaunch(mg->vgraph[k], st);
@@ -1148,6 +1392,19 @@ static cudaError_t vcycle_run(ia_handle* h, PoissonMG* mg, cudaStream_t st) {
 bool coef16_fits(double lrho) {
     const double lo = lrho < 1.0 ? lrho : 1.0, hi = lrho < 1.0 ? 1.0 : lrho;
     return lo > 0.0 && 1.0 / lo <= 60000.0 && 1.0 / hi >= 1e-4;
+}
+
+// Rows per slab of the finest-level wavefront: the bytes a stage touches per interior row (x, b, the
+// inverse diagonal and the coefficients) times the rows of a slab within about 3/5 of L2, a multiple of
+// 8 rows (measured at 256x512x256: 64 rows 45.7 ms per step, 32 rows 47.0, 16 rows 49.9, whole-level
+// half-sweeps 46.3: smaller slabs lose more to launches and partial blocks than they gain in L2 hits).
+// 0 (whole-level half-sweeps) where the wavefront does not apply.
+static int default_slab_rows(const Grid& g, bool mixed, bool c16, long long l2_bytes) {
+    if (!mixed || g.D != 3 || g.isper(1) || l2_bytes <= 0) return 0;
+    const long long row = (long long)(g.n[0] - 2) * (g.n[2] - 2) * (4 + 4 + 4 + (c16 ? 6 : 12));
+    const long long rows = ((l2_bytes * 3 / 5) / std::max(row, 1LL)) / 8 * 8;   // whole 8-row blocks at every lag
+    if (rows < 8 || rows >= g.n[1] - 2) return 0;
+    return int(rows);
 }
 
 int mg_create(ia_handle* h) {
@@ -1211,7 +1468,11 @@ int mg_create(ia_handle* h) {
     e = e ? e : cudaMalloc(&mg->p, 8 * N);
     e = e ? e : cudaMalloc(&mg->q, 8 * N);
     mg->kb = kblocks(g0);
-    e = e ? e : cudaMalloc(&mg->partial, 8 * 2 * (size_t)KBLOCKS);
+    {
+        const dim3 mv = mv_tile_grid(g0);
+        mg->mvb = (long long)mv.x * mv.y * mv.z;
+    }
+    e = e ? e : cudaMalloc(&mg->partial, 8 * std::max<size_t>(2 * (size_t)KBLOCKS, (size_t)mg->mvb));
     e = e ? e : cudaMalloc(&mg->diag64, 8 * N);
     if (!e) cudaMemset(mg->diag64, 0, 8 * N);
     if (mixed) {
@@ -1235,6 +1496,8 @@ int mg_create(ia_handle* h) {
         }
     }
     e = e ? e : cudaMalloc(&mg->dsc, 8 * 16);
+    e = e ? e : cudaMalloc(&mg->fcg, sizeof(FcgDev));
+    if (!e) cudaMemset(mg->fcg, 0, sizeof(FcgDev));
     e = e ? e : cudaMallocHost(&mg->hsc, 8 * 16);
     if (e != cudaSuccess) return IA_ERR_CUDA;
     cudaMemset(mg->r, 0, 8 * N);
@@ -1245,9 +1508,11 @@ int mg_create(ia_handle* h) {
     mg->nu2 = 2;
     mg->nuc = 16;
     {
-        int dev = 0;
+        int dev = 0, l2 = 0;
         cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&mg->nsm, cudaDevAttrMultiProcessorCount, dev);
+        cudaDeviceGetAttribute(&l2, cudaDevAttrL2CacheSize, dev);
+        mg->slab_rows = default_slab_rows(g0, mixed, mg->coef16 != 0, (long long)l2);
     }
     return IA_OK;
 }
@@ -1263,7 +1528,7 @@ void mg_destroy(ia_handle* h) {
     cudaFree(mg->r); cudaFree(mg->s); cudaFree(mg->p); cudaFree(mg->q);
     cudaFree(mg->p32); cudaFree(mg->q32); cudaFree(mg->e32);
     cudaFree(mg->rl32); cudaFree(mg->nl32); cudaFree(mg->t32);
-    cudaFree(mg->partial); cudaFree(mg->dsc); cudaFree(mg->diag64);
+    cudaFree(mg->partial); cudaFree(mg->dsc); cudaFree(mg->fcg); cudaFree(mg->diag64);
     for (int k = 0; k < 2; ++k)
         if (mg->vgraph[k]) cudaGraphExecDestroy(mg->vgraph[k]);
     if (mg->capture) cudaStreamDestroy(mg->capture);
@@ -1279,7 +1544,7 @@ static cudaError_t mg_setup(ia_handle* h, const double* L0) {
     const bool mixed = h->cfg.poisson_mode != IA_POISSON_FP64;
     MGLevel& F = mg->lev[0];
     const long long nv = F.g.N * F.g.D;
-    { set_diag64_k<<<mg->kb, KTHREADS, 0, st>>>(F.g, L0, mg->diag64); ia::note_launch(); }
+    if (!mixed) { set_diag64_k<<<mg->kb, KTHREADS, 0, st>>>(F.g, L0, mg->diag64); ia::note_launch(); }
     if (!mixed) {
         cudaMemcpyAsync(F.L, L0, 8 * nv, cudaMemcpyDeviceToDevice, st);
         { set_diag_k<double><<<grd(F.g), blk(), 0, st>>>(F.g, F.L, F.iD); ia::note_launch(); }
@@ -1289,11 +1554,10 @@ static cudaError_t mg_setup(ia_handle* h, const double* L0) {
             { set_diag_k<double><<<grd(mg->lev[l].g), blk(), 0, st>>>(mg->lev[l].g, mg->lev[l].L, mg->lev[l].iD); ia::note_launch(); }
         }
     } else {
-        // the FP64 -> FP32 conversion runs in a memory-bound pass of its own: conversions issue on
-        // the FP64 pipe, which the FP64 diagonal pass already saturates
-        { to_f32_k<<<1216, 256, 0, st>>>(nv, L0, F.L32); ia::note_launch(); }
-        if (mg->coef16) { to_f16_k<<<1216, 256, 0, st>>>(nv, F.L32, F.L16); ia::note_launch(); }
-        { set_diag_k<float><<<grd(F.g), blk(), 0, st>>>(F.g, F.L32, F.iD32); ia::note_launch(); }
+        // FP64 diagonal, FP32 (and FP16) coefficient copies and the FP32 inverse diagonal in one pass
+        const dim3 gg((F.g.n[0] + 31) / 32, (F.g.n[1] + 7) / 8, F.g.D == 3 ? F.g.n[2] : 1);
+        __half* l16 = mg->coef16 ? F.L16 : nullptr;
+        LAUNCH_D(F.g, setup_fine_k, gg, blk(), F.g, L0, mg->diag64, F.L32, l16, F.iD32);
         for (int l = 1; l < mg->nlev; ++l) {
             { restrict_L_k<float><<<grd(mg->lev[l].g), blk(), 0, st>>>(mg->lev[l].g, mg->lev[l - 1].g,
                                                                       mg->lev[l - 1].L32, mg->lev[l].L32); ia::note_launch(); }
@@ -1330,6 +1594,15 @@ static cudaError_t mg_precondition(ia_handle* h) {
     return cudaGetLastError();
 }
 
+// r = z - A x with the FP64 operator and the precomputed diagonal; L∞(r), as the bit pattern of |r|,
+// into *dlinf
+static void true_residual(PoissonMG* mg, const Grid& g, const double* L, const double* zz, const double* xv,
+                          unsigned long long* dlinf, cudaStream_t st) {
+    unsigned long long* pmax = reinterpret_cast<unsigned long long*>(mg->partial);
+    LAUNCH_D(g, true_resid_tile_k, mv_tile_grid(g), KTHREADS, g, L, mg->diag64, zz, xv, mg->r, pmax);
+    { finalize_max_k<<<1, 1024, 0, st>>>(pmax, mg->mvb, dlinf); ia::note_launch(); }
+}
+
 static double read_linf(ia_handle* h, unsigned long long* dlinf) {
     unsigned long long v = 0;
     cudaMemcpyAsync(&h->mg->hsc[0], dlinf, 8, cudaMemcpyDeviceToHost, h->stream);
@@ -1338,16 +1611,6 @@ static double read_linf(ia_handle* h, unsigned long long* dlinf) {
     double d;
     std::memcpy(&d, &v, 8);
     return d;
-}
-
-static double read_linf32(ia_handle* h, unsigned int* d) {
-    unsigned int v = 0;
-    cudaMemcpyAsync(&h->mg->hsc[0], d, 4, cudaMemcpyDeviceToHost, h->stream);
-    cudaStreamSynchronize(h->stream);
-    std::memcpy(&v, &h->mg->hsc[0], 4);
-    float f;
-    std::memcpy(&f, &v, 4);
-    return double(f);
 }
 
 // Mixed precision: FP64 defect correction x += e, e from an inner flexible CG run
@@ -1364,8 +1627,6 @@ static int poisson_solve_mixed(ia_handle* h, double* xv, const double* zz, const
     MGLevel& F = mg->lev[0];
     const long long N = g.N;
     unsigned long long* dlinf = reinterpret_cast<unsigned long long*>(mg->dsc + 8);
-    unsigned int* dlinf32 = reinterpret_cast<unsigned int*>(mg->dsc + 9);
-    double* dots = mg->dsc;
     double* hdots = mg->dsc + 12;                                  // hybrid n·t, n·An
     const bool learned = h->cfg.poisson_mode == IA_POISSON_LEARNED;
     // inner residual: the V-cycle reads its right-hand side from F.b32, so the plain mixed
@@ -1415,9 +1676,8 @@ static int poisson_solve_mixed(ia_handle* h, double* xv, const double* zz, const
         return cudaGetLastError() == cudaSuccess;
     };
     int total = 0;
-    cudaMemsetAsync(dlinf, 0, 8, st);
     int tk = timing_begin(h, TK_KRYLOV);
-    LAUNCH_D(g, true_resid_k, mg->kb, KTHREADS, g, L, mg->diag64, zz, xv, mg->r, dlinf);
+    true_residual(mg, g, L, zz, xv, dlinf, st);
     timing_end(h, tk);
     double res = read_linf(h, dlinf);
     while (!(res <= tol) && total < itmx) {
@@ -1426,43 +1686,36 @@ static int poisson_solve_mixed(ia_handle* h, double* xv, const double* zz, const
         { zero_k<float><<<1216, 256, 0, st>>>(N, mg->e32); ia::note_launch(); }
         timing_end(h, tk);
         const double target = std::fmax(0.5 * tol / res, mg->inner_rtol) * res;
-        double rho_prev = 0.0, alpha_prev = 0.0;
+        FcgDev* S = mg->fcg;
         for (int it = 0; it < mg->inner_max && total < itmx; ++it) {
             float* sv = nullptr;
             if (!precond(sv)) return IA_ERR_CUDA;
+            // β, the direction, q = A p, α and the update without a host round trip; one read-back of
+            // the inner residual and the breakdown flag per step
             tk = timing_begin(h, TK_KRYLOV);
             { dot2_32_k<<<mg->kb, KTHREADS, 0, st>>>(N, sv, mg->q32, rr, mg->partial); ia::note_launch(); }
-            { finalize_k<<<1, 1024, 0, st>>>(mg->partial, mg->kb, 2, dots); ia::note_launch(); }
+            { fcg_beta_k<<<1, 1024, 0, st>>>(mg->partial, mg->kb, S, it == 0 ? 1 : 0); ia::note_launch(); }
+            { xpby32_k<<<mg->kb, KTHREADS, 0, st>>>(N, sv, S, mg->p32); ia::note_launch(); }
+            LAUNCH_D(g, matvec32_tile_k, mv_tile_grid(g), KTHREADS, g, F.L32, mg->p32, mg->q32, mg->partial);
+            { fcg_alpha_k<<<1, 1024, 0, st>>>(mg->partial, mg->mvb, S); ia::note_launch(); }
+            { update32_k<<<mg->kb, KTHREADS, 0, st>>>(N, S, mg->p32, mg->q32, mg->e32, rr); ia::note_launch(); }
             timing_end(h, tk);
-            cudaMemcpyAsync(mg->hsc + 2, dots, 16, cudaMemcpyDeviceToHost, st);
+            cudaMemcpyAsync(mg->hsc + 2, &S->rin, 8, cudaMemcpyDeviceToHost, st);
             if (cudaStreamSynchronize(st) != cudaSuccess) return IA_ERR_CUDA;
-            const double sq = mg->hsc[2], sr = mg->hsc[3];
-            const double beta = (it == 0) ? 0.0 : (-alpha_prev * sq) / rho_prev;
-            tk = timing_begin(h, TK_KRYLOV);
-            { xpby32_k<<<mg->kb, KTHREADS, 0, st>>>(N, sv, float(beta), mg->p32); ia::note_launch(); }
-            LAUNCH_D(g, matvec32_dot_k, mg->kb, KTHREADS, g, F.L32, mg->p32, mg->q32, mg->partial);
-            { finalize_k<<<1, 1024, 0, st>>>(mg->partial, mg->kb, 1, dots); ia::note_launch(); }
-            timing_end(h, tk);
-            cudaMemcpyAsync(mg->hsc + 2, dots, 8, cudaMemcpyDeviceToHost, st);
-            if (cudaStreamSynchronize(st) != cudaSuccess) return IA_ERR_CUDA;
-            const double pq = mg->hsc[2];
+            unsigned int rin_bits = 0;
+            int stop = 0;
+            std::memcpy(&rin_bits, reinterpret_cast<const char*>(mg->hsc + 2), 4);
+            std::memcpy(&stop, reinterpret_cast<const char*>(mg->hsc + 2) + 4, 4);
             ++total;
             mg->stats[3]++;
-            if (!(pq != 0.0) || !std::isfinite(pq) || !std::isfinite(sr) || !std::isfinite(beta)) break;
-            const double alpha = sr / pq;
-            cudaMemsetAsync(dlinf32, 0, 4, st);
-            tk = timing_begin(h, TK_KRYLOV);
-            { update32_k<<<mg->kb, KTHREADS, 0, st>>>(N, float(alpha), mg->p32, mg->q32, mg->e32, rr, dlinf32); ia::note_launch(); }
-            timing_end(h, tk);
-            const double rin = read_linf32(h, dlinf32);
-            rho_prev = sr;
-            alpha_prev = alpha;
-            if (rin <= target) break;
+            if (stop) break;
+            float rinf;
+            std::memcpy(&rinf, &rin_bits, 4);
+            if (double(rinf) <= target) break;
         }
         tk = timing_begin(h, TK_KRYLOV);
-        { add_correction_k<<<mg->kb, KTHREADS, 0, st>>>(g, mg->e32, xv); ia::note_launch(); }
-        cudaMemsetAsync(dlinf, 0, 8, st);
-        LAUNCH_D(g, true_resid_k, mg->kb, KTHREADS, g, L, mg->diag64, zz, xv, mg->r, dlinf);
+        LAUNCH_D(g, add_correction_k, mv_tile_grid(g), KTHREADS, g, mg->e32, xv);
+        true_residual(mg, g, L, zz, xv, dlinf, st);
         timing_end(h, tk);
         const double res_old = res;
         res = read_linf(h, dlinf);
@@ -1509,9 +1762,8 @@ int poisson_solve(ia_handle* h, double* xv, const double* zz, const double* L, d
     if (mg_setup(h, L) != cudaSuccess) return IA_ERR_CUDA;
     unsigned long long* dlinf = reinterpret_cast<unsigned long long*>(mg->dsc + 8);
     double* dots = mg->dsc;
-    cudaMemsetAsync(dlinf, 0, 8, st);
     int tk = timing_begin(h, TK_KRYLOV);
-    LAUNCH_D(g, true_resid_k, mg->kb, KTHREADS, g, L, mg->diag64, zz, xv, mg->r, dlinf);
+    true_residual(mg, g, L, zz, xv, dlinf, st);
     timing_end(h, tk);
     double res = read_linf(h, dlinf);
     int it = 0;

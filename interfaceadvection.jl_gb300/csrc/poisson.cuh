@@ -11,6 +11,16 @@ namespace ia {
 
 constexpr int MG_MAX_LEVELS = 12;
 
+// Step scalars of the mixed solver's inner FCG, kept on the device so that only the convergence test
+// is read back each iteration: β and α in FP64 (and as the FP32 values the vector kernels use), the
+// previous step's α and s·r, the stop flag of a breakdown, and L∞ of the inner residual (FP32 bits).
+struct FcgDev {
+    double alpha_prev, rho_prev, sr, beta;
+    float beta32, alpha32;
+    unsigned int rin;   // read back together with stop (8 bytes)
+    int stop;
+};
+
 struct MGLevel {
     Grid g;
     // FP64 operator and vectors (IA_POISSON_FP64)
@@ -49,14 +59,17 @@ struct PoissonMG {
     int inner_max = 30;                                               // inner FCG iterations per correction
     double inner_rtol = 1e-3;                                         // inner relative residual target
     double* partial = nullptr;                                        // per-block dot partials
+    long long mvb = 0;                                                // blocks (partials) of the tiled FP32 matvec
     int kb = 0;                                                       // blocks of the Krylov row loops
     double* diag64 = nullptr;                                         // FP64 operator diagonal
     double* dsc = nullptr;                                            // device scalars
+    ia::FcgDev* fcg = nullptr;                                        // the inner FCG's step scalars
     double* hsc = nullptr;                                            // pinned host scalars
     int nu1 = 2, nu2 = 2, nuc = 16;
     int smoother = 0;                                                 // IA_SMOOTHER_* (FP32 V-cycle)
     double omega = 1.15;                                              // smoother relaxation factor
     int coef16 = 0;                                                   // finest-level smoother on L16 (mixed)
+    int slab_rows = 0;                                                // finest-level wavefront slab (rows; 0 off)
     int nsm = 0;                                                      // multiprocessors of the device
     // each precision's finest-level V-cycle is captured once into a CUDA graph (its launch
     // sequence and arguments are fixed for the handle) and replayed; recaptured when the
@@ -66,6 +79,7 @@ struct PoissonMG {
     int vgraph_nu[2][4] = {{0, 0, 0, 0}, {0, 0, 0, 0}};
     double vgraph_omega[2] = {1.0, 1.0};
     int vgraph_c16[2] = {0, 0};
+    int vgraph_slab[2] = {0, 0};
     cudaStream_t capture = nullptr;
 };
 

@@ -385,6 +385,13 @@ int ia_poisson_coef16(ia_handle* h, int32_t on) {
     return IA_OK;
 }
 
+int ia_poisson_slab_rows(ia_handle* h, int32_t rows) {
+    if (!h || rows < 0 || (rows > 0 && rows < 8)) return IA_ERR_INVALID;
+    if (ensure_scratch(h) != IA_OK) return IA_ERR_CUDA;
+    h->mg->slab_rows = rows;
+    return IA_OK;
+}
+
 int ia_poisson_stats(ia_handle* h, int64_t* out5) {
     if (!h || !out5) return IA_ERR_INVALID;
     for (int i = 0; i < 5; ++i) out5[i] = h->mg ? h->mg->stats[i] : 0;

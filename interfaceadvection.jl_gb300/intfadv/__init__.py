@@ -13,11 +13,11 @@ from .fields import cell_coords, face_coords, ffrom, fones, fzeros, is_fortran
 from .levelset import LevelSet, computeL, redistaning
 from .vtk import VTKWriter
 from .vtk import load as load_vtk
-from .simulation import (MPCFL, MPFMomStep, NoBody, TwoPhaseSimulation, poisson_stats, set_learned, set_momentum_arith, set_poisson_coef16, set_smoother, sim_info,
+from .simulation import (MPCFL, MPFMomStep, NoBody, TwoPhaseSimulation, poisson_stats, set_learned, set_momentum_arith, set_poisson_coef16, set_poisson_slab_rows, set_smoother, sim_info,
                          sim_step, surfTen)
 
 __all__ = ["Flow", "Handle", "advect", "advect_vof_raw", "advectVOF", "apply_vof", "applyVOF", "cVOF",
            "get_vof_flux", "getVOFFlux", "make_config", "reconstruct_interface", "reconstructInterface", "build",
            "cell_coords", "face_coords", "ffrom", "fones", "fzeros", "is_fortran", "MPCFL", "MPFMomStep", "NoBody",
-           "TwoPhaseSimulation", "sim_info", "sim_step", "surfTen", "poisson_stats", "set_learned", "set_momentum_arith", "set_poisson_coef16", "set_smoother", "metrics", "sim_metrics", "LevelSet", "redistaning",
+           "TwoPhaseSimulation", "sim_info", "sim_step", "surfTen", "poisson_stats", "set_learned", "set_momentum_arith", "set_poisson_coef16", "set_poisson_slab_rows", "set_smoother", "metrics", "sim_metrics", "LevelSet", "redistaning",
            "computeL", "VTKWriter", "load_vtk"]

@@ -114,6 +114,12 @@ def set_poisson_coef16(handle, on: bool) -> None:
     _lib.check(handle.call("ia_poisson_coef16", C.c_int32(1 if on else 0)), "ia_poisson_coef16")
 
 
+def set_poisson_slab_rows(handle, rows: int) -> None:
+    """Rows per slab of the finest-level smoothing wavefront (ia_poisson_slab_rows; 0 = whole-level
+    half-sweeps); the results do not depend on it."""
+    _lib.check(handle.call("ia_poisson_slab_rows", C.c_int32(int(rows))), "ia_poisson_slab_rows")
+
+
 def set_smoother(handle, kind: str = "halfsweep", omega: float | None = None) -> None:
     """Smoother of the FP32 V-cycle: "halfsweep" (one launch per red-black half-sweep, the default)
     or "blocked" (all half-sweeps of a smoothing in one z-wavefront launch, relaxation factor 1 only);

@@ -9,6 +9,7 @@
 // (split inputs carry |lo| up to one ulp of hi, so the dropped lo·lo term and the roundings of the
 // FMA chain reach about 9 u in a product)
 //   widen:       exact for every normal FP32 number
+//   f32_rn:      float(v) bit for bit (round to nearest even)
 //   order:       ff_lt agrees with the order of the values unless they are within 8 u of each other
 // plus an absolute 2^-140 on every result: below about 2^-100 the low part of a pair reaches the FP32
 // subnormal range and the relative bound no longer holds (operands here span 2^-60 .. 2^60, so products
@@ -16,6 +17,7 @@
 // Exit status 0 on success.
 #include <cmath>
 #include <cstdint>
+#include <cfloat>
 #include <cstdio>
 #include <random>
 
@@ -84,6 +86,24 @@ int main() {
         if (std::fabs(ff_join(ff_split(x)) - x) > us * std::fabs(x)) fail("fixed", x, 0, ff_join(ff_split(x)), x);
     if (!ff_pos(ff_split(1e-20)) || ff_pos(ff_split(-0.0)) || ff_pos(ff_split(0.0)) || !ff_neg(ff_split(-2.0)))
         fail("sign", 0, 0, 0, 0);
+    // f32_rn is float(v) bit for bit: random patterns over every exponent and around the FP32 range,
+    // exact ties (both parities), carries into the exponent, the largest finite values and zeros
+    auto same = [](float x, float y) { return ff_fbits(x) == ff_fbits(y) || (std::isnan(x) && std::isnan(y)); };
+    std::uniform_int_distribution<uint64_t> b64(0, ~0ull);
+    std::uniform_int_distribution<int> enear(880, 1160);
+    for (int it = 0; it < 4000000; ++it) {
+        uint64_t w = b64(rng);
+        if (it & 1) w = (w & 0x800FFFFFFFFFFFFFull) | (uint64_t(enear(rng)) << 52);
+        if ((it & 7) == 2) w = (w & ~0x1FFFFFFFull) | 0x10000000ull;   // a tie
+        if ((it & 7) == 4) w |= 0x000FFFFFE0000000ull;                   // top 23 bits all ones
+        const double v = ff_bitsd(w);
+        if (!same(f32_rn(v), (float)v)) fail("f32_rn", v, 0, f32_rn(v), (float)v);
+    }
+    for (double v : {0.0, -0.0, 1.0, -1.0, 1e-3, 1000.0, (double)FLT_MAX, -(double)FLT_MAX,
+                     std::nextafter((double)FLT_MAX, INFINITY), 3.4028235677973366e38, 3.4028235677973362e38,
+                     (double)FLT_MIN, std::nextafter((double)FLT_MIN, 0.0), 1e-45, 1e-300, 1e300, (double)INFINITY,
+                     -(double)INFINITY, (double)NAN})
+        if (!same(f32_rn(v), (float)v)) fail("f32_rn fixed", v, 0, f32_rn(v), (float)v);
     std::printf(bad ? "FAIL %d\n" : "ok\n", bad);
     return bad != 0;
 }

@@ -34,10 +34,12 @@ def system(dims, perdir):
     return sim.flow.mu0.clone(), sim.flow.sigma.clone()
 
 
-def solve(dims, perdir, L, z, smoother, nu=(2, 2), omega=1.0, coef16=False):
+def solve(dims, perdir, L, z, smoother, nu=(2, 2), omega=1.0, coef16=False, slab=0):
     # the smoother comparisons run on the FP32 coefficients (the blocked smoother has no FP16 form)
+    # and whole-level half-sweeps (slab 0) unless asked
     h = ia.Handle(ia.make_config(dims, perdir=perdir, poisson="mixed", lrho=1e-3))
     ia.set_poisson_coef16(h, coef16)
+    ia.set_poisson_slab_rows(h, slab)
     ia.set_smoother(h, smoother, omega)
     _lib.check(h.call("ia_poisson_mg_params", nu[0], nu[1], 16), "ia_poisson_mg_params")
     x = fzeros(z.shape)
@@ -119,3 +121,34 @@ def test_fp16_smoother_coefficients_give_the_same_step(cuda):
     du = float((a.flow.u - b.flow.u).abs().max()) / float(a.flow.u.abs().max())
     assert du < 1e-10, du
     assert all(abs(x - y) <= 2 for x, y in zip(ia_, ib)), (ia_, ib)
+
+
+@pytest.mark.parametrize("nu", [(2, 2), (1, 1), (1, 2), (3, 2)])
+@pytest.mark.parametrize("slab,coef16", [(8, True), (11, False), (16, True)])
+def test_slab_wavefront_is_bit_identical(cuda, nu, slab, coef16):
+    # the finest level's half-sweeps and restriction run slab by slab over y, each stage one row behind
+    # the previous (ia_poisson_slab_rows): the same updates as whole-level half-sweeps, so the same
+    # pressure bit for bit and the same iteration count; 46 interior rows leave a short last slab
+    dims, perdir = (40, 46, 24), (0, 2)
+    L, z = system(dims, perdir)
+    xa, ita, resa, _ = solve(dims, perdir, L, z, "halfsweep", nu, omega=1.15, coef16=coef16, slab=0)
+    xb, itb, resb, _ = solve(dims, perdir, L, z, "halfsweep", nu, omega=1.15, coef16=coef16, slab=slab)
+    assert resa <= 1e-8 and ita == itb and resa == resb
+    assert torch.equal(xa, xb)
+
+
+def test_slab_wavefront_skips_periodic_y(cuda):
+    # with y periodic the wavefront would read rows across the wrap before they are final: the setting
+    # is accepted and the half-sweeps run whole-level
+    dims, perdir = (32, 32, 32), (0, 1, 2)
+    L, z = system(dims, perdir)
+    xa, ita, _, _ = solve(dims, perdir, L, z, "halfsweep", omega=1.15, slab=0)
+    xb, itb, _, _ = solve(dims, perdir, L, z, "halfsweep", omega=1.15, slab=8)
+    assert ita == itb and torch.equal(xa, xb)
+
+
+def test_slab_rows_rejects_small_slabs(cuda):
+    h = ia.Handle(ia.make_config((16, 16, 16), poisson="mixed"))
+    assert h.call("ia_poisson_slab_rows", 4) == _lib.IA_ERR_INVALID
+    assert h.call("ia_poisson_slab_rows", -1) == _lib.IA_ERR_INVALID
+    assert h.call("ia_poisson_slab_rows", 0) == _lib.IA_OK
