@@ -367,8 +367,10 @@ __global__ void __launch_bounds__(256, 4) momflux_ff_bulk(FluxCtx F, FluxFF Q, c
                 const ff dd = pos ? u00[i] : um1[i];
                 const ff m = limiter_corr_ff<LIM>(Q, uu, cc, dd);
                 const ff aP = ff_abs(Psi[i]);
-                const ff v = ff_lt(thr, aP) ? ff_mul(Psi[i], cc) : blend(Psi[i], ff_mul(aP, kl), cc, m);
-                stff(Phi + K + i * g.N, v);
+                // above the threshold the face takes Ψ c, which is the blend at l₂ = 1: (1 - 1) m = ±0 and
+                // c ± 0 = c exactly for the normalised stored pair c
+                const ff l2 = ff_lt(thr, aP) ? ff_from(1.0f) : ff_mul(aP, kl);
+                stff(Phi + K + i * g.N, blend(Psi[i], l2, cc, m));
             }
         }
     }

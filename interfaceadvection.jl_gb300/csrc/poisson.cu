@@ -747,7 +747,7 @@ __global__ void setup_fine_k(Grid g, const double* __restrict__ L, double* __res
     iD32[I] = (df * df < 2.0f * eps) ? 0.0f : 1.0f / df;
 }
 
-constexpr int MV_ZT = 4;   // z planes per block of the tiled stencil kernels
+constexpr int MV_ZT = 8;   // z planes per block of the tiled stencil kernels
 inline dim3 mv_tile_grid(const Grid& g) {
     return dim3((g.n[0] - 2 + 31) / 32, (g.n[1] - 2 + 7) / 8, g.D == 3 ? (g.n[2] - 2 + MV_ZT - 1) / MV_ZT : 1);
 }
@@ -878,32 +878,61 @@ __global__ void finalize_k(const double* __restrict__ partial, long long n, int 
         if (threadIdx.x == 0) out[qd] = v;
     }
 }
-// The inner FCG's scalars on the device, in the host's former FP64 operations: β from the partials of
-// s·q and s·r (β = 0 on the first step), then α = (s·r)/(p·q) with the breakdown test; on a breakdown
-// the update is skipped and α, s·r are not carried to the next step.
-__global__ void fcg_beta_k(const double* __restrict__ partial, long long n, FcgDev* S, int first) {
-    const double sq = finalize_sum(partial, n, 0);
-    const double sr = finalize_sum(partial, n, 1);
-    if (threadIdx.x == 0) {
-        const double beta = first ? 0.0 : (-S->alpha_prev * sq) / S->rho_prev;
-        S->sr = sr;
-        S->beta = beta;
-        S->beta32 = float(beta);
+// finalize_sum's value (its 1024 strided partial sums, then its pairwise tree, so the same roundings)
+// computed by a block of 256 threads, four strands each; valid in every thread.  sm: 1024 shared doubles.
+__device__ double sum1024_by256(const double* partial, long long n, int qd, double* sm) {
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        const int v = int(threadIdx.x) + 256 * k;
+        double acc = 0.0;
+        for (long long i = v; i < n; i += 1024) acc += __ldcg(partial + qd * n + i);
+        sm[v] = acc;
     }
-}
-__global__ void fcg_alpha_k(const double* __restrict__ partial, long long n, FcgDev* S) {
-    const double pq = finalize_sum(partial, n, 0);
-    if (threadIdx.x == 0) {
-        const double sr = S->sr;
-        const bool stop = !(pq != 0.0) || !isfinite(pq) || !isfinite(sr) || !isfinite(S->beta);
-        const double alpha = sr / pq;
-        S->alpha32 = float(alpha);
-        S->stop = stop ? 1 : 0;
-        S->rin = 0u;
-        if (!stop) {
-            S->rho_prev = sr;
-            S->alpha_prev = alpha;
+    __syncthreads();
+    for (int w = 512; w > 0; w >>= 1) {
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            const int v = int(threadIdx.x) + 256 * k;
+            if (v < w) sm[v] += sm[v + w];
         }
+        __syncthreads();
+    }
+    const double r = sm[0];
+    __syncthreads();
+    return r;
+}
+// After thread 0 of every block has written the block's partials: true in the last block to finish,
+// which then sees every partial (each block's write is fenced before its count); the counter is reset
+// for the next launch by that block.
+__device__ bool last_block(unsigned int* done, unsigned int nblocks) {
+    __shared__ bool am_last;
+    if (threadIdx.x == 0) {
+        __threadfence();
+        am_last = atomicAdd(done, 1u) == nblocks - 1;
+    }
+    __syncthreads();
+    if (am_last && threadIdx.x == 0) *done = 0u;
+    return am_last;
+}
+// The inner FCG's scalars on the device, in the host's former FP64 operations: β from s·q and s·r (β = 0
+// on the first step), then α = (s·r)/(p·q) with the breakdown test; on a breakdown the update is skipped
+// and α, s·r are not carried to the next step.
+__device__ void fcg_beta(FcgDev* S, double sq, double sr, int first) {
+    const double beta = first ? 0.0 : (-S->alpha_prev * sq) / S->rho_prev;
+    S->sr = sr;
+    S->beta = beta;
+    S->beta32 = float(beta);
+}
+__device__ void fcg_alpha(FcgDev* S, double pq) {
+    const double sr = S->sr;
+    const bool stop = !(pq != 0.0) || !isfinite(pq) || !isfinite(sr) || !isfinite(S->beta);
+    const double alpha = sr / pq;
+    S->alpha32 = float(alpha);
+    S->stop = stop ? 1 : 0;
+    S->rin = 0u;
+    if (!stop) {
+        S->rho_prev = sr;
+        S->alpha_prev = alpha;
     }
 }
 
@@ -939,7 +968,7 @@ __global__ void update_k(Grid g, double alpha, const double* __restrict__ pv, co
 template <int D>
 __global__ void __launch_bounds__(256) matvec32_tile_k(Grid g, const float* __restrict__ L,
                                                        const float* __restrict__ pv, float* __restrict__ q,
-                                                       double* __restrict__ partial) {
+                                                       double* __restrict__ partial, FcgDev* S) {
     const int x = 1 + int(blockIdx.x) * 32 + int(threadIdx.x & 31), y = 1 + int(blockIdx.y) * 8 + int(threadIdx.x >> 5);
     const int z0 = D == 3 ? 1 + MV_ZT * int(blockIdx.z) : 0;
     float acc = 0.f;
@@ -961,11 +990,17 @@ __global__ void __launch_bounds__(256) matvec32_tile_k(Grid g, const float* __re
     __shared__ double ws[8];
     if ((threadIdx.x & 31) == 0) ws[threadIdx.x >> 5] = double(acc);
     __syncthreads();
+    const unsigned int nb = gridDim.x * gridDim.y * gridDim.z;
     if (threadIdx.x == 0) {
         double a = 0.0;
         for (int w = 0; w < 8; ++w) a += ws[w];
         partial[blockIdx.x + gridDim.x * (blockIdx.y + gridDim.y * blockIdx.z)] = a;
     }
+    // the last block: p·q in a fixed order, then α
+    if (!last_block(&S->done_mv, nb)) return;
+    __shared__ double sm[1024];
+    const double pq = sum1024_by256(partial, nb, 0, sm);
+    if (threadIdx.x == 0) fcg_alpha(S, pq);
 }
 
 // Whole-array FP32 vector kernels of the inner solve.  Only interior cells of these vectors are
@@ -973,7 +1008,7 @@ __global__ void __launch_bounds__(256) matvec32_tile_k(Grid g, const float* __re
 // those over the interior; the arrays are streamed as 16-byte vectors (cudaMalloc alignment),
 // the N mod 4 tail by the first threads.
 __global__ void dot2_32_k(long long n, const float* __restrict__ sv, const float* __restrict__ q,
-                          const float* __restrict__ r, double* __restrict__ partial) {
+                          const float* __restrict__ r, double* __restrict__ partial, FcgDev* S, int first) {
     float a1 = 0.f, a2 = 0.f;
     const long long n4 = n / 4, stride = (long long)gridDim.x * blockDim.x;
     const long long t0 = blockIdx.x * (long long)blockDim.x + threadIdx.x;
@@ -996,6 +1031,12 @@ __global__ void dot2_32_k(long long n, const float* __restrict__ sv, const float
         partial[blockIdx.x] = b1;
         partial[gridDim.x + blockIdx.x] = b2;
     }
+    // the last block: s·q and s·r in a fixed order, then β
+    if (!last_block(&S->done_dot, gridDim.x)) return;
+    __shared__ double sm[1024];
+    const double sq = sum1024_by256(partial, gridDim.x, 0, sm);
+    const double sr = sum1024_by256(partial, gridDim.x, 1, sm);
+    if (threadIdx.x == 0) fcg_beta(S, sq, sr, first);
 }
 
 // p = s + β p; β = 0 restarts from s without reading the old direction (which a rejected
@@ -1693,11 +1734,9 @@ static int poisson_solve_mixed(ia_handle* h, double* xv, const double* zz, const
             // β, the direction, q = A p, α and the update without a host round trip; one read-back of
             // the inner residual and the breakdown flag per step
             tk = timing_begin(h, TK_KRYLOV);
-            { dot2_32_k<<<mg->kb, KTHREADS, 0, st>>>(N, sv, mg->q32, rr, mg->partial); ia::note_launch(); }
-            { fcg_beta_k<<<1, 1024, 0, st>>>(mg->partial, mg->kb, S, it == 0 ? 1 : 0); ia::note_launch(); }
+            { dot2_32_k<<<mg->kb, KTHREADS, 0, st>>>(N, sv, mg->q32, rr, mg->partial, S, it == 0 ? 1 : 0); ia::note_launch(); }
             { xpby32_k<<<mg->kb, KTHREADS, 0, st>>>(N, sv, S, mg->p32); ia::note_launch(); }
-            LAUNCH_D(g, matvec32_tile_k, mv_tile_grid(g), KTHREADS, g, F.L32, mg->p32, mg->q32, mg->partial);
-            { fcg_alpha_k<<<1, 1024, 0, st>>>(mg->partial, mg->mvb, S); ia::note_launch(); }
+            LAUNCH_D(g, matvec32_tile_k, mv_tile_grid(g), KTHREADS, g, F.L32, mg->p32, mg->q32, mg->partial, S);
             { update32_k<<<mg->kb, KTHREADS, 0, st>>>(N, S, mg->p32, mg->q32, mg->e32, rr); ia::note_launch(); }
             timing_end(h, tk);
             cudaMemcpyAsync(mg->hsc + 2, &S->rin, 8, cudaMemcpyDeviceToHost, st);

@@ -19,6 +19,7 @@ struct FcgDev {
     float beta32, alpha32;
     unsigned int rin;   // read back together with stop (8 bytes)
     int stop;
+    unsigned int done_dot, done_mv;   // blocks finished in the current reduction kernel (0 between launches)
 };
 
 struct MGLevel {
