@@ -77,6 +77,8 @@ def parse():
     ap.add_argument("--slab-rows", type=int, default=None,
                     help="rows per slab of the finest-level smoothing wavefront (0: whole-level half-sweeps; "
                          "default: the library's, from the L2 size)")
+    ap.add_argument("--fine-nu", default=None,
+                    help="pre,post smoothings of the finest V-cycle level only (default: the library's)")
     return ap.parse_args()
 
 
@@ -361,6 +363,9 @@ def run_bubble(args, world, local_rank):
         ia.set_poisson_coef16(sim.handle, False)
     if args.slab_rows is not None:
         ia.set_poisson_slab_rows(sim.handle, args.slab_rows)
+    if args.fine_nu:
+        n1, n2 = (int(v) for v in args.fine_nu.split(","))
+        _lib.check(sim.handle.call("ia_poisson_mg_fine", C.c_int32(n1), C.c_int32(n2)), "ia_poisson_mg_fine")
     m0 = sim.intf.mass()
     for _ in range(args.warmup):
         ia.sim_step(sim)

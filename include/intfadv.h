@@ -349,6 +349,10 @@ int ia_poisson_mg_relax(ia_handle* h, double omega);
  * stops on the FP64 true residual.  Default 1 when the coefficients 1/ρ (between 1/max(λρ,1) and
  * 1/min(λρ,1)) fit FP16's range, which IA_ERR_UNSUPPORTED reports otherwise. */
 int ia_poisson_coef16(ia_handle* h, int32_t on);
+/* smoothings of the finest level's half-sweep V-cycle (no reference counterpart): nu1 pre- and nu2
+ * post-smoothings on the finest level only, the coarser levels keeping ia_poisson_mg_params' counts;
+ * 0 = the same as the coarser levels (default).  nu1 >= 1 takes effect; 0..16. */
+int ia_poisson_mg_fine(ia_handle* h, int32_t nu1, int32_t nu2);
 /* rows per slab of the finest-level wavefront in the MIXED / LEARNED modes (no reference counterpart):
  * the red-black half-sweeps and the residual restriction of a smoothing run slab by slab over y, each
  * half-sweep one row behind the previous, so that the later half-sweeps read the slab from L2.  Same

@@ -465,8 +465,8 @@ __device__ __noinline__ void viscflux_ff_mixed(const ViscCtx& V, const ViscFF& W
         }
 }
 
-// Bulk pass: cells whose faces and edges no boundary rule reaches and whose viscosities all read one pure
-// phase; every other cell goes to the list (mixed viscosities or boundary rules, viscflux_ff_list)
+// Bulk pass: cells whose faces and edges no wall rule reaches and whose viscosities all read one pure
+// phase; every other cell goes to the list (mixed viscosities, wall rules, ghost cells: viscflux_ff_list)
 template <int D>
 __global__ void __launch_bounds__(256, 5) viscflux_ff_bulk(ViscCtx V, ViscFF W, float2* __restrict__ Phi6,
                                                            unsigned int* __restrict__ list,
@@ -474,23 +474,39 @@ __global__ void __launch_bounds__(256, 5) viscflux_ff_bulk(ViscCtx V, ViscFF W, 
     const Grid& g = V.k.g;
     SPLIT_XYZ
     const long long K = lin(g, x, y, z);
-    bool inner = x >= 3 && x <= g.n[0] - 3 && y >= 3 && y <= g.n[1] - 3;
-    if (D == 3) inner = inner && z >= 3 && z <= g.n[2] - 3;
+    // Cells two or more cells inside a wall dimension, and anywhere in the interior of a periodic one:
+    // there get_mu's fface reads f at the face cell and the cell below it, the face cell remapped by
+    // face_bc only where its periodic coordinate is 0 (to n-2); every other read is either unmapped or a
+    // ghost that holds a bitwise copy of its source.
+    const int cc[3] = {x, y, z};
+    bool inner = true;
+#pragma unroll
+    for (int e = 0; e < D; ++e) {
+        const bool per = g.isper(e);
+        inner = inner && cc[e] >= (per ? 1 : 3) && cc[e] <= g.n[e] - (per ? 2 : 3);
+    }
     bool pure = false;
     unsigned long long b0 = 0ull;
     if (inner) {
-        // the fractions any of the D(D+1)/2 viscosities reads (get_mu_inner: K, K-s_e, K-2s_e, K-s_i-s_j)
-        // (every compare evaluated, no short circuit: the loads issue together instead of one after
-        // another's compare)
+        // the fractions the D(D+1)/2 viscosities read, with P_k the face cell c - δk as face_bc maps it:
+        // face (e, c): K, K - s_e; face (k, c - δk): P_k, P_k - s_k; faces (b, c - δa) and (a, c - δb):
+        // P_a, P_a - s_b, P_b, P_b - s_a (every compare evaluated, no short circuit: the loads issue
+        // together instead of one after another's compare)
         const double* f = V.f;
+        long long P[D];
+#pragma unroll
+        for (int k = 0; k < D; ++k)
+            P[k] = (g.isper(k) && cc[k] == 1) ? K + (long long)(g.n[k] - 3) * g.s[k] : K - g.s[k];
         b0 = dbits(f[K]);
         bool same = true;
 #pragma unroll
-        for (int e = 0; e < D; ++e) same = same & (dbits(f[K - g.s[e]]) == b0) & (dbits(f[K - 2 * g.s[e]]) == b0);
+        for (int e = 0; e < D; ++e)
+            same = same & (dbits(f[K - g.s[e]]) == b0) & (dbits(f[P[e]]) == b0) & (dbits(f[P[e] - g.s[e]]) == b0);
 #pragma unroll
         for (int a = 0; a < D; ++a)
 #pragma unroll
-            for (int b = a + 1; b < D; ++b) same = same & (dbits(f[K - g.s[a] - g.s[b]]) == b0);
+            for (int b = a + 1; b < D; ++b)
+                same = same & (dbits(f[P[a] - g.s[b]]) == b0) & (dbits(f[P[b] - g.s[a]]) == b0);
         pure = same & ((b0 == 0ull) | (b0 == kOneBits));
     }
     if (pure) {

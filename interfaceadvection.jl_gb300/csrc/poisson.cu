@@ -1258,6 +1258,10 @@ static cudaError_t vcycle(ia_handle* h, PoissonMG* mg, int l, cudaStream_t st, i
             return cudaGetLastError();
         }
     }
+    // the finest level may smooth a different number of times than the coarser ones (ia_poisson_mg_fine);
+    // the recursion below passes the coarse counts on
+    const int nu1_here = (l == 0 && mg->nu1f > 0) ? mg->nu1f : nu1;
+    const int nu2_here = (l == 0 && mg->nu2f > 0) ? mg->nu2f : nu2;
     // the finest mixed level's half-sweeps and residual restriction read the FP16 coefficient copy
     const __half* L16 = nullptr;
     if constexpr (sizeof(T) == 4) L16 = (l == 0 && mg->coef16) ? L.L16 : nullptr;
@@ -1298,7 +1302,7 @@ static cudaError_t vcycle(ia_handle* h, PoissonMG* mg, int l, cudaStream_t st, i
     // are then stored, and the post-smoothing's first red half-sweep adds the coarse correction
     // to the value it reads
     const bool relax = mg->omega != 1.0;
-    const int write_red = (nu1 == 1 || relax) ? 1 : 0;
+    const int write_red = (nu1_here == 1 || relax) ? 1 : 0;
     // first black half-sweep: from x = 0 (pre) or from x + P(x_coarse) (post)
     auto first = [&](bool prol, int y0, int y1) {
         const int tk = (l == 0) ? timing_begin(h, TK_MG_FIRST) : -1;
@@ -1363,19 +1367,19 @@ static cudaError_t vcycle(ia_handle* h, PoissonMG* mg, int l, cudaStream_t st, i
         }
     };
     // pre-smoothing: first (black with the red values in place), then (red, black) nu1 - 1 times
-    chain(2 * nu1 - 1, [&](int s, int y0, int y1) {
+    chain(2 * nu1_here - 1, [&](int s, int y0, int y1) {
         if (s == 0) first(false, y0, y1);
         else half((s & 1) ? 0 : 1, y0, y1);
     }, true);
     cudaError_t e = vcycle<T>(h, mg, l + 1, st, nu1, nu2, nuc);
     if (e != cudaSuccess) return e;
-    if (nu2 == 0) {
+    if (nu2_here == 0) {
         { prolong_k<T><<<grd(L.g), blk(), 0, st>>>(L.g, C.g, C.template x_<T>(), x); ia::note_launch(); }
         return cudaGetLastError();
     }
     // post-smoothing: first (black from x + P(x_coarse)), red (adding the correction when relaxed),
     // then (black, red) nu2 - 1 times
-    chain(2 * nu2, [&](int s, int y0, int y1) {
+    chain(2 * nu2_here, [&](int s, int y0, int y1) {
         if (s == 0) first(true, y0, y1);
         else if (s == 1 && relax) half_prol(y0, y1);
         else half((s & 1) ? 0 : 1, y0, y1);
@@ -1391,7 +1395,7 @@ static cudaError_t vcycle_run(ia_handle* h, PoissonMG* mg, cudaStream_t st) {
     int* nu = mg->vgraph_nu[k];
     if (mg->vgraph[k] && (nu[0] != mg->nu1 || nu[1] != mg->nu2 || nu[2] != mg->nuc || nu[3] != mg->smoother ||
                           mg->vgraph_omega[k] != mg->omega || mg->vgraph_c16[k] != mg->coef16 ||
-                          mg->vgraph_slab[k] != mg->slab_rows)) {
+                          mg->vgraph_slab[k] != mg->slab_rows || mg->vgraph_fine[k] != mg->nu1f * 64 + mg->nu2f)) {
         cudaGraphExecDestroy(mg->vgraph[k]);
         mg->vgraph[k] = nullptr;
     }
@@ -1423,6 +1427,7 @@ static cudaError_t vcycle_run(ia_handle* h, PoissonMG* mg, cudaStream_t st) {
         mg->vgraph_omega[k] = mg->omega;
         mg->vgraph_c16[k] = mg->coef16;
         mg->vgraph_slab[k] = mg->slab_rows;
+        mg->vgraph_fine[k] = mg->nu1f * 64 + mg->nu2f;
     }
     note_launches(mg->vgraph_kernels[k]);
     return cudaGraphLaunch(mg->vgraph[k], st);

@@ -67,6 +67,7 @@ struct PoissonMG {
     ia::FcgDev* fcg = nullptr;                                        // the inner FCG's step scalars
     double* hsc = nullptr;                                            // pinned host scalars
     int nu1 = 2, nu2 = 2, nuc = 16;
+    int nu1f = 0, nu2f = 0;                                           // finest-level smoothings (0: nu1, nu2)
     int smoother = 0;                                                 // IA_SMOOTHER_* (FP32 V-cycle)
     double omega = 1.15;                                              // smoother relaxation factor
     int coef16 = 0;                                                   // finest-level smoother on L16 (mixed)
@@ -81,6 +82,7 @@ struct PoissonMG {
     double vgraph_omega[2] = {1.0, 1.0};
     int vgraph_c16[2] = {0, 0};
     int vgraph_slab[2] = {0, 0};
+    int vgraph_fine[2] = {0, 0};                                      // nu1f * 64 + nu2f of the graph
     cudaStream_t capture = nullptr;
 };
 

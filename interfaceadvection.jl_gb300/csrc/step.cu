@@ -385,6 +385,14 @@ int ia_poisson_coef16(ia_handle* h, int32_t on) {
     return IA_OK;
 }
 
+int ia_poisson_mg_fine(ia_handle* h, int32_t nu1, int32_t nu2) {
+    if (!h || nu1 < 0 || nu2 < 0 || nu1 > 16 || nu2 > 16) return IA_ERR_INVALID;
+    if (ensure_scratch(h) != IA_OK) return IA_ERR_CUDA;
+    h->mg->nu1f = nu1;
+    h->mg->nu2f = nu2;
+    return IA_OK;
+}
+
 int ia_poisson_slab_rows(ia_handle* h, int32_t rows) {
     if (!h || rows < 0 || (rows > 0 && rows < 8)) return IA_ERR_INVALID;
     if (ensure_scratch(h) != IA_OK) return IA_ERR_CUDA;

@@ -152,3 +152,22 @@ def test_slab_rows_rejects_small_slabs(cuda):
     assert h.call("ia_poisson_slab_rows", 4) == _lib.IA_ERR_INVALID
     assert h.call("ia_poisson_slab_rows", -1) == _lib.IA_ERR_INVALID
     assert h.call("ia_poisson_slab_rows", 0) == _lib.IA_OK
+
+
+def test_finest_level_smoothing_override(cuda):
+    # ia_poisson_mg_fine: other pre/post counts on the finest level only; the solve still converges to
+    # the same pressure (to the solver tolerance), with its own iteration count
+    dims, perdir = (40, 48, 24), (0, 2)
+    L, z = system(dims, perdir)
+    xa, ita, resa, _ = solve(dims, perdir, L, z, "halfsweep", omega=1.15)
+    h = ia.Handle(ia.make_config(dims, perdir=perdir, poisson="mixed", lrho=1e-3))
+    assert h.call("ia_poisson_mg_fine", -1, 2) == _lib.IA_ERR_INVALID
+    _lib.check(h.call("ia_poisson_mg_fine", 1, 2), "ia_poisson_mg_fine")
+    x = fzeros(z.shape)
+    it, res = C.c_int32(), C.c_double()
+    _lib.check(h.call("ia_poisson_solve", ptr(x), ptr(z), ptr(L), 1e-8, 2000, C.byref(it), C.byref(res)),
+               "ia_poisson_solve")
+    assert resa <= 1e-8 and res.value <= 1e-8
+    xi = lambda v: v[1:-1, 1:-1, 1:-1] - v[1:-1, 1:-1, 1:-1].mean()
+    e = float((xi(xa) - xi(x)).abs().max() / xi(xa).abs().max())
+    assert e < 1e-5, e
