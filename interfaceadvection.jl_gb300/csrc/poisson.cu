@@ -803,17 +803,23 @@ __global__ void __launch_bounds__(256) true_resid_tile_k(Grid g, const double* _
     const int x = 1 + int(blockIdx.x) * 32 + int(threadIdx.x & 31), y = 1 + int(blockIdx.y) * 8 + int(threadIdx.x >> 5);
     const int z0 = D == 3 ? 1 + MV_ZT * int(blockIdx.z) : 0;
     unsigned long long m = 0ull;
+    auto cell = [&](int z) {
+        const int I = x + y * int(g.s[1]) + z * int(g.s[2]);
+        const Nb o = nb_of<D>(g, x, y, z);
+        const double v = resid_cell<D>(g, L, diag[I], zz, xv, I, o);
+        r[I] = v;
+        const unsigned long long b = abs_bits(v);
+        m = b > m ? b : m;
+    };
     if (x <= g.n[0] - 2 && y <= g.n[1] - 2) {
+        if (D == 3 && z0 + MV_ZT - 1 <= g.n[2] - 2) {
 #pragma unroll
-        for (int k = 0; k < (D == 3 ? MV_ZT : 1); ++k) {
-            const int z = z0 + k;
-            if (D == 3 && z > g.n[2] - 2) break;
-            const int I = x + y * int(g.s[1]) + z * int(g.s[2]);
-            const Nb o = nb_of<D>(g, x, y, z);
-            const double v = resid_cell<D>(g, L, diag[I], zz, xv, I, o);
-            r[I] = v;
-            const unsigned long long b = abs_bits(v);
-            m = b > m ? b : m;
+            for (int k = 0; k < MV_ZT; ++k) cell(z0 + k);   // a full tile (see matvec32_tile_k)
+        } else {
+            for (int k = 0; k < (D == 3 ? MV_ZT : 1); ++k) {
+                if (D == 3 && z0 + k > g.n[2] - 2) break;
+                cell(z0 + k);
+            }
         }
     }
     m = block_max(m);
@@ -880,14 +886,21 @@ __global__ void finalize_k(const double* __restrict__ partial, long long n, int 
 }
 // finalize_sum's value (its 1024 strided partial sums, then its pairwise tree, so the same roundings)
 // computed by a block of 256 threads, four strands each; valid in every thread.  sm: 1024 shared doubles.
-__device__ double sum1024_by256(const double* partial, long long n, int qd, double* sm) {
+// Out of line: only the last block of a reduction calls it, and inlined it would raise the streaming
+// loop's register count.
+__device__ __noinline__ double sum1024_by256(const double* partial, long long n, int qd, double* sm) {
+    // the four strands advance together (each still in increasing index order), so that their loads
+    // are in flight at the same time
+    const double* p = partial + qd * n;
+    double acc[4] = {0.0, 0.0, 0.0, 0.0};
+#pragma unroll 2
+    for (long long i0 = threadIdx.x; i0 < n; i0 += 1024) {
 #pragma unroll
-    for (int k = 0; k < 4; ++k) {
-        const int v = int(threadIdx.x) + 256 * k;
-        double acc = 0.0;
-        for (long long i = v; i < n; i += 1024) acc += __ldcg(partial + qd * n + i);
-        sm[v] = acc;
+        for (int k = 0; k < 4; ++k)
+            if (i0 + 256 * k < n) acc[k] += __ldcg(p + i0 + 256 * k);
     }
+#pragma unroll
+    for (int k = 0; k < 4; ++k) sm[int(threadIdx.x) + 256 * k] = acc[k];
     __syncthreads();
     for (int w = 512; w > 0; w >>= 1) {
 #pragma unroll
@@ -972,16 +985,24 @@ __global__ void __launch_bounds__(256) matvec32_tile_k(Grid g, const float* __re
     const int x = 1 + int(blockIdx.x) * 32 + int(threadIdx.x & 31), y = 1 + int(blockIdx.y) * 8 + int(threadIdx.x >> 5);
     const int z0 = D == 3 ? 1 + MV_ZT * int(blockIdx.z) : 0;
     float acc = 0.f;
+    auto cell = [&](int z) {
+        const int I = x + y * int(g.s[1]) + z * int(g.s[2]);
+        const Nb o = nb_of<D>(g, x, y, z);
+        const float v = off7<D>(g, L, pv, I, o) + diag7<D>(g, L, I) * pv[I];
+        q[I] = v;
+        acc += pv[I] * v;
+    };
     if (x <= g.n[0] - 2 && y <= g.n[1] - 2) {
+        if (D == 3 && z0 + MV_ZT - 1 <= g.n[2] - 2) {
+            // a full tile: no bound test between the planes, so that their loads can be issued early
+            // and a plane's values reused as the next plane's z neighbours
 #pragma unroll
-        for (int k = 0; k < (D == 3 ? MV_ZT : 1); ++k) {
-            const int z = z0 + k;
-            if (D == 3 && z > g.n[2] - 2) break;
-            const int I = x + y * int(g.s[1]) + z * int(g.s[2]);
-            const Nb o = nb_of<D>(g, x, y, z);
-            const float v = off7<D>(g, L, pv, I, o) + diag7<D>(g, L, I) * pv[I];
-            q[I] = v;
-            acc += pv[I] * v;
+            for (int k = 0; k < MV_ZT; ++k) cell(z0 + k);
+        } else {
+            for (int k = 0; k < (D == 3 ? MV_ZT : 1); ++k) {
+                if (D == 3 && z0 + k > g.n[2] - 2) break;
+                cell(z0 + k);
+            }
         }
     }
     // the warp's sum in FP32 (a fixed shuffle tree), the block's eight warp sums in FP64 by one thread:
