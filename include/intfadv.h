@@ -349,6 +349,11 @@ int ia_poisson_mg_relax(ia_handle* h, double omega);
  * stops on the FP64 true residual.  Default 1 when the coefficients 1/ρ (between 1/max(λρ,1) and
  * 1/min(λρ,1)) fit FP16's range, which IA_ERR_UNSUPPORTED reports otherwise. */
 int ia_poisson_coef16(ia_handle* h, int32_t on);
+/* 1: the momentum and viscous flux bulk passes use their 64-bit cell-offset variants whatever the grid
+ * size; 0 (default): the 32-bit variants wherever every vector entry index fits 32 bits (fewer
+ * instructions per address), the 64-bit ones beyond.  Same results either way; the switch lets the
+ * 64-bit variants be tested on small grids (no reference counterpart). */
+int ia_wide_offsets(ia_handle* h, int32_t on);
 /* smoothings of the finest level's half-sweep V-cycle (no reference counterpart): nu1 pre- and nu2
  * post-smoothings on the finest level only, the coarser levels keeping ia_poisson_mg_params' counts;
  * 0 = the same as the coarser levels (default).  nu1 >= 1 takes effect; 0..16. */

@@ -44,6 +44,7 @@ struct ia_handle {
     double* dscalar = nullptr;         // device scalars
     int8_t* cbar_own = nullptr;        // c̄ when the caller binds none
     int mom_arith = -1;                // IA_ARITH_* of the momentum kernels (-1: by Poisson mode)
+    int wide_offsets = 0;              // ia_wide_offsets
     Timing timing;
     MomScratch* mom = nullptr;
     PoissonMG* mg = nullptr;

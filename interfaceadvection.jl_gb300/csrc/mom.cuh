@@ -13,6 +13,7 @@ struct MomConsts {
     double uBC[3];
     double gvec[3];
     int has_g;
+    int wide = 0;   // 1: the bulk passes' 64-bit offset variants whatever the grid size
 };
 
 // ρu2u! + BC! → uStar (src/VOFutil.jl:198-201; WaterLily BC!)

@@ -296,7 +296,9 @@ __device__ __forceinline__ void list_append(unsigned int* list, unsigned int* co
 // Bulk pass: faces whose stencil no boundary rule reaches and whose donor cells' old fractions are all
 // one pure phase (for every component) take the short path below; every other cell goes to the list.
 // No out-of-line calls and no local arrays on this path.
-template <int LIM>
+// IDX: the type of the cell offsets, int where every vector entry index (3N) fits 32 bits (fewer
+// instructions per address in this issue-bound pass), long long otherwise
+template <int LIM, class IDX>
 __global__ void __launch_bounds__(256, 4) momflux_ff_bulk(FluxCtx F, FluxFF Q, const float2* __restrict__ us,
                                                           float2* __restrict__ Phi, unsigned int* __restrict__ list,
                                                           unsigned int* __restrict__ count) {
@@ -314,12 +316,13 @@ __global__ void __launch_bounds__(256, 4) momflux_ff_bulk(FluxCtx F, FluxFF Q, c
             if (c[e] < 3 || c[e] > g.n[e] - 3) inner = false;
         }
     }
-    const long long K = lin(g, x, y, z);
+    const IDX K = IDX(x) + IDX(y) * IDX(g.s[1]) + IDX(z) * IDX(g.s[2]);
+    const IDX N = IDX(g.N);
     bool defer = in_range && !inner;
     if (in_range && inner) {
         // every load first, for both signs of Ψ (the donor row K - δj or K, the upwind stencil
         // K - 2δj .. K or K + δj .. K - δj), so that no load waits for the FP64 Ψ or the pure-phase test
-        const long long sj = g.s[j];
+        const IDX sj = IDX(g.s[j]);
         const double rK = F.rj[K];
         const unsigned long long oK = dbits(F.fold[K]), oKj = dbits(F.fold[K - sj]);
         double rI[3];
@@ -328,11 +331,11 @@ __global__ void __launch_bounds__(256, 4) momflux_ff_bulk(FluxCtx F, FluxFF Q, c
 #pragma unroll
         for (int i = 0; i < 3; ++i) {
             if (i >= g.D) break;
-            const long long si = g.s[i];
+            const IDX si = IDX(g.s[i]);
             rI[i] = F.rj[K - si];
             oKi[i] = dbits(F.fold[K - si]);
             oKji[i] = dbits(F.fold[K - sj - si]);
-            const float2* u = us + i * g.N;
+            const float2* u = us + IDX(i) * N;
             um2[i] = ldff(u + K - 2 * sj);
             um1[i] = ldff(u + K - sj);
             u00[i] = ldff(u + K);
@@ -370,7 +373,7 @@ __global__ void __launch_bounds__(256, 4) momflux_ff_bulk(FluxCtx F, FluxFF Q, c
                 // above the threshold the face takes Ψ c, which is the blend at l₂ = 1: (1 - 1) m = ±0 and
                 // c ± 0 = c exactly for the normalised stored pair c
                 const ff l2 = ff_lt(thr, aP) ? ff_from(1.0f) : ff_mul(aP, kl);
-                stff(Phi + K + i * g.N, blend(Psi[i], l2, cc, m));
+                stff(Phi + (K + IDX(i) * N), blend(Psi[i], l2, cc, m));
             }
         }
     }
@@ -467,13 +470,15 @@ __device__ __noinline__ void viscflux_ff_mixed(const ViscCtx& V, const ViscFF& W
 
 // Bulk pass: cells whose faces and edges no wall rule reaches and whose viscosities all read one pure
 // phase; every other cell goes to the list (mixed viscosities, wall rules, ghost cells: viscflux_ff_list)
-template <int D>
-__global__ void __launch_bounds__(256, 5) viscflux_ff_bulk(ViscCtx V, ViscFF W, float2* __restrict__ Phi6,
+// IDX: int where every vector entry index (6N for the fluxes) fits 32 bits, long long otherwise
+template <int D, class IDX>
+__global__ void __launch_bounds__(256, sizeof(IDX) == 4 ? 5 : 4) viscflux_ff_bulk(ViscCtx V, ViscFF W, float2* __restrict__ Phi6,
                                                            unsigned int* __restrict__ list,
                                                            unsigned int* __restrict__ count) {
     const Grid& g = V.k.g;
     SPLIT_XYZ
-    const long long K = lin(g, x, y, z);
+    const IDX K = IDX(x) + IDX(y) * IDX(g.s[1]) + IDX(z) * IDX(g.s[2]);
+    const IDX N = IDX(g.N);
     // Cells two or more cells inside a wall dimension, and anywhere in the interior of a periodic one:
     // there get_mu's fface reads f at the face cell and the cell below it, the face cell remapped by
     // face_bc only where its periodic coordinate is 0 (to n-2); every other read is either unmapped or a
@@ -493,35 +498,35 @@ __global__ void __launch_bounds__(256, 5) viscflux_ff_bulk(ViscCtx V, ViscFF W, 
         // P_a, P_a - s_b, P_b, P_b - s_a (every compare evaluated, no short circuit: the loads issue
         // together instead of one after another's compare)
         const double* f = V.f;
-        long long P[D];
+        IDX P[D];
 #pragma unroll
         for (int k = 0; k < D; ++k)
-            P[k] = (g.isper(k) && cc[k] == 1) ? K + (long long)(g.n[k] - 3) * g.s[k] : K - g.s[k];
+            P[k] = (g.isper(k) && cc[k] == 1) ? K + IDX(g.n[k] - 3) * IDX(g.s[k]) : K - IDX(g.s[k]);
         b0 = dbits(f[K]);
         bool same = true;
 #pragma unroll
         for (int e = 0; e < D; ++e)
-            same = same & (dbits(f[K - g.s[e]]) == b0) & (dbits(f[P[e]]) == b0) & (dbits(f[P[e] - g.s[e]]) == b0);
+            same = same & (dbits(f[K - IDX(g.s[e])]) == b0) & (dbits(f[P[e]]) == b0) & (dbits(f[P[e] - IDX(g.s[e])]) == b0);
 #pragma unroll
         for (int a = 0; a < D; ++a)
 #pragma unroll
             for (int b = a + 1; b < D; ++b)
-                same = same & (dbits(f[P[a] - g.s[b]]) == b0) & (dbits(f[P[b] - g.s[a]]) == b0);
+                same = same & (dbits(f[P[a] - IDX(g.s[b])]) == b0) & (dbits(f[P[b] - IDX(g.s[a])]) == b0);
         pure = same & ((b0 == 0ull) | (b0 == kOneBits));
     }
     if (pure) {
         const ff mu = b0 == 0ull ? W.mu_face0 : W.mu_face1;
         ff uK[D];
 #pragma unroll
-        for (int i = 0; i < D; ++i) uK[i] = ff_split(V.u[K + i * g.N]);
+        for (int i = 0; i < D; ++i) uK[i] = ff_split(V.u[K + IDX(i) * N]);
 #pragma unroll
         for (int i = 0; i < D; ++i)
 #pragma unroll
             for (int j = i; j < D; ++j) {
                 // ∂ⱼuᵢ + ∂ᵢuⱼ; on the diagonal the two are the same difference
-                const ff sji = ff_sub(uK[i], ff_split(V.u[K - g.s[j] + i * g.N]));
-                const ff s2 = (i == j) ? ff_scale2(sji, 2.0f) : ff_add(sji, ff_sub(uK[j], ff_split(V.u[K - g.s[i] + j * g.N])));
-                stff(Phi6 + pair_index(D, i, j) * g.N + K, -ff_mul(mu, s2));
+                const ff sji = ff_sub(uK[i], ff_split(V.u[K - IDX(g.s[j]) + IDX(i) * N]));
+                const ff s2 = (i == j) ? ff_scale2(sji, 2.0f) : ff_add(sji, ff_sub(uK[j], ff_split(V.u[K - IDX(g.s[i]) + IDX(j) * N])));
+                stff(Phi6 + IDX(pair_index(D, i, j)) * N + K, -ff_mul(mu, s2));
             }
     }
     list_append(list, count, !pure, (unsigned int)K);
@@ -746,9 +751,11 @@ cudaError_t k_momflux_ff(const MomConsts& k, int j, int limiter, const float2* u
     Q.sixth = ff_split(1.0 / 6.0);
     const dim3 gr = split_grid(k.g);
     if (cudaMemsetAsync(count, 0, sizeof(unsigned int), s) != cudaSuccess) return cudaGetLastError();
+    const bool narrow = !k.wide && 3LL * k.g.N < (1LL << 31);
 #define MF_FF(L_)                                                                                         \
     {                                                                                                     \
-        momflux_ff_bulk<L_><<<gr, blk(), 0, s>>>(F, Q, ustar, Phi, list, count);                         \
+        if (narrow) momflux_ff_bulk<L_, int><<<gr, blk(), 0, s>>>(F, Q, ustar, Phi, list, count);         \
+        else momflux_ff_bulk<L_, long long><<<gr, blk(), 0, s>>>(F, Q, ustar, Phi, list, count);          \
         momflux_ff_list<L_><<<list_blocks, 128, 0, s>>>(F, Q, ustar, Phi, list, count);                  \
         ia::note_launches(2);                                                                             \
     }
@@ -797,13 +804,16 @@ cudaError_t k_visc_ff(const MomConsts& k, const double* u, const double* f, doub
     std::memcpy(&W.mu1bits, &V.mu_face1, 8);
     W.mu_face0 = ff_split(V.mu_face0);
     W.mu_face1 = ff_split(V.mu_face1);
+    const bool narrow = !k.wide && 6LL * k.g.N < (1LL << 31);   // the six flux components' entries in 32 bits
     if (cudaMemsetAsync(count, 0, sizeof(unsigned int), s) != cudaSuccess) return cudaGetLastError();
     if (k.g.D == 3) {
-        { viscflux_ff_bulk<3><<<split_grid(k.g), blk(), 0, s>>>(V, W, Phi6, list, count); ia::note_launch(); }
+        if (narrow) { viscflux_ff_bulk<3, int><<<split_grid(k.g), blk(), 0, s>>>(V, W, Phi6, list, count); ia::note_launch(); }
+        else { viscflux_ff_bulk<3, long long><<<split_grid(k.g), blk(), 0, s>>>(V, W, Phi6, list, count); ia::note_launch(); }
         { viscflux_ff_list<3><<<list_blocks, 128, 0, s>>>(V, W, Phi6, list, count); ia::note_launch(); }
         { viscacc_ff_kern<3><<<igrd(k.g), blk(), 0, s>>>(k.g, Phi6, r); ia::note_launch(); }
     } else {
-        { viscflux_ff_bulk<2><<<split_grid(k.g), blk(), 0, s>>>(V, W, Phi6, list, count); ia::note_launch(); }
+        if (narrow) { viscflux_ff_bulk<2, int><<<split_grid(k.g), blk(), 0, s>>>(V, W, Phi6, list, count); ia::note_launch(); }
+        else { viscflux_ff_bulk<2, long long><<<split_grid(k.g), blk(), 0, s>>>(V, W, Phi6, list, count); ia::note_launch(); }
         { viscflux_ff_list<2><<<list_blocks, 128, 0, s>>>(V, W, Phi6, list, count); ia::note_launch(); }
         { viscacc_ff_kern<2><<<igrd(k.g), blk(), 0, s>>>(k.g, Phi6, r); ia::note_launch(); }
     }

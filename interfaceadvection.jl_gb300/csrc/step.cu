@@ -41,6 +41,7 @@ static MomConsts consts(ia_handle* h) {
         k.gvec[d] = h->cfg.g[d];
     }
     k.has_g = h->cfg.has_g;
+    k.wide = h->wide_offsets;
     return k;
 }
 
@@ -382,6 +383,12 @@ int ia_poisson_coef16(ia_handle* h, int32_t on) {
     if (on && !coef16_fits(h->cfg.lrho)) return IA_ERR_UNSUPPORTED;
     if (ensure_scratch(h) != IA_OK) return IA_ERR_CUDA;
     h->mg->coef16 = on;
+    return IA_OK;
+}
+
+int ia_wide_offsets(ia_handle* h, int32_t on) {
+    if (!h || (on != 0 && on != 1)) return IA_ERR_INVALID;
+    h->wide_offsets = on;
     return IA_OK;
 }
 

@@ -85,6 +85,7 @@ _SIGS = {
     "ia_poisson_coef16": (C.c_int, [C.c_void_p, C.c_int32]),
     "ia_poisson_slab_rows": (C.c_int, [C.c_void_p, C.c_int32]),
     "ia_poisson_mg_fine": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32]),
+    "ia_wide_offsets": (C.c_int, [C.c_void_p, C.c_int32]),
     "ia_probe_fma_rates": (C.c_int, [C.POINTER(C.c_double), C.POINTER(C.c_double)]),
     "ia_advect_vof_noalloc": (C.c_int, [C.POINTER(Config), C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                         C.c_double, C.c_int64, C.c_void_p, C.c_void_p, C.POINTER(Status)]),

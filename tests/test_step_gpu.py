@@ -153,6 +153,19 @@ def test_mixed_poisson_agrees_with_fp64(cuda):
     assert b.last_status.poisson_iters[1] >= a.last_status.poisson_iters[1] - 1
 
 
+def test_wide_offset_variants_give_the_same_steps(cuda):
+    # the momentum and viscous flux bulk passes run with 32-bit cell offsets on grids this size; their
+    # 64-bit variants (grids past 2^31 vector entries) forced with ia_wide_offsets give the same steps
+    a, _ = bubble_pair(poisson="mixed")
+    b, _ = bubble_pair(poisson="mixed")
+    assert b.handle.call("ia_wide_offsets", 2) == _lib.IA_ERR_INVALID
+    _lib.check(b.handle.call("ia_wide_offsets", 1), "ia_wide_offsets")
+    for _ in range(3):
+        ia.sim_step(a)
+        ia.sim_step(b)
+    assert torch.equal(a.flow.u, b.flow.u) and torch.equal(a.intf.f, b.intf.f) and torch.equal(a.flow.p, b.flow.p)
+
+
 def test_mpcfl_matches_oracle(cuda):
     sim, orc = bubble_pair()
     ia.sim_step(sim)
