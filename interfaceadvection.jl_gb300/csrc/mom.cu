@@ -579,11 +579,23 @@ __global__ void div_scale_kern(Grid g, const double* __restrict__ u, double* __r
     zz[I] = s;
 }
 
+// u -= L ∂x on interior cells (the dimension fixed at compile time: every load issued first, no
+// dynamically indexed grid strides)
+template <int D>
 __global__ void correct_kern(Grid g, double* __restrict__ u, const double* __restrict__ L,
                              const double* __restrict__ xx) {
     ICELL_XYZ
     const long long I = lin(g, x, y, z);
-    for (int i = 0; i < g.D; ++i) u[I + i * g.N] -= L[I + i * g.N] * (xx[I] - xx[I - g.s[i]]);
+    const double xI = xx[I];
+    double uu[D], ll[D], xm[D];
+#pragma unroll
+    for (int i = 0; i < D; ++i) {
+        uu[i] = u[I + i * g.N];
+        ll[i] = L[I + i * g.N];
+        xm[i] = xx[I - g.s[i]];
+    }
+#pragma unroll
+    for (int i = 0; i < D; ++i) u[I + i * g.N] = uu[i] - ll[i] * (xI - xm[i]);
 }
 
 __global__ void scale_kern(double* a, long long n, double s) {
@@ -769,7 +781,8 @@ cudaError_t k_div_scale(const MomConsts& k, const double* u, double* zz, double*
     return cudaGetLastError();
 }
 cudaError_t k_correct(const MomConsts& k, double* u, const double* L, double* xx, double dt, cudaStream_t s) {
-    { correct_kern<<<igrd(k.g), blk(), 0, s>>>(k.g, u, L, xx); ia::note_launch(); }
+    if (k.g.D == 3) { correct_kern<3><<<igrd(k.g), blk(), 0, s>>>(k.g, u, L, xx); ia::note_launch(); }
+    else { correct_kern<2><<<igrd(k.g), blk(), 0, s>>>(k.g, u, L, xx); ia::note_launch(); }
     { scale_kern<<<1216, 256, 0, s>>>(xx, k.g.N, 1.0 / dt); ia::note_launch(); }
     return cudaGetLastError();
 }
