@@ -151,15 +151,9 @@ __device__ __forceinline__ ff limiter_corr_ff(const FluxFF& Q, ff u, ff c, ff d)
         }
         return ff_signed(s, r);
     }
-    // Koren: median((7c + d - 2u)/6, c, median(2c - u, c, d)) = c + median((2δ₁ + δ₂)/6, 0, median(δ₁, 0, δ₂)).
-    // For δ₁, δ₂ of one sign, τ = (2δ₁ + δ₂)/6 has that sign as well, so the two medians pick the one of
-    // τ, δ₁, δ₂ of smallest magnitude; otherwise the inner median is 0 and so is the correction.
+    // Koren: median((7c + d - 2u)/6, c, median(2c - u, c, d)) = c + median((2δ₁ + δ₂)/6, 0, median(δ₁, 0, δ₂))
     const ff tau = ff_mul(ff_add(ff_scale2(d1, 2.0f), d2), Q.sixth);
-    const bool same = (d1.hi > 0.0f && d2.hi > 0.0f) || (d1.hi < 0.0f && d2.hi < 0.0f);
-    const ff a1 = ff_abs(d1), a2 = ff_abs(d2), at = ff_abs(tau);
-    const bool second = ff_lt(a2, a1);
-    const ff r = second ? d2 : d1, ar = second ? a2 : a1;
-    return same ? (ff_lt(at, ar) ? tau : r) : ff_from(0.0f);
+    return ff_minmod(tau, ff_minmod(d1, d2));
 }
 
 // SynDRoM blend Ψ (v_d + l₂ (v_I - v_d)) = Ψ (c + (1 - l₂) m) once l₂ is known (src/flow.jl:37-57)
