@@ -115,9 +115,9 @@ __device__ __forceinline__ bool face_simple(const SweepArgs& a, long long K, int
 // is δl for a full donor and δl λρ for an empty one (two FP64 operations;
 // the products are re-associated, a relative change below 1e-15).  Returns
 // false when the donor needs reconstruction.
-__device__ __forceinline__ bool face_mass_simple(const SweepArgs& a, long long K, int kd, double& m) {
+__device__ __forceinline__ bool face_mass_simple(const SweepArgs& a, long long K, int kd, double s, double& m) {
+    // s = u1[K] + u2[K]
     const long long sd = a.g.s[a.d];
-    const double s = a.u1[K] + a.u2[K];
     const unsigned long long sb = bits(s);
     if ((sb & ABS_MASK) == 0ull) {   // δl == 0: ρuf stays 0
         m = 0.0;
@@ -138,6 +138,10 @@ __device__ __forceinline__ bool face_mass_simple(const SweepArgs& a, long long K
     }
     return false;
 }
+
+// u1[K] + u2[K] for the rare faces whose sum the caller has not formed (out of line: a call is not
+// if-converted into the common path)
+__device__ __noinline__ double face_sum_cold(const double* u1, const double* u2, long long K) { return u1[K] + u2[K]; }
 
 template <int D>
 __device__ __forceinline__ void coords_of(const Grid& g, long long O, int c[3]) {
@@ -168,7 +172,7 @@ __device__ __forceinline__ void warp_append(unsigned int* list, unsigned int* co
     if (pred) list[base + __popc(mask & ((1u << lane) - 1u))] = val;
 }
 
-template <int D, bool FIRST>
+template <int D, bool FIRST, bool DILA>
 __global__ void __launch_bounds__(256) vof_bulk(SweepArgs a) {
     // x in [1, n-2] one cell per lane, so that a row of 32k interior cells fills k warps; the
     // last block column's first warp takes the ghost cells x = 0 and n-1 of the block's 8 rows.
@@ -202,15 +206,18 @@ __global__ void __launch_bounds__(256) vof_bulk(SweepArgs a) {
                           abs_le(bits(a.u1[S]), a.ulim) && abs_le(bits(a.u1[S + sd]), a.ulim) &&
                           abs_le(bits(a.u2[S]), a.ulim) && abs_le(bits(a.u2[S + sd]), a.ulim);
         need_cell = !bulk;
-        if (a.dila) {
+        double sS = 0.0;   // u1[S] + u2[S]: the dilation difference's and an interior face's mass flux sum
+        if (DILA) {
             // the momentum update's dilation term of this (ghost-mapped) cell, on FP32 pairs: c̄ of the
             // source cell (in the first sweep from its fraction, as the c̄ pass above computes it)
             int cs;
             if (FIRST) cs = (((bc & ABS_MASK) <= 0x7FF0000000000000ull) && ((bc >> 63) || bc < 0x3FE0000000000000ull)) ? 0 : 1;
             else cs = cb;
-            // the velocity differences in FP64, as the reference forms them (three FP64 additions on a
-            // pipe this kernel leaves mostly idle), then one split and a pair product
-            const double du = (a.u1[S + sd] - a.u1[S]) + (a.u2[S + sd] - a.u2[S]);
+            // the velocity difference in FP64 as (u1 + u2)(S + δd) − (u1 + u2)(S): the second sum is the face
+            // mass flux's for an interior cell, so the cell issues two FP64 additions for both instead of
+            // four (this pass is bound by its FP64 work), then one split and a pair product
+            sS = a.u1[S] + a.u2[S];
+            const double du = (a.u1[S + sd] + a.u2[S + sd]) - sS;
             const ff rq = cs ? ff{a.rq_1_hi, a.rq_1_lo} : ff{a.rq_l_hi, a.rq_l_lo};
             const ff dq = ff_mul(rq, ff_split(du));
             a.dila[O] = make_float2(dq.hi, dq.lo);
@@ -221,7 +228,8 @@ __global__ void __launch_bounds__(256) vof_bulk(SweepArgs a) {
             a.fout[O] = (bc == ONE_BITS) ? 1.0 : 0.0;
         if (in_face_range<D>(g, a.d, c)) {
             double m;
-            if (face_mass_simple(a, O, c[a.d], m)) {
+            const double sO = DILA ? (O == S ? sS : face_sum_cold(a.u1, a.u2, O)) : a.u1[O] + a.u2[O];
+            if (face_mass_simple(a, O, c[a.d], sO, m)) {
                 if (a.rhouf_d) a.rhouf_d[O] = m;
             } else {
                 need_face = true;
@@ -300,7 +308,8 @@ template <int D, bool FIRST>
 void launch_bulk(const SweepArgs& a, cudaStream_t st) {
     dim3 blk(32, 8, 1);
     dim3 grd((a.g.n[0] - 2 + 31) / 32 + 1, (a.g.n[1] + 7) / 8, a.g.n[2]);
-    { vof_bulk<D, FIRST><<<grd, blk, 0, st>>>(a); ia::note_launch(); }
+    if (a.dila) { vof_bulk<D, FIRST, true><<<grd, blk, 0, st>>>(a); ia::note_launch(); }
+    else { vof_bulk<D, FIRST, false><<<grd, blk, 0, st>>>(a); ia::note_launch(); }
 }
 
 }  // namespace
