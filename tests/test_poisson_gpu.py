@@ -137,6 +137,18 @@ def test_slab_wavefront_is_bit_identical(cuda, nu, slab, coef16):
     assert torch.equal(xa, xb)
 
 
+@pytest.mark.parametrize("nu", [(2, 2), (1, 2)])
+def test_slab_wavefront_is_bit_identical_unrelaxed(cuda, nu):
+    # relaxation factor 1: the post-smoothing's first red half-sweep is a plain one and the first
+    # half-sweep writes the red values only for nu1 = 1
+    dims, perdir = (40, 46, 24), (0, 2)
+    L, z = system(dims, perdir)
+    xa, ita, resa, _ = solve(dims, perdir, L, z, "halfsweep", nu, omega=1.0, coef16=True, slab=0)
+    xb, itb, resb, _ = solve(dims, perdir, L, z, "halfsweep", nu, omega=1.0, coef16=True, slab=8)
+    assert resa <= 1e-8 and ita == itb and resa == resb
+    assert torch.equal(xa, xb)
+
+
 def test_slab_wavefront_skips_periodic_y(cuda):
     # with y periodic the wavefront would read rows across the wrap before they are final: the setting
     # is accepted and the half-sweeps run whole-level
