@@ -392,6 +392,7 @@ __device__ __forceinline__ double fbuffer_at(const Grid& g, const double* __rest
 
 // fbuffer along every d in one pass over f, and per d the list of interior cells where it is mixed
 // (the only cells surften_kern changes), appended one warp at a time
+template <int D>
 __global__ void fbuffer_kern(MomConsts k, const double* __restrict__ f, const double* __restrict__ prev0,
                              double* __restrict__ fb, int* __restrict__ list, unsigned int* __restrict__ count) {
     const Grid& g = k.g;
@@ -401,12 +402,19 @@ __global__ void fbuffer_kern(MomConsts k, const double* __restrict__ f, const do
     const long long I = lin(g, x, y, z);
     const int lane = int(threadIdx.x) & 31;
     // interior cells: no ghost or never-written position, the face fractions of this cell directly
+    // (the dimension fixed at compile time, so that the D + 1 loads issue before the first list append)
     const bool deep = inner && x <= g.n[0] - 2 && y <= g.n[1] - 2;
-    for (int d = 0; d < g.D; ++d) {
+    double fI = 0.0, fm[D];
+    if (deep) {
+        fI = f[I];
+#pragma unroll
+        for (int d = 0; d < D; ++d) fm[d] = f[I - g.s[d]];
+    }
+#pragma unroll
+    for (int d = 0; d < D; ++d) {
         double v;
         if (deep) {
-            const double fa = f[I], fm = f[I - g.s[d]];
-            v = (dbits(fa) == dbits(fm)) ? fa : face_avg(fa, fm);
+            v = (dbits(fI) == dbits(fm[d])) ? fI : face_avg(fI, fm[d]);
         } else {
             v = fbuffer_at(g, f, d, c0, prev0);
         }
@@ -755,7 +763,8 @@ cudaError_t k_surften(const MomConsts& k, const double* f, const double* prev0, 
                       int* list, unsigned int* count, cudaStream_t s) {
     const Grid& g = k.g;
     cudaMemsetAsync(count, 0, sizeof(unsigned int) * g.D, s);
-    { fbuffer_kern<<<ggrd(g), blk(), 0, s>>>(k, f, prev0, fb, list, count); ia::note_launch(); }
+    if (k.g.D == 3) { fbuffer_kern<3><<<ggrd(g), blk(), 0, s>>>(k, f, prev0, fb, list, count); ia::note_launch(); }
+    else { fbuffer_kern<2><<<ggrd(g), blk(), 0, s>>>(k, f, prev0, fb, list, count); ia::note_launch(); }
     for (int d = 0; d < g.D; ++d) {
         double* fbd = fb + d * g.N;
         const int* ld = list + d * g.N;
