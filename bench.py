@@ -396,7 +396,7 @@ def run_bubble(args, world, local_rank):
         hu = pinned(fl.u).copy_(fl.u)
         hf = pinned(it.f).copy_(it.f)
         hp = pinned(fl.p)
-        e_steps = max(2, min(args.steps, 4))
+        e_steps = args.steps
         torch.cuda.synchronize()
         barrier()
         t0 = time.perf_counter()
@@ -421,19 +421,23 @@ def run_bubble(args, world, local_rank):
         nb = fl.u.numel() * 8 + it.f.numel() * 8
         e2e = {"value": world * cells * e_steps / el / 1e6, "unit": METRIC, "h2d_bytes_per_step": nb,
                "d2h_bytes_per_step": nb + fl.p.numel() * 8 + C.sizeof(_lib.Status),
+               "steps": e_steps,
                "note": "state on the host: u, f uploaded and u, f, p downloaded every step around sim_step"}
     out["e2e"] = e2e
     del sim
     torch.cuda.empty_cache()
     if args.no_secondary or args.quick:
         return out
-    k = max(2, min(args.steps, 5))
+    # the comparison runs over the same window of the same run as the headline: the same warm-up steps
+    # from the same initial state, then the same number of timed steps
+    k = args.steps
     for key, arith in (("fp64_mg", "fp64"), ("fp64_mg_ff", "ff")):
         ref = make_bubble(N, "fp64", dev, arith)
-        for _ in range(max(1, args.warmup - 1)):
+        for _ in range(args.warmup):
             ia.sim_step(ref)
         ms2, its2, res2, _ = timed_steps(ref, k, barrier, False, local_rank)
-        out[key] = {"value": world * cells * k / (ms2 / 1e3) / 1e6, "ms_per_step": ms2 / k,
+        out[key] = {"value": world * cells * k / (ms2 / 1e3) / 1e6, "ms_per_step": ms2 / k, "steps": k,
+                    "warmup": args.warmup,
                     "poisson_iters_per_step": statistics.mean(its2), "max_resid": max(res2),
                     "momentum_arith": arith, "mg_vcycle_ms_per_step": kernel_times(ref, 2)["mg_vcycle"]["ms_per_step"]}
         del ref
@@ -443,14 +447,15 @@ def run_bubble(args, world, local_rank):
     if os.path.exists(learned.WEIGHTS):
         # learned preconditioner: the same step with the inner FCG preconditioned by V-cycle + net
         lrn = make_bubble(N, "learned", dev)
-        for _ in range(max(1, args.warmup - 1)):
+        for _ in range(args.warmup):
             ia.sim_step(lrn)
         st0 = ia.poisson_stats(lrn.handle)
         ms3, its3, res3, _ = timed_steps(lrn, k, barrier, False, local_rank)
         st1 = ia.poisson_stats(lrn.handle)
         kt3 = kernel_times(lrn, 2)
         out["learned_hybrid"] = {
-            "value": world * cells * k / (ms3 / 1e3) / 1e6, "ms_per_step": ms3 / k,
+            "value": world * cells * k / (ms3 / 1e3) / 1e6, "ms_per_step": ms3 / k, "steps": k,
+            "warmup": args.warmup,
             "poisson_iters_per_step": statistics.mean(its3), "max_resid": max(res3),
             "fallbacks": st1["fallbacks"] - st0["fallbacks"],
             "net_ms_per_step": kt3["nn_precond"]["ms_per_step"],
