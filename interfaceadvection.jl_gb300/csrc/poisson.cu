@@ -1755,6 +1755,9 @@ static int poisson_solve_mixed(ia_handle* h, double* xv, const double* zz, const
         timing_end(h, tk);
         const double target = std::fmax(0.5 * tol / res, mg->inner_rtol) * res;
         FcgDev* S = mg->fcg;
+        // the reductions' last-block counters start from zero in every inner solve (each launch leaves
+        // them at zero, but not one that an error cut short)
+        cudaMemsetAsync(&S->done_dot, 0, 2 * sizeof(unsigned int), st);
         for (int it = 0; it < mg->inner_max && total < itmx; ++it) {
             float* sv = nullptr;
             if (!precond(sv)) return IA_ERR_CUDA;
