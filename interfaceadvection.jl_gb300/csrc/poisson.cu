@@ -794,12 +794,16 @@ __global__ void true_resid_k(Grid g, const double* __restrict__ L, const double*
 // The same on the x-y tiles of matvec32_tile_k (32 x 8 cells, MV_ZT z planes per block of 256 threads) with
 // the precomputed diagonal; each block's L∞ (as the bit pattern of |r|) into pmax[block], reduced by
 // finalize_max_k.
+// With r32 given, also the next inner solve's start: r32 = float(r) (integer rounding, no FP64-pipe
+// conversion in this FP64-bound kernel) and e32 = 0 on the same interior cells (their ghost entries stay
+// zero from the allocation: the whole-array vector updates only ever add zero there).
 template <int D>
 __global__ void __launch_bounds__(256) true_resid_tile_k(Grid g, const double* __restrict__ L,
                                                          const double* __restrict__ diag,
                                                          const double* __restrict__ zz,
                                                          const double* __restrict__ xv, double* __restrict__ r,
-                                                         unsigned long long* __restrict__ pmax) {
+                                                         unsigned long long* __restrict__ pmax,
+                                                         float* __restrict__ r32, float* __restrict__ e32) {
     const int x = 1 + int(blockIdx.x) * 32 + int(threadIdx.x & 31), y = 1 + int(blockIdx.y) * 8 + int(threadIdx.x >> 5);
     const int z0 = D == 3 ? 1 + MV_ZT * int(blockIdx.z) : 0;
     unsigned long long m = 0ull;
@@ -808,6 +812,10 @@ __global__ void __launch_bounds__(256) true_resid_tile_k(Grid g, const double* _
         const Nb o = nb_of<D>(g, x, y, z);
         const double v = resid_cell<D>(g, L, diag[I], zz, xv, I, o);
         r[I] = v;
+        if (r32) {
+            r32[I] = f32_rn(v);
+            e32[I] = 0.f;
+        }
         const unsigned long long b = abs_bits(v);
         m = b > m ? b : m;
     };
@@ -1665,9 +1673,9 @@ static cudaError_t mg_precondition(ia_handle* h) {
 // r = z - A x with the FP64 operator and the precomputed diagonal; L∞(r), as the bit pattern of |r|,
 // into *dlinf
 static void true_residual(PoissonMG* mg, const Grid& g, const double* L, const double* zz, const double* xv,
-                          unsigned long long* dlinf, cudaStream_t st) {
+                          unsigned long long* dlinf, cudaStream_t st, float* r32 = nullptr, float* e32 = nullptr) {
     unsigned long long* pmax = reinterpret_cast<unsigned long long*>(mg->partial);
-    LAUNCH_D(g, true_resid_tile_k, mv_tile_grid(g), KTHREADS, g, L, mg->diag64, zz, xv, mg->r, pmax);
+    LAUNCH_D(g, true_resid_tile_k, mv_tile_grid(g), KTHREADS, g, L, mg->diag64, zz, xv, mg->r, pmax, r32, e32);
     { finalize_max_k<<<1, 1024, 0, st>>>(pmax, mg->mvb, dlinf); ia::note_launch(); }
 }
 
@@ -1745,14 +1753,11 @@ static int poisson_solve_mixed(ia_handle* h, double* xv, const double* zz, const
     };
     int total = 0;
     int tk = timing_begin(h, TK_KRYLOV);
-    true_residual(mg, g, L, zz, xv, dlinf, st);
+    // every FP64 residual also starts the next inner solve: rr = float(r), e32 = 0
+    true_residual(mg, g, L, zz, xv, dlinf, st, rr, mg->e32);
     timing_end(h, tk);
     double res = read_linf(h, dlinf);
     while (!(res <= tol) && total < itmx) {
-        tk = timing_begin(h, TK_MG_TRANSFER);
-        { to_f32_k<<<1216, 256, 0, st>>>(N, mg->r, rr); ia::note_launch(); }
-        { zero_k<float><<<1216, 256, 0, st>>>(N, mg->e32); ia::note_launch(); }
-        timing_end(h, tk);
         const double target = std::fmax(0.5 * tol / res, mg->inner_rtol) * res;
         FcgDev* S = mg->fcg;
         // the reductions' last-block counters start from zero in every inner solve (each launch leaves
@@ -1784,7 +1789,7 @@ static int poisson_solve_mixed(ia_handle* h, double* xv, const double* zz, const
         }
         tk = timing_begin(h, TK_KRYLOV);
         LAUNCH_D(g, add_correction_k, mv_tile_grid(g), KTHREADS, g, mg->e32, xv);
-        true_residual(mg, g, L, zz, xv, dlinf, st);
+        true_residual(mg, g, L, zz, xv, dlinf, st, rr, mg->e32);
         timing_end(h, tk);
         const double res_old = res;
         res = read_linf(h, dlinf);
