@@ -59,13 +59,22 @@ cudaError_t k_average(double* a, const double* b, long long n, cudaStream_t s);
 // Float-float (FP32-pair) counterparts of the momentum chain (mom_ff.cu): uStar, the face fluxes and
 // the viscous fluxes are pairs (float2); ρu, u and the forcing r stay FP64 fields.
 cudaError_t k_ustar_ff(const MomConsts& k, const double* rhou, const double* f, float2* ustar, cudaStream_t s);
+// k_stage_start plus the first sweep's uStar (the values k_ustar_ff gives after k_stage_start)
+cudaError_t k_stage_start_ff(const MomConsts& k, const double* us, double* ud, const double* fs, double* fd, double* rhou,
+                             float2* ustar, cudaStream_t s);
+// uStar on the ghost cells only (some coordinate 0 or n-1), for a sweep whose interior cells k_momupdate_ff
+// wrote
+cudaError_t k_ustar_ff_planes(const MomConsts& k, const double* rhou, const double* f, float2* ustar,
+                              cudaStream_t s);
 // the bulk faces directly, every other cell through a list (list: N entries, count: one counter)
 cudaError_t k_momflux_ff(const MomConsts& k, int j, int limiter, const float2* ustar, const double* rhouf_j,
                          const double* fold, double dt, float2* Phi, unsigned int* list, unsigned int* count,
                          int list_blocks, cudaStream_t s);
-// dq: the dilation term ρ̄∂ⱼuⱼ/2 of every cell as pairs, written by the sweep's VOF bulk pass
+// dq: the dilation term ρ̄∂ⱼuⱼ/2 of every cell as pairs, written by the sweep's VOF bulk pass.  With
+// us_next, also the next sweep's uStar from the new ρu and fn on the interior cells (the same values
+// k_ustar_ff gives there)
 cudaError_t k_momupdate_ff(const MomConsts& k, int j, const float2* Phi, const float2* dq, const double* uOld, double dt,
-                           double* rhou, cudaStream_t s);
+                           double* rhou, const double* fn, float2* us_next, cudaStream_t s);
 cudaError_t k_visc_ff(const MomConsts& k, const double* u, const double* f, double lmu, double mu, float2* Phi6,
                       double* r, unsigned int* list, unsigned int* count, int list_blocks, cudaStream_t s);
 // z = div(u) (pair sums), x *= dt; MPCFL's maxima with pair sums

@@ -77,6 +77,25 @@ __device__ __forceinline__ ff mul_rho_ff(const MomConsts& k, const MomFF& q, ff 
 
 // ------------------------------------------------------------------ uStar = BC!(ρu / ρ(f))
 // (components unrolled: the boundary value of component i is then a fixed parameter offset)
+// a cell with a Dirichlet face or a ghost source for some component: the general rules
+template <int D>
+__device__ __forceinline__ void ustar_ff_edge(const MomConsts& k, const MomFF& q, const double* __restrict__ rhou,
+                                              const double* __restrict__ f, float2* __restrict__ us, int x, int y,
+                                              int z, long long O) {
+    const Grid& g = k.g;
+#pragma unroll
+    for (int i = 0; i < D; ++i) {
+        int c[3] = {x, y, z};
+        ff v;
+        if (vel_bc(g, i, c)) {
+            v = q.uBC[i];
+        } else {
+            const long long P = lin3(g, c);
+            v = div_rho_ff(k, q, ff_split(rhou[P + i * g.N]), f[P], f[P - g.s[i]]);
+        }
+        stff(us + O + i * g.N, v);
+    }
+}
 template <int D>
 __global__ void ustar_ff_kern(MomConsts k, MomFF q, const double* __restrict__ rhou, const double* __restrict__ f,
                               float2* __restrict__ us) {
@@ -96,6 +115,22 @@ __global__ void ustar_ff_kern(MomConsts k, MomFF q, const double* __restrict__ r
         for (int i = 0; i < D; ++i) stff(us + O + i * g.N, div_rho_ff(k, q, ff_split(r[i]), fO, fm[i]));
         return;
     }
+    ustar_ff_edge<D>(k, q, rhou, f, us, x, y, z, O);
+}
+
+// BC!(u) at an interior cell (every coordinate in [1, n-2]) keeps the cell's own value, except the normal
+// component on the low wall face of a non-periodic dimension (c[i] = 1), which is the Dirichlet constant
+__device__ __forceinline__ bool interior_dirichlet(const Grid& g, int i, const int c[3]) {
+    return !g.isper(i) && c[i] == 1;
+}
+
+// uStar at a ghost cell straight from u and f: ρu at the source P of a non-Dirichlet
+// component is mul_rho of u and f there, as u2ρu! forms it (P lies in [1, n-2] in every dimension)
+template <int D>
+__device__ __forceinline__ void ustar_ff_edge_u(const MomConsts& k, const MomFF& q, const double* __restrict__ u,
+                                             const double* __restrict__ f, float2* __restrict__ us, int x, int y,
+                                             int z, long long O) {
+    const Grid& g = k.g;
 #pragma unroll
     for (int i = 0; i < D; ++i) {
         int c[3] = {x, y, z};
@@ -104,10 +139,56 @@ __global__ void ustar_ff_kern(MomConsts k, MomFF q, const double* __restrict__ r
             v = q.uBC[i];
         } else {
             const long long P = lin3(g, c);
-            v = div_rho_ff(k, q, ff_split(rhou[P + i * g.N]), f[P], f[P - g.s[i]]);
+            const double fP = f[P], fm = f[P - g.s[i]];
+            v = div_rho_ff(k, q, ff_split(mul_rho(k, u[P + i * g.N], fP, fm)), fP, fm);
         }
         stff(us + O + i * g.N, v);
     }
+}
+
+// copyto!(u⁰,u); copyto!(f⁰,f); u2ρu!(ρu,u⁰,f⁰) in one pass (as stage_start_kern), plus the first sweep's
+// uStar = BC!(ρu / ρ(f⁰)) on every cell from the FP64 ρu: the values ustar_ff_kern gives after that pass
+template <int D>
+__global__ void stage_start_ff_kern(MomConsts k, MomFF q, const double* __restrict__ us, double* __restrict__ ud,
+                                    const double* __restrict__ fs, double* __restrict__ fd,
+                                    double* __restrict__ rhou, float2* __restrict__ ustar) {
+    const Grid& g = k.g;
+    GCELL_XYZ
+    const long long O = lin(g, x, y, z);
+    const double fO = fs[O];
+    fd[O] = fO;
+    double uv[D];
+#pragma unroll
+    for (int i = 0; i < D; ++i) {
+        uv[i] = us[O + i * g.N];
+        if (ud) ud[O + i * g.N] = uv[i];
+    }
+    if (x < 1 || x > g.n[0] - 2 || y < 1 || y > g.n[1] - 2 || (D == 3 && (z < 1 || z > g.n[2] - 2))) {
+        ustar_ff_edge_u<D>(k, q, us, fs, ustar, x, y, z, O);
+        return;
+    }
+    const int c[3] = {x, y, z};
+    double fm[D];
+#pragma unroll
+    for (int i = 0; i < D; ++i) fm[i] = fs[O - g.s[i]];
+#pragma unroll
+    for (int i = 0; i < D; ++i) {
+        const double r = mul_rho(k, uv[i], fO, fm[i]);
+        rhou[O + i * g.N] = r;
+        stff(ustar + O + i * g.N, interior_dirichlet(g, i, c) ? q.uBC[i] : div_rho_ff(k, q, ff_split(r), fO, fm[i]));
+    }
+}
+
+// uStar on the ghost cells (some c[e] in {0, n_e - 1}), for a sweep whose interior cells the previous
+// sweep's momentum update has written; one thread per cell of the planes bc_plane_cell numbers, the
+// interior ones return, and a cell on an edge or corner is written once per plane with the same value
+template <int D>
+__global__ void ustar_ff_planes(MomConsts k, MomFF q, const double* __restrict__ rhou, const double* __restrict__ f,
+                                float2* __restrict__ us) {
+    const Grid& g = k.g;
+    int c[3];
+    if (!bc_plane_cell(g, blockIdx.x * (long long)blockDim.x + threadIdx.x, c) || is_interior(g, c)) return;
+    ustar_ff_edge<D>(k, q, rhou, f, us, c[0], c[1], c[2], lin3(g, c));
 }
 
 // ------------------------------------------------------------------ limiters (src/flow.jl:5-15)
@@ -395,16 +476,22 @@ __global__ void __launch_bounds__(128) momflux_ff_list(FluxCtx F, FluxFF Q, cons
 // ------------------------------------------------------------------ ρu += δt (Φ(I) - Φ(I+δj) + uOld ϕ(i,I,ρ̄∂ⱼuⱼ))
 // dq = ρ̄∂ⱼuⱼ/2 of every cell (ghosts mapped), written by the sweep's VOF bulk pass, so that
 // ϕ(i, I, ρ̄∂ⱼuⱼ) = dq(I) + dq(I-δi); one interior cell per thread, every load issued first.
-template <int D>
-__global__ void __launch_bounds__(256) momupdate_ff_kern(Grid g, long long sj, const float2* __restrict__ Phi,
+// With NEXT, also the next sweep's uStar = BC!(ρu / ρ(f_next)) on every interior cell: from the FP64 ρu
+// just written, split as ustar_ff_kern splits what it reads, so the values are the same; ustar_ff_planes
+// then covers the ghost cells.
+template <int D, bool NEXT>
+__global__ void __launch_bounds__(256, 4) momupdate_ff_kern(MomConsts k, MomFF q, long long sj,
+                                                         const float2* __restrict__ Phi,
                                                          const float2* __restrict__ dq,
                                                          const double* __restrict__ uOld, ff dt,
-                                                         double* __restrict__ rhou) {
+                                                         double* __restrict__ rhou, const double* __restrict__ fn,
+                                                         float2* __restrict__ usn) {
+    const Grid& g = k.g;
     ICELL_XYZ
     const long long I = lin(g, x, y, z);
     const ff dI = ldff(dq + I);
     ff dm[D], p0[D], p1[D];
-    double uo[D], r0[D];
+    double uo[D], r0[D], fm[D], fI = 0.0;
 #pragma unroll
     for (int i = 0; i < D; ++i) {
         dm[i] = ldff(dq + I - g.s[i]);
@@ -413,10 +500,19 @@ __global__ void __launch_bounds__(256) momupdate_ff_kern(Grid g, long long sj, c
         uo[i] = uOld[I + i * g.N];
         r0[i] = rhou[I + i * g.N];
     }
+    if (NEXT) {
+        fI = fn[I];
+#pragma unroll
+        for (int i = 0; i < D; ++i) fm[i] = fn[I - g.s[i]];
+    }
+    const int c[3] = {x, y, z};
 #pragma unroll
     for (int i = 0; i < D; ++i) {
         const ff r = ff_add(ff_mul(ff_split(uo[i]), ff_add(dI, dm[i])), ff_sub(p0[i], p1[i]));
-        rhou[I + i * g.N] = ff_join(ff_add(ff_mul(dt, r), ff_split(r0[i])));
+        const double rn = ff_join(ff_add(ff_mul(dt, r), ff_split(r0[i])));
+        rhou[I + i * g.N] = rn;
+        if (NEXT)
+            stff(usn + I + i * g.N, interior_dirichlet(g, i, c) ? q.uBC[i] : div_rho_ff(k, q, ff_split(rn), fI, fm[i]));
     }
 }
 
@@ -774,11 +870,31 @@ cudaError_t k_momflux_ff(const MomConsts& k, int j, int limiter, const float2* u
 }
 
 cudaError_t k_momupdate_ff(const MomConsts& k, int j, const float2* Phi, const float2* dq, const double* uOld, double dt,
-                           double* rhou, cudaStream_t s) {
+                           double* rhou, const double* fn, float2* us_next, cudaStream_t s) {
     const ff dtf = ff_split(dt);
     const long long sj = k.g.s[j];
-    if (k.g.D == 3) { momupdate_ff_kern<3><<<igrd(k.g), blk(), 0, s>>>(k.g, sj, Phi, dq, uOld, dtf, rhou); ia::note_launch(); }
-    else { momupdate_ff_kern<2><<<igrd(k.g), blk(), 0, s>>>(k.g, sj, Phi, dq, uOld, dtf, rhou); ia::note_launch(); }
+    const MomFF q = mom_ff_consts(k);
+#define IA_MU(D, NX) momupdate_ff_kern<D, NX><<<igrd(k.g), blk(), 0, s>>>(k, q, sj, Phi, dq, uOld, dtf, rhou, fn, us_next)
+    if (k.g.D == 3) { if (us_next) IA_MU(3, true); else IA_MU(3, false); }
+    else { if (us_next) IA_MU(2, true); else IA_MU(2, false); }
+#undef IA_MU
+    ia::note_launch();
+    return cudaGetLastError();
+}
+
+cudaError_t k_stage_start_ff(const MomConsts& k, const double* us, double* ud, const double* fs, double* fd, double* rhou,
+                             float2* ustar, cudaStream_t s) {
+    if (k.g.D == 3) stage_start_ff_kern<3><<<ggrd(k.g), blk(), 0, s>>>(k, mom_ff_consts(k), us, ud, fs, fd, rhou, ustar);
+    else stage_start_ff_kern<2><<<ggrd(k.g), blk(), 0, s>>>(k, mom_ff_consts(k), us, ud, fs, fd, rhou, ustar);
+    ia::note_launch();
+    return cudaGetLastError();
+}
+
+cudaError_t k_ustar_ff_planes(const MomConsts& k, const double* rhou, const double* f, float2* ustar, cudaStream_t s) {
+    const unsigned nb = unsigned((bc_plane_cells(k.g) + 255) / 256);
+    if (k.g.D == 3) ustar_ff_planes<3><<<nb, 256, 0, s>>>(k, mom_ff_consts(k), rhou, f, ustar);
+    else ustar_ff_planes<2><<<nb, 256, 0, s>>>(k, mom_ff_consts(k), rhou, f, ustar);
+    ia::note_launch();
     return cudaGetLastError();
 }
 

@@ -102,8 +102,9 @@ void extra_destroy(ia_handle* h) {
 
 // advectfq! → advectVOFρuu! (src/flow.jl:157-232): per direction, uStar = BC!(ρu/ρ(f)),
 // the VOF sweep f → f' with its mass flux, the CMOM fluxes and ρu += δt r.
+// us_ready: k_stage_start_ff wrote the first sweep's uStar (float-float mode)
 static int advect_fq(ia_handle* h, double* f, const double* u1, const double* u2, const double* uOld, double dt,
-                     const int* dirs, int counter_base) {
+                     const int* dirs, int counter_base, bool us_ready) {
     const Grid& g = h->g;
     MomScratch* m = h->mom;
     const MomConsts k = consts(h);
@@ -121,7 +122,11 @@ static int advect_fq(ia_handle* h, double* f, const double* u1, const double* u2
         float2* us2 = reinterpret_cast<float2*>(m->ustar);
         float2* Phi2 = reinterpret_cast<float2*>(m->Phi);
         int tk = timing_begin(h, TK_MOM);
-        cudaError_t e = ff ? k_ustar_ff(k, h->fld.rhou, fin, us2, st) : k_ustar(k, h->fld.rhou, fin, m->ustar, st);
+        // after the first sweep the previous momentum update wrote uStar on the interior cells
+        cudaError_t e = cudaSuccess;
+        if (!ff) e = k_ustar(k, h->fld.rhou, fin, m->ustar, st);
+        else if (q > 0) e = k_ustar_ff_planes(k, h->fld.rhou, fin, us2, st);
+        else if (!us_ready) e = k_ustar_ff(k, h->fld.rhou, fin, us2, st);
         if (e != cudaSuccess) return IA_ERR_CUDA;
         timing_end(h, tk);
         float2* dq2 = ff ? reinterpret_cast<float2*>(m->dq) : nullptr;
@@ -136,7 +141,7 @@ static int advect_fq(ia_handle* h, double* f, const double* u1, const double* u2
         if (e != cudaSuccess) return IA_ERR_CUDA;
         timing_end(h, tk);
         tk = timing_begin(h, TK_MOM_UPDATE);
-        e = ff ? k_momupdate_ff(k, d, Phi2, dq2, uOld, dt, h->fld.rhou, st)
+        e = ff ? k_momupdate_ff(k, d, Phi2, dq2, uOld, dt, h->fld.rhou, fout, q + 1 < g.D ? us2 : nullptr, st)
                : k_momupdate(k, d, m->Phi, uOld, u1, u2, cbar, dt, h->fld.rhou, st);
         if (e != cudaSuccess) return IA_ERR_CUDA;
         timing_end(h, tk);
@@ -242,10 +247,14 @@ int ia_mom_step(ia_handle* h, double dt, int64_t n_dt, double t_now, ia_status* 
     // ---- predictor: u(n) → u(n+½) with u(n)
     int tk = timing_begin(h, TK_UPDATE);
     // copyto!(u⁰,u); copyto!(f⁰,f); u2ρu!(ρu,u⁰,f⁰) in one pass
-    if (k_stage_start(k, F.u, F.u0, F.f, F.f0, F.rhou, st) != cudaSuccess) return IA_ERR_CUDA;
+    const bool ff = use_ff(h);
+    float2* us2 = reinterpret_cast<float2*>(h->mom->ustar);
+    if ((ff ? k_stage_start_ff(k, F.u, F.u0, F.f, F.f0, F.rhou, us2, st)
+            : k_stage_start(k, F.u, F.u0, F.f, F.f0, F.rhou, st)) != cudaSuccess)
+        return IA_ERR_CUDA;
     timing_end(h, tk);
     int rc = status_reset(h);
-    if (rc == IA_OK) rc = advect_fq(h, F.f0, F.u0, F.u, F.u, dt, dirs, 0);
+    if (rc == IA_OK) rc = advect_fq(h, F.f0, F.u0, F.u, F.u, dt, dirs, 0, ff);
     if (rc != IA_OK) return rc;
     rc = status_collect(h, F.u0, F.u, &S, true);
     if (rc == IA_ERR_NAN || rc == IA_ERR_DIVERGENCE || rc == IA_ERR_CUDA) {
@@ -272,10 +281,12 @@ int ia_mom_step(ia_handle* h, double dt, int64_t n_dt, double t_now, ia_status* 
     // ---- corrector: u(n) → u(n+1) with u(n+½)
     tk = timing_begin(h, TK_UPDATE);
     // copyto!(f⁰,f); u2ρu!(ρu,u⁰,f) in one pass
-    if (k_stage_start(k, F.u0, nullptr, F.f, F.f0, F.rhou, st) != cudaSuccess) return IA_ERR_CUDA;
+    if ((ff ? k_stage_start_ff(k, F.u0, nullptr, F.f, F.f0, F.rhou, us2, st)
+            : k_stage_start(k, F.u0, nullptr, F.f, F.f0, F.rhou, st)) != cudaSuccess)
+        return IA_ERR_CUDA;
     timing_end(h, tk);
     rc = status_reset(h);
-    if (rc == IA_OK) rc = advect_fq(h, F.f, F.u, F.u, F.u0, dt, dirs, 8);
+    if (rc == IA_OK) rc = advect_fq(h, F.f, F.u, F.u, F.u0, dt, dirs, 8, ff);
     if (rc != IA_OK) return rc;
     rc = status_collect(h, F.u, F.u, &S, true);
     if (rc == IA_ERR_NAN || rc == IA_ERR_DIVERGENCE || rc == IA_ERR_CUDA) {
@@ -431,7 +442,7 @@ int ia_advect_momentum(ia_handle* h, double* f, const double* u1, const double* 
     int dirs[3];
     for (int i = 1; i <= h->g.D; ++i) dirs[i - 1] = int((n_dt + i) % h->g.D);
     int rc = status_reset(h);
-    if (rc == IA_OK) rc = advect_fq(h, f, u1, u2, uOld, dt, dirs, 0);
+    if (rc == IA_OK) rc = advect_fq(h, f, u1, u2, uOld, dt, dirs, 0, false);
     if (rc != IA_OK) return rc;
     return status_collect(h, u1, u2, status, false);
 }

@@ -196,15 +196,19 @@ def test_every_limiter_matches_oracle(cuda, limiter, arith):
     assert ef < 1e-10 and eu < 1e-10 and ep < 1e-6, (limiter, ef, eu, ep)
 
 
-@pytest.mark.parametrize("dims,per,eta", [((16, 12), (), 0.0), ((12, 10, 8), (0, 2), 0.05)])
-def test_float_float_momentum_agrees_with_fp64(cuda, dims, per, eta):
+@pytest.mark.parametrize("dims,per,eta,uBC", [((16, 12), (), 0.0, None), ((12, 10, 8), (0, 2), 0.05, None),
+                                              ((16, 12), (1,), 0.0, (0.05, 0.0)),
+                                              ((12, 10, 8), (2,), 0.0, (0.04, -0.03, 0.0))])
+def test_float_float_momentum_agrees_with_fp64(cuda, dims, per, eta, uBC):
     # the same step with the momentum kernels in FP32 pairs and in FP64 (both with the FP64 solver):
-    # the pair arithmetic carries ~2^-46 relative error per operation
+    # the pair arithmetic carries ~2^-46 relative error per operation.  A wall-normal uBC puts the
+    # Dirichlet value on the low wall face, which the fused uStar passes write
     D = len(dims)
+    uBC = uBC or (0.0,) * D
     c = tuple(0.5 * n + 0.7 for n in dims)
     sdf = lambda x: torch.sqrt(sum((x[d] - c[d]) ** 2 for d in range(D))) - 0.3 * dims[0]
     g = (0.0, -0.01) + ((0.0,) if D == 3 else ())
-    mk = lambda arith: ia.TwoPhaseSimulation(dims, (0.0,) * D, float(dims[0]), perdir=per, InterfaceSDF=sdf, λρ=1e-3,
+    mk = lambda arith: ia.TwoPhaseSimulation(dims, uBC, float(dims[0]), perdir=per, InterfaceSDF=sdf, λρ=1e-3,
                                              λμ=1e-2, ν=0.02, g=g, η=(eta or None), poisson="fp64", poisson_tol=PTOL,
                                              poisson_itmx=500, momentum_arith=arith)
     a, b = mk("fp64"), mk("ff")
