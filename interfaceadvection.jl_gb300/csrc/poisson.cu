@@ -183,29 +183,78 @@ __global__ void restrict_L_k(Grid gc, Grid gf, const T* __restrict__ Lf, T* __re
 // (same value and zero-diagonal rule as set_diag_k).
 // With PROL (over-relaxed first red half-sweep of a post-smoothing whose prolongation is fused
 // into the sweeps) the cell's previous value is x + the injected coarse correction.
+// In 3D a thread takes its pair in RB_ZT consecutive z planes and reads every plane's operands before
+// it stores: a half-sweep reads only the other colour, so no plane's store changes what another plane
+// reads, and the loads of all planes are in flight at once (the z neighbours of one plane are the x
+// neighbours of the next, a repeated address).  The values are those of one plane per thread.
+constexpr int RB_ZT = 2;
+inline dim3 pair_grid(const Grid& g) {
+    const int pairs = (g.n[0] - 2 + 1) / 2;
+    return dim3((pairs + 31) / 32, (g.n[1] - 2 + 7) / 8, g.D == 3 ? g.n[2] - 2 : 1);
+}
+inline dim3 pair_tile_grid(const Grid& g) {
+    const int pairs = (g.n[0] - 2 + 1) / 2;
+    return dim3((pairs + 31) / 32, (g.n[1] - 2 + 7) / 8, g.D == 3 ? (g.n[2] - 2 + RB_ZT - 1) / RB_ZT : 1);
+}
 template <class T, int D, bool PROL = false, class TL = T>
 __global__ void rbgs_pair_k(Grid g, int y0, int y1, const TL* __restrict__ L, const T* __restrict__ b,
                             T* __restrict__ xv, int color, T omega, Grid gc = Grid(),
                             const T* __restrict__ xc = nullptr) {
     const int y = y0 + int(blockIdx.y * blockDim.y + threadIdx.y);   // rows [y0, y1) of the interior
-    const int z = D == 3 ? 1 + int(blockIdx.z) : 0;
     if (y >= y1) return;
-    int x = 1 + 2 * (blockIdx.x * blockDim.x + threadIdx.x);
-    if (((x + y + z) & 1) != color) ++x;
-    if (x > g.n[0] - 2) return;
-    const int I = x + y * int(g.s[1]) + z * int(g.s[2]);
-    const Nb o = nb_of<D>(g, x, y, z);
-    const T off = off7<D>(g, L, xv, I, o);
-    const T dd = diag7<D>(g, L, I);
+    const int xp = 1 + 2 * (blockIdx.x * blockDim.x + threadIdx.x);
+    const int z0 = D == 3 ? 1 + RB_ZT * int(blockIdx.z) : 0;
     const T eps = sizeof(T) == 8 ? T(2.220446049250313e-16) : T(1.1920929e-7);
-    const T iD = (dd * dd < T(2) * eps) ? T(0) : T(1) / dd;
-    const T gs = (b[I] - off) * iD;
-    if (omega == T(1)) {
-        xv[I] = gs;
-    } else {   // over-relaxation: x + ω (x_GS - x)
-        T xo = xv[I];
-        if (PROL) xo += xc[lin(gc, (x + 1) / 2, (y + 1) / 2, D == 3 ? (z + 1) / 2 : 0)];
-        xv[I] = xo + omega * (gs - xo);
+    // plane k's cell of this colour and its operands: the off-diagonal sum, the diagonal, b and
+    // (over-relaxed) the previous value
+    auto cell_of = [&](int z) {
+        int x = xp;
+        if (((x + y + z) & 1) != color) ++x;
+        return x;
+    };
+    auto load = [&](int x, int z, int& I, T& off, T& dd, T& bv, T& xo) {
+        I = x + y * int(g.s[1]) + z * int(g.s[2]);
+        const Nb o = nb_of<D>(g, x, y, z);
+        off = off7<D>(g, L, xv, I, o);
+        dd = diag7<D>(g, L, I);
+        bv = b[I];
+        if (omega != T(1)) {
+            xo = xv[I];
+            if (PROL) xo += xc[lin(gc, (x + 1) / 2, (y + 1) / 2, D == 3 ? (z + 1) / 2 : 0)];
+        }
+    };
+    auto store = [&](int I, T off, T dd, T bv, T xo) {
+        const T iD = (dd * dd < T(2) * eps) ? T(0) : T(1) / dd;
+        const T gs = (bv - off) * iD;
+        if (omega == T(1)) xv[I] = gs;
+        else xv[I] = xo + omega * (gs - xo);   // over-relaxation: x + ω (x_GS - x)
+    };
+    const int xmax = g.n[0] - 2;
+    if (D == 3 && z0 + RB_ZT - 1 <= g.n[2] - 2) {
+        int I[RB_ZT];
+        T off[RB_ZT], dd[RB_ZT], bv[RB_ZT], xo[RB_ZT];
+        bool ok[RB_ZT];
+#pragma unroll
+        for (int k = 0; k < RB_ZT; ++k) {
+            const int x = cell_of(z0 + k);
+            ok[k] = x <= xmax;
+            xo[k] = T(0);
+            if (ok[k]) load(x, z0 + k, I[k], off[k], dd[k], bv[k], xo[k]);
+        }
+#pragma unroll
+        for (int k = 0; k < RB_ZT; ++k)
+            if (ok[k]) store(I[k], off[k], dd[k], bv[k], xo[k]);
+        return;
+    }
+    for (int k = 0; k < (D == 3 ? RB_ZT : 1); ++k) {
+        const int z = z0 + k;
+        if (D == 3 && z > g.n[2] - 2) break;
+        const int x = cell_of(z);
+        if (x > xmax) continue;
+        int I;
+        T off, dd, bv, xo = T(0);
+        load(x, z, I, off, dd, bv, xo);
+        store(I, off, dd, bv, xo);
     }
 }
 
@@ -483,10 +532,6 @@ __global__ void __launch_bounds__(TB_T, 4) rbgs_tb_k(TbArgs a) {
             __syncthreads();
         }
     }
-}
-inline dim3 pair_grid(const Grid& g) {
-    const int pairs = (g.n[0] - 2 + 1) / 2;
-    return dim3((pairs + 31) / 32, (g.n[1] - 2 + 7) / 8, g.D == 3 ? g.n[2] - 2 : 1);
 }
 
 
@@ -1304,7 +1349,7 @@ static cudaError_t vcycle(ia_handle* h, PoissonMG* mg, int l, cudaStream_t st, i
     };
     auto half = [&](int color, int y0, int y1) {
         const int tk = (l == 0) ? timing_begin(h, TK_MG_FINE) : -1;
-        const dim3 gr = rows(pair_grid(L.g), y0, y1);
+        const dim3 gr = rows(pair_tile_grid(L.g), y0, y1);
         if (L16) {
             if (L.g.D == 3) rbgs_pair_k<T, 3, false, __half><<<gr, blk(), 0, st>>>(L.g, y0, y1, L16, b, x, color, om);
             else rbgs_pair_k<T, 2, false, __half><<<gr, blk(), 0, st>>>(L.g, y0, y1, L16, b, x, color, om);
@@ -1319,7 +1364,7 @@ static cudaError_t vcycle(ia_handle* h, PoissonMG* mg, int l, cudaStream_t st, i
     // coarse correction, which it adds to the value it reads
     auto half_prol = [&](int y0, int y1) {
         const int tk = (l == 0) ? timing_begin(h, TK_MG_FINE) : -1;
-        const dim3 gr = rows(pair_grid(L.g), y0, y1);
+        const dim3 gr = rows(pair_tile_grid(L.g), y0, y1);
         const T* xc = C.template x_<T>();
         if (L16 && L.g.D == 3) rbgs_pair_k<T, 3, true, __half><<<gr, blk(), 0, st>>>(L.g, y0, y1, L16, b, x, 0, om, C.g, xc);
         else if (L16) rbgs_pair_k<T, 2, true, __half><<<gr, blk(), 0, st>>>(L.g, y0, y1, L16, b, x, 0, om, C.g, xc);
