@@ -51,11 +51,14 @@ TK = {"vof_bulk": 0, "vof_cells": 1, "ustar": 2, "forcing": 3, "mg_vcycle": 4, "
 ROOF = {
     "momflux": dict(bytes=64, traffic=None, kernel="momflux (CMOM face fluxes of one sweep: read uStar 3, "
                                                    "ρuf_j, f_old; write Φ 3)"),
-    "momupdate": dict(bytes=113, traffic=None, kernel="momupdate (ρu += δt(Φ(I)-Φ(I+δj)+uOld ϕ(ρ̄∂ⱼuⱼ)))"),
+    # the first two of a stage's three updates also write the next sweep's uStar (24 B) from the new
+    # fractions (8 B): 113, 145 and 145 B per cell, 134.3 on average per launch
+    "momupdate": dict(bytes=(113 + 2 * 145) / 3, traffic=None,
+                      kernel="momupdate (ρu += δt(Φ(I)-Φ(I+δj)+uOld ϕ(ρ̄∂ⱼuⱼ)); in sweeps 1-2 also uStar of the next sweep)"),
     # a finest-level half-sweep runs as one launch or, in the y-slab wavefront, as one launch per slab:
     # its unit is the whole-level half-sweep, 5 per V-cycle at nu = (2, 2) with over-relaxation (2 in the
     # pre-smoothing after the fused first one, 3 in the post-smoothing)
-    "mg_fine_rbgs": dict(bytes=18, traffic=15.4, per_vcycle=5,
+    "mg_fine_rbgs": dict(bytes=18, traffic=15.0, per_vcycle=5,
                          kernel="rbgs_pair_k<float> (finest-level red-black half-sweep)"),
 }
 
