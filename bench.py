@@ -400,24 +400,46 @@ def run_bubble(args, world, local_rank):
         hf = pinned(it.f).copy_(it.f)
         hp = pinned(fl.p)
         e_steps = args.steps
+        # flat views of the dense fields and their pinned copies (same strides), cut into chunks of ~100 MB
+        def flat(t):
+            dense = 1
+            for d in sorted(range(t.dim()), key=lambda d: t.stride(d)):
+                assert t.size(d) == 1 or t.stride(d) == dense, "e2e chunks need a dense field"
+                dense *= t.size(d)
+            return t.as_strided((t.numel(),), (1,), t.storage_offset())
+        def chunks(dv, hv, n=8):
+            dv, hv = flat(dv), flat(hv)
+            step = (dv.numel() + n - 1) // n
+            return [(dv[a:a + step], hv[a:a + step]) for a in range(0, dv.numel(), step)]
+        state = chunks(fl.u, hu) + chunks(it.f, hf)
         torch.cuda.synchronize()
         barrier()
         t0 = time.perf_counter()
-        # the link copies ~200 GB/s one way and ~340 GB/s both ways at once: the downloads of f and p
-        # run on a second stream, beside the next step's upload of u.  Every copy still follows what
-        # it depends on: u is uploaded after its download (same stream), f after its download and the
-        # next step's kernels after the download of p (the f upload waits for the second stream)
-        main, side = torch.cuda.current_stream(), torch.cuda.Stream()
-        for _ in range(e_steps):
+        # the link copies ~200 GB/s one way and ~340 GB/s both ways at once.  After a step, p and then u
+        # and f go down chunk by chunk on one stream; each chunk goes back up for the next step on a
+        # second stream as soon as its own download has landed, so the two directions overlap.  The next
+        # step's kernels wait for both streams (its input is uploaded and p, which it rewrites, is down).
+        main, down, up = torch.cuda.current_stream(), torch.cuda.Stream(), torch.cuda.Stream()
+        up.wait_stream(main)
+        with torch.cuda.stream(up):
             fl.u.copy_(hu, non_blocking=True)
-            main.wait_stream(side)
             it.f.copy_(hf, non_blocking=True)
+        for s in range(e_steps):
+            main.wait_stream(up)
+            main.wait_stream(down)
             ia.sim_step(sim)
-            hu.copy_(fl.u, non_blocking=True)
-            side.wait_stream(main)
-            with torch.cuda.stream(side):
-                hf.copy_(it.f, non_blocking=True)
+            down.wait_stream(main)
+            with torch.cuda.stream(down):
                 hp.copy_(fl.p, non_blocking=True)
+            for dv, hv in state:
+                with torch.cuda.stream(down):
+                    hv.copy_(dv, non_blocking=True)
+                    ev = torch.cuda.Event()
+                    ev.record(down)
+                if s + 1 < e_steps:
+                    up.wait_event(ev)
+                    with torch.cuda.stream(up):
+                        dv.copy_(hv, non_blocking=True)
         torch.cuda.synchronize()
         barrier()
         el = time.perf_counter() - t0
@@ -425,7 +447,8 @@ def run_bubble(args, world, local_rank):
         e2e = {"value": world * cells * e_steps / el / 1e6, "unit": METRIC, "h2d_bytes_per_step": nb,
                "d2h_bytes_per_step": nb + fl.p.numel() * 8 + C.sizeof(_lib.Status),
                "steps": e_steps,
-               "note": "state on the host: u, f uploaded and u, f, p downloaded every step around sim_step"}
+               "note": "state on the host: u, f uploaded and u, f, p downloaded every step around sim_step "
+                       "(in chunks, each chunk's upload after its own download, both directions at once)"}
     out["e2e"] = e2e
     del sim
     torch.cuda.empty_cache()
