@@ -362,7 +362,8 @@ int ia_poisson_mg_fine(ia_handle* h, int32_t nu1, int32_t nu2);
  * the red-black half-sweeps and the residual restriction of a smoothing run slab by slab over y, each
  * half-sweep one row behind the previous, so that the later half-sweeps read the slab from L2.  Same
  * results as whole-level half-sweeps, bit for bit.  0 = whole-level half-sweeps; otherwise at least 8.
- * Applies in 3D with walls in y; default from the device's L2 size (about 3/5 of it per slab). */
+ * Applies in 3D with walls in y.  Default 0: with two z planes per half-sweep thread the wavefront no
+ * longer shortens the step (a slab within about 3/5 of L2, 64 rows at 256x512x256, ties). */
 int ia_poisson_slab_rows(ia_handle* h, int32_t rows);
 /* counters since the handle's creation: [0] net applications, [1] V-cycles, [2] fallbacks
  * to the V-cycle, [3] inner FCG iterations, [4] outer corrections */

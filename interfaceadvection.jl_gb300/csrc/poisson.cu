@@ -1520,14 +1520,6 @@ bool coef16_fits(double lrho) {
 // 8 rows (measured at 256x512x256: 64 rows 45.7 ms per step, 32 rows 47.0, 16 rows 49.9, whole-level
 // half-sweeps 46.3: smaller slabs lose more to launches and partial blocks than they gain in L2 hits).
 // 0 (whole-level half-sweeps) where the wavefront does not apply.
-static int default_slab_rows(const Grid& g, bool mixed, bool c16, long long l2_bytes) {
-    if (!mixed || g.D != 3 || g.isper(1) || l2_bytes <= 0) return 0;
-    const long long row = (long long)(g.n[0] - 2) * (g.n[2] - 2) * (4 + 4 + 4 + (c16 ? 6 : 12));
-    const long long rows = ((l2_bytes * 3 / 5) / std::max(row, 1LL)) / 8 * 8;   // whole 8-row blocks at every lag
-    if (rows < 8 || rows >= g.n[1] - 2) return 0;
-    return int(rows);
-}
-
 int mg_create(ia_handle* h) {
     PoissonMG* mg = new PoissonMG();
     h->mg = mg;
@@ -1629,11 +1621,12 @@ int mg_create(ia_handle* h) {
     mg->nu2 = 2;
     mg->nuc = 16;
     {
-        int dev = 0, l2 = 0;
+        int dev = 0;
         cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&mg->nsm, cudaDevAttrMultiProcessorCount, dev);
-        cudaDeviceGetAttribute(&l2, cudaDevAttrL2CacheSize, dev);
-        mg->slab_rows = default_slab_rows(g0, mixed, mg->coef16 != 0, (long long)l2);
+        // whole-level half-sweeps by default: with two z planes per half-sweep thread the y-slab wavefront
+        // (ia_poisson_slab_rows) no longer shortens the step
+        mg->slab_rows = 0;
     }
     return IA_OK;
 }
